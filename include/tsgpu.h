@@ -1,0 +1,224 @@
+/*
+ * tsgpu.h — C ABI of the GB300-native texture-synthesis hot loop.
+ *
+ * The entry points mirror the reference's Rust API for the synthesis path
+ * (EmbarkStudios/texture-synthesis):
+ *
+ *   Session::builder() -> SessionBuilder setters -> build() -> Session::run()
+ *   -> GeneratedImage
+ *
+ * so that a Rust (or any FFI) front end can keep that API and forward every
+ * call here.  Images cross the boundary as already-decoded RGBA8 buffers
+ * (row-major, 4 bytes per pixel, no padding); decoding files stays with the
+ * caller.  The library copies every input buffer when it is passed, so the
+ * caller may free it immediately.  All computation runs on one CUDA device:
+ * there is no CPU fallback, and a missing or unusable device is reported as
+ * TS_ERR_CUDA.
+ *
+ * Errors: every fallible call returns a ts_status.  Builder and session
+ * objects keep a message for the last error (ts_builder_last_error,
+ * ts_session_last_error).  No exception crosses the ABI.
+ *
+ * Threading: objects are independent and may be used from different host
+ * threads, but one object must not be used by two threads at once.
+ * ts_session_run blocks the calling thread and invokes the progress
+ * callback on it.
+ */
+#ifndef TSGPU_H
+#define TSGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  TS_ERR_INVALID_RANGE, TS_ERR_SIZE_MISMATCH,
+ * TS_ERR_EXAMPLE_GUIDE_MISMATCH, TS_ERR_NO_EXAMPLES and
+ * TS_ERR_MAPS_COUNT_MISMATCH mirror texture_synthesis::Error
+ * (lib/src/errors.rs:37-57); TS_ERR_IMAGE stands for Error::Image (a buffer
+ * whose size does not match its dimensions). */
+typedef enum ts_status {
+  TS_OK = 0,
+  TS_ERR_INVALID_RANGE = 1,
+  TS_ERR_SIZE_MISMATCH = 2,
+  TS_ERR_EXAMPLE_GUIDE_MISMATCH = 3,
+  TS_ERR_NO_EXAMPLES = 4,
+  TS_ERR_MAPS_COUNT_MISMATCH = 5,
+  TS_ERR_IMAGE = 6,
+  /* A feature of the reference that this library does not provide
+   * (automatic guide maps for style transfer, lib.rs:575-582). */
+  TS_ERR_UNSUPPORTED = 7,
+  /* A sample mask with no usable texel: the reference loops forever
+   * (ms.rs:562-574); this library refuses it. */
+  TS_ERR_NO_VALID_SAMPLE = 8,
+  /* A map id beyond the non-ignored example list, where the reference
+   * panics on an out-of-bounds index. */
+  TS_ERR_INDEX = 9,
+  TS_ERR_CUDA = 10,
+  /* A call out of order: a consumed builder or session used again. */
+  TS_ERR_STATE = 11,
+  /* A parameter beyond this library's stated limits (ts_limits). */
+  TS_ERR_LIMIT = 12,
+  TS_ERR_OUT_OF_MEMORY = 13,
+  TS_ERR_NULL = 14
+} ts_status;
+
+/* SampleMethod (lib.rs:458-484). */
+typedef enum ts_sample_method {
+  TS_SAMPLE_ALL = 0,
+  TS_SAMPLE_IGNORE = 1,
+  TS_SAMPLE_IMAGE = 2
+} ts_sample_method;
+
+/* ChannelMask (utils.rs:46-53). */
+typedef enum ts_channel { TS_CHANNEL_R = 0, TS_CHANNEL_G = 1, TS_CHANNEL_B = 2, TS_CHANNEL_A = 3 } ts_channel;
+
+typedef struct ts_builder ts_builder;
+typedef struct ts_session ts_session;
+typedef struct ts_generated ts_generated;
+
+/* One example image with its optional guide and sample mask
+ * (Example / ExampleBuilder, lib.rs:486-623).  guide == NULL means no guide;
+ * mask is read when sample_method == TS_SAMPLE_IMAGE (its R channel != 0
+ * marks texels that may be sampled, ms.rs:1544-1547). */
+typedef struct ts_example_desc {
+  const uint8_t *rgba;
+  uint32_t width, height;
+  const uint8_t *guide_rgba;
+  uint32_t guide_width, guide_height;
+  int32_t sample_method; /* ts_sample_method */
+  const uint8_t *mask_rgba;
+  uint32_t mask_width, mask_height;
+} ts_example_desc;
+
+/* Stated limits of this implementation. */
+typedef struct ts_limits {
+  uint32_t max_nearest_neighbors;    /* k */
+  uint32_t max_random_sample_locations; /* m */
+  uint32_t max_examples;
+  uint32_t max_image_side;           /* example and output sides */
+} ts_limits;
+
+/* Progress, once per synthesis stage, on the thread that called run
+ * (GeneratorProgress / ProgressUpdate, session.rs:527-558).  image points at
+ * the current output RGBA8 (width*height*4) and stays valid only during the
+ * call. */
+typedef struct ts_progress {
+  const uint8_t *image;
+  uint32_t width, height;
+  uint64_t total_current, total_total;
+  uint64_t stage_current, stage_total;
+} ts_progress;
+typedef void (*ts_progress_fn)(const ts_progress *update, void *user);
+
+/* Run statistics of a generated image. */
+typedef struct ts_run_stats {
+  uint64_t resolves;      /* work items resolved in the stage loop */
+  uint64_t cost_evals;    /* candidate-cost evaluations (coherence + random candidates) */
+  uint64_t batches;       /* batch steps */
+  uint64_t stages;
+  uint64_t kernel_launches;
+  double gpu_ms;          /* device time of run (CUDA events) */
+  double wall_ms;         /* host wall time of run */
+} ts_run_stats;
+
+const char *ts_status_str(int status);
+void ts_get_limits(ts_limits *out);
+
+/* ---- SessionBuilder (session.rs:69-448) ---------------------------------- */
+
+/* Session::builder(): a builder with the reference defaults (lib.rs:342-359):
+ * k=50, m=50, cauchy 1.0, backtrack 0.5 x 5, output 500x500, alpha 0.8,
+ * seed 0, no tiling, no random init. */
+ts_builder *ts_builder_new(void);
+void ts_builder_free(ts_builder *b);
+const char *ts_builder_last_error(const ts_builder *b);
+
+/* SessionBuilder::add_example (session.rs:98-101) */
+int ts_builder_add_example(ts_builder *b, const ts_example_desc *ex);
+/* SessionBuilder::inpaint_example (session.rs:147-159): mask R<255 marks the
+ * pixels to synthesise; width x height is the output (and input) size. */
+int ts_builder_inpaint_example(ts_builder *b, const uint8_t *mask_rgba, uint32_t mask_width, uint32_t mask_height,
+                               const ts_example_desc *ex, uint32_t width, uint32_t height);
+/* SessionBuilder::inpaint_example_channel (session.rs:177-190) */
+int ts_builder_inpaint_example_channel(ts_builder *b, int32_t channel, const ts_example_desc *ex, uint32_t width,
+                                       uint32_t height);
+/* SessionBuilder::load_target_guide (session.rs:200-203) */
+int ts_builder_load_target_guide(ts_builder *b, const uint8_t *rgba, uint32_t width, uint32_t height);
+/* SessionBuilder::resize_input (session.rs:206-209) */
+int ts_builder_resize_input(ts_builder *b, uint32_t width, uint32_t height);
+/* SessionBuilder::seed (session.rs:216-219) */
+int ts_builder_seed(ts_builder *b, uint64_t seed);
+/* SessionBuilder::tiling_mode (session.rs:224-227) */
+int ts_builder_tiling_mode(ts_builder *b, int32_t tiling);
+/* SessionBuilder::nearest_neighbors (session.rs:234-237) */
+int ts_builder_nearest_neighbors(ts_builder *b, uint32_t count);
+/* SessionBuilder::random_sample_locations (session.rs:245-248) */
+int ts_builder_random_sample_locations(ts_builder *b, uint64_t count);
+/* SessionBuilder::random_init (session.rs:254-257) */
+int ts_builder_random_init(ts_builder *b, uint64_t count);
+/* SessionBuilder::cauchy_dispersion (session.rs:269-272) */
+int ts_builder_cauchy_dispersion(ts_builder *b, float value);
+/* SessionBuilder::guide_alpha (session.rs:284-287) */
+int ts_builder_guide_alpha(ts_builder *b, float value);
+/* SessionBuilder::backtrack_percent (session.rs:293-296) */
+int ts_builder_backtrack_percent(ts_builder *b, float value);
+/* SessionBuilder::backtrack_stages (session.rs:305-308) */
+int ts_builder_backtrack_stages(ts_builder *b, uint32_t stages);
+/* SessionBuilder::output_size (session.rs:313-316) */
+int ts_builder_output_size(ts_builder *b, uint32_t width, uint32_t height);
+/* SessionBuilder::max_thread_count (session.rs:329-332).  Validated as in the
+ * reference (0 is an error); the GPU schedule does not depend on it. */
+int ts_builder_max_thread_count(ts_builder *b, uint64_t count);
+
+/* GB300-specific knobs (no reference counterpart).  batch_divisor sets the
+ * batch-snapshot schedule: each batch step holds max(1, R / divisor) work
+ * items, R being the resolved count when the batch starts (default 8);
+ * 0 gives batches of one item, the reference's single-thread semantics.
+ * max_batch caps a batch (0 = no cap). */
+int ts_builder_batch_schedule(ts_builder *b, uint32_t batch_divisor, uint32_t max_batch);
+/* CUDA device ordinal (default 0). */
+int ts_builder_device(ts_builder *b, int32_t device);
+
+/* SessionBuilder::build (session.rs:336-448).  Consumes the builder on
+ * success and on failure (as the Rust method takes self); the builder must
+ * still be freed with ts_builder_free, which is then the only valid call
+ * besides ts_builder_last_error.  Validation mirrors
+ * check_parameters_validity / check_images_validity (session.rs:450-524);
+ * example pyramids are built on the device here. */
+int ts_builder_build(ts_builder *b, ts_session **out);
+
+/* ---- Session (session.rs:22-66) ------------------------------------------ */
+
+/* Session::run: random init (if set), then the coarse-to-fine stage loop.
+ * Consumes the session: afterwards only ts_session_free and
+ * ts_session_last_error are valid.  progress may be NULL. */
+int ts_session_run(ts_session *s, ts_progress_fn progress, void *user, ts_generated **out);
+void ts_session_free(ts_session *s);
+const char *ts_session_last_error(const ts_session *s);
+
+/* ---- GeneratedImage (lib.rs:378-455) ------------------------------------- */
+
+void ts_generated_dims(const ts_generated *g, uint32_t *width, uint32_t *height);
+/* The output image, width*height*4 bytes (GeneratedImage::into_image). */
+int ts_generated_image(const ts_generated *g, uint8_t *out_rgba);
+/* Source coordinate of every output pixel: width*height*3 u32 (x, y, map),
+ * the buffer behind get_coordinate_transform (ms.rs:655-684). */
+int ts_generated_coord_map(const ts_generated *g, uint32_t *out_xym);
+/* Patch id and map id of every output pixel: width*height*2 u32
+ * (ms.rs:605-636). */
+int ts_generated_id_map(const ts_generated *g, uint32_t *out_pm);
+/* Length of the resolved list, and the list itself (flat pixel index) with
+ * the score recorded when each entry was first resolved (ms.rs:639-653). */
+uint64_t ts_generated_resolved_count(const ts_generated *g);
+int ts_generated_resolved(const ts_generated *g, uint32_t *out_flat, float *out_score);
+void ts_generated_stats(const ts_generated *g, ts_run_stats *out);
+void ts_generated_free(ts_generated *g);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TSGPU_H */

@@ -1,0 +1,450 @@
+"""GB300-native texture synthesis: Python mirror of the reference's session API.
+
+The reference (EmbarkStudios/texture-synthesis, Rust) is used as
+
+    let session = Session::builder()
+        .add_example(&"imgs/1.jpg")
+        .seed(10)
+        .build()?;
+    let generated = session.run(None);
+
+and this package keeps that shape over the C ABI in include/tsgpu.h:
+
+    import importlib
+    ts = importlib.import_module("texture-synthesis_gb300")
+    session = ts.Session.builder().add_example(rgba).seed(10).build()
+    generated = session.run()
+    image = generated.into_image()          # H x W x 4 uint8
+
+Images are numpy RGBA8 arrays (H x W x 4); decoding files is the caller's
+job.  Every call runs on one CUDA device through libtsgpu.so; there is no
+CPU fallback, and the package refuses to load when the library is missing.
+"""
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libtsgpu.so")
+_lib = None
+
+# ts_status (tsgpu.h); the first five mirror texture_synthesis::Error
+STATUS = {
+    0: "Ok", 1: "InvalidRange", 2: "SizeMismatch", 3: "ExampleGuideMismatch", 4: "NoExamples",
+    5: "MapsCountMismatch", 6: "Image", 7: "Unsupported", 8: "NoValidSample", 9: "Index", 10: "Cuda",
+    11: "State", 12: "Limit", 13: "OutOfMemory", 14: "Null",
+}
+
+
+class Error(Exception):
+    """texture_synthesis::Error (lib/src/errors.rs:37-57) plus this library's
+    own statuses; `kind` names the variant, `status` is the C status code."""
+
+    def __init__(self, status, message):
+        self.status = status
+        self.kind = STATUS.get(status, "Unknown")
+        super().__init__("%s: %s" % (self.kind, message))
+
+
+class _ExampleDesc(C.Structure):
+    _fields_ = [
+        ("rgba", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),
+        ("guide_rgba", C.c_void_p), ("guide_width", C.c_uint32), ("guide_height", C.c_uint32),
+        ("sample_method", C.c_int32),
+        ("mask_rgba", C.c_void_p), ("mask_width", C.c_uint32), ("mask_height", C.c_uint32),
+    ]
+
+
+class _Limits(C.Structure):
+    _fields_ = [("max_nearest_neighbors", C.c_uint32), ("max_random_sample_locations", C.c_uint32),
+                ("max_examples", C.c_uint32), ("max_image_side", C.c_uint32)]
+
+
+class _Progress(C.Structure):
+    _fields_ = [("image", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("total_current", C.c_uint64), ("total_total", C.c_uint64),
+                ("stage_current", C.c_uint64), ("stage_total", C.c_uint64)]
+
+
+class RunStats(C.Structure):
+    _fields_ = [("resolves", C.c_uint64), ("cost_evals", C.c_uint64), ("batches", C.c_uint64),
+                ("stages", C.c_uint64), ("kernel_launches", C.c_uint64), ("gpu_ms", C.c_double),
+                ("wall_ms", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_PROGRESS_FN = C.CFUNCTYPE(None, C.POINTER(_Progress), C.c_void_p)
+
+# every function tsgpu.h declares: name -> (restype, argtypes)
+SIGNATURES = {
+    "ts_status_str": (C.c_char_p, [C.c_int]),
+    "ts_get_limits": (None, [C.POINTER(_Limits)]),
+    "ts_builder_new": (C.c_void_p, []),
+    "ts_builder_free": (None, [C.c_void_p]),
+    "ts_builder_last_error": (C.c_char_p, [C.c_void_p]),
+    "ts_builder_add_example": (C.c_int, [C.c_void_p, C.POINTER(_ExampleDesc)]),
+    "ts_builder_inpaint_example": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                             C.POINTER(_ExampleDesc), C.c_uint32, C.c_uint32]),
+    "ts_builder_inpaint_example_channel": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(_ExampleDesc),
+                                                     C.c_uint32, C.c_uint32]),
+    "ts_builder_load_target_guide": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32]),
+    "ts_builder_resize_input": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
+    "ts_builder_seed": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "ts_builder_tiling_mode": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ts_builder_nearest_neighbors": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "ts_builder_random_sample_locations": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "ts_builder_random_init": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "ts_builder_cauchy_dispersion": (C.c_int, [C.c_void_p, C.c_float]),
+    "ts_builder_guide_alpha": (C.c_int, [C.c_void_p, C.c_float]),
+    "ts_builder_backtrack_percent": (C.c_int, [C.c_void_p, C.c_float]),
+    "ts_builder_backtrack_stages": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "ts_builder_output_size": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
+    "ts_builder_max_thread_count": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "ts_builder_batch_schedule": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
+    "ts_builder_device": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ts_builder_build": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "ts_session_run": (C.c_int, [C.c_void_p, _PROGRESS_FN, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "ts_session_free": (None, [C.c_void_p]),
+    "ts_session_last_error": (C.c_char_p, [C.c_void_p]),
+    "ts_generated_dims": (None, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "ts_generated_image": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ts_generated_coord_map": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ts_generated_id_map": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ts_generated_resolved_count": (C.c_uint64, [C.c_void_p]),
+    "ts_generated_resolved": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ts_generated_stats": (None, [C.c_void_p, C.POINTER(RunStats)]),
+    "ts_generated_free": (None, [C.c_void_p]),
+}
+
+
+def library_path():
+    return _LIB_PATH
+
+
+def lib():
+    """The loaded libtsgpu.so.  Raises if it has not been built: there is no
+    other implementation to fall back to."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            raise RuntimeError("libtsgpu.so is not built (%s); run __graft_entry__.build() or "
+                               "python texture-synthesis_gb300/build.py" % _LIB_PATH)
+        L = C.CDLL(_LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def limits():
+    out = _Limits()
+    lib().ts_get_limits(C.byref(out))
+    return {f: getattr(out, f) for f, _ in out._fields_}
+
+
+@dataclass(frozen=True)
+class Dims:
+    """Dims (lib.rs:141-158)."""
+    width: int
+    height: int
+
+    @staticmethod
+    def square(size):
+        return Dims(size, size)
+
+
+class ChannelMask:
+    """ChannelMask (utils.rs:46-53)."""
+    R, G, B, A = 0, 1, 2, 3
+
+
+class SampleMethod:
+    """SampleMethod (lib.rs:458-484): ALL, IGNORE, or Image(mask)."""
+    ALL = "all"
+    IGNORE = "ignore"
+
+    class Image:
+        def __init__(self, mask):
+            self.mask = _rgba(mask)
+
+
+def _rgba(a):
+    a = np.ascontiguousarray(a, dtype=np.uint8)
+    if a.ndim != 3 or a.shape[2] != 4:
+        raise ValueError("images are H x W x 4 RGBA8 arrays")
+    return a
+
+
+class Example:
+    """Example / ExampleBuilder (lib.rs:486-623)."""
+
+    def __init__(self, image):
+        self.image = _rgba(image)
+        self.guide = None
+        self.sample_method = SampleMethod.ALL
+
+    @staticmethod
+    def builder(image):
+        return Example(image)
+
+    def with_guide(self, guide):
+        self.guide = _rgba(guide)
+        return self
+
+    def set_sample_method(self, method):
+        if isinstance(method, np.ndarray):
+            method = SampleMethod.Image(method)
+        self.sample_method = method
+        return self
+
+    def _desc(self, keep):
+        d = _ExampleDesc()
+        keep.append(self.image)
+        d.rgba = self.image.ctypes.data
+        d.height, d.width = self.image.shape[:2]
+        if self.guide is not None:
+            keep.append(self.guide)
+            d.guide_rgba = self.guide.ctypes.data
+            d.guide_height, d.guide_width = self.guide.shape[:2]
+        sm = self.sample_method
+        if isinstance(sm, SampleMethod.Image):
+            d.sample_method = 2
+            keep.append(sm.mask)
+            d.mask_rgba = sm.mask.ctypes.data
+            d.mask_height, d.mask_width = sm.mask.shape[:2]
+        elif sm == SampleMethod.IGNORE:
+            d.sample_method = 1
+        else:
+            d.sample_method = 0
+        return d
+
+
+def _as_example(e):
+    return e if isinstance(e, Example) else Example(e)
+
+
+class SessionBuilder:
+    """SessionBuilder (session.rs:69-448).  Setters return self."""
+
+    def __init__(self):
+        self._h = lib().ts_builder_new()
+        if not self._h:
+            raise MemoryError("ts_builder_new")
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.ts_builder_free(self._h)
+            self._h = None
+
+    def _check(self, rc):
+        if rc:
+            msg = lib().ts_builder_last_error(self._h)
+            raise Error(rc, msg.decode() if msg else "")
+        return self
+
+    def add_example(self, example):
+        keep = []
+        d = _as_example(example)._desc(keep)
+        return self._check(lib().ts_builder_add_example(self._h, C.byref(d)))
+
+    def add_examples(self, examples):
+        for e in examples:
+            self.add_example(e)
+        return self
+
+    def inpaint_example(self, inpaint_mask, example, size):
+        keep = []
+        m = _rgba(inpaint_mask)
+        d = _as_example(example)._desc(keep)
+        return self._check(lib().ts_builder_inpaint_example(self._h, m.ctypes.data, m.shape[1], m.shape[0],
+                                                            C.byref(d), size.width, size.height))
+
+    def inpaint_example_channel(self, mask, example, size):
+        keep = []
+        d = _as_example(example)._desc(keep)
+        return self._check(lib().ts_builder_inpaint_example_channel(self._h, int(mask), C.byref(d),
+                                                                    size.width, size.height))
+
+    def load_target_guide(self, guide):
+        g = _rgba(guide)
+        return self._check(lib().ts_builder_load_target_guide(self._h, g.ctypes.data, g.shape[1], g.shape[0]))
+
+    def resize_input(self, dims):
+        return self._check(lib().ts_builder_resize_input(self._h, dims.width, dims.height))
+
+    def seed(self, value):
+        return self._check(lib().ts_builder_seed(self._h, int(value)))
+
+    def tiling_mode(self, is_tiling):
+        return self._check(lib().ts_builder_tiling_mode(self._h, 1 if is_tiling else 0))
+
+    def nearest_neighbors(self, count):
+        return self._check(lib().ts_builder_nearest_neighbors(self._h, int(count)))
+
+    def random_sample_locations(self, count):
+        return self._check(lib().ts_builder_random_sample_locations(self._h, int(count)))
+
+    def random_init(self, count):
+        return self._check(lib().ts_builder_random_init(self._h, int(count)))
+
+    def cauchy_dispersion(self, value):
+        return self._check(lib().ts_builder_cauchy_dispersion(self._h, float(value)))
+
+    def guide_alpha(self, value):
+        return self._check(lib().ts_builder_guide_alpha(self._h, float(value)))
+
+    def backtrack_percent(self, value):
+        return self._check(lib().ts_builder_backtrack_percent(self._h, float(value)))
+
+    def backtrack_stages(self, stages):
+        return self._check(lib().ts_builder_backtrack_stages(self._h, int(stages)))
+
+    def output_size(self, dims):
+        return self._check(lib().ts_builder_output_size(self._h, dims.width, dims.height))
+
+    def max_thread_count(self, count):
+        return self._check(lib().ts_builder_max_thread_count(self._h, int(count)))
+
+    def batch_schedule(self, divisor, max_batch=0):
+        """Batch-snapshot schedule: max(1, R // divisor) items per batch step
+        (R = resolved count at the step), capped at max_batch; divisor 0 means
+        one item per step (the reference's single-thread semantics)."""
+        return self._check(lib().ts_builder_batch_schedule(self._h, int(divisor), int(max_batch)))
+
+    def device(self, ordinal):
+        return self._check(lib().ts_builder_device(self._h, int(ordinal)))
+
+    def build(self):
+        out = C.c_void_p()
+        rc = lib().ts_builder_build(self._h, C.byref(out))
+        self._check(rc)
+        return Session(out.value)
+
+
+class Session:
+    """Session (session.rs:22-66)."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @staticmethod
+    def builder():
+        return SessionBuilder()
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.ts_session_free(self._h)
+            self._h = None
+
+    def run(self, progress=None):
+        """Session::run: consumes the session.  progress(dict) is called once
+        per stage with the current image and counters."""
+        def _cb(p, _user):
+            u = p.contents
+            img = np.ctypeslib.as_array(C.cast(u.image, C.POINTER(C.c_uint8)),
+                                        shape=(u.height, u.width, 4)).copy()
+            progress({"image": img, "total": (u.total_current, u.total_total),
+                      "stage": (u.stage_current, u.stage_total)})
+
+        cb = _PROGRESS_FN(_cb) if progress else _PROGRESS_FN()
+        out = C.c_void_p()
+        rc = lib().ts_session_run(self._h, cb, None, C.byref(out))
+        if rc:
+            msg = lib().ts_session_last_error(self._h)
+            raise Error(rc, msg.decode() if msg else "")
+        return GeneratedImage(out.value)
+
+
+class GeneratedImage:
+    """GeneratedImage (lib.rs:378-455) with the generator's maps."""
+
+    def __init__(self, handle):
+        self._h = handle
+        w, h = C.c_uint32(), C.c_uint32()
+        lib().ts_generated_dims(self._h, C.byref(w), C.byref(h))
+        self.width, self.height = w.value, h.value
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.ts_generated_free(self._h)
+            self._h = None
+
+    def into_image(self):
+        out = np.empty((self.height, self.width, 4), np.uint8)
+        lib().ts_generated_image(self._h, out.ctypes.data)
+        return out
+
+    def coord_map(self):
+        """(x, y, map) source coordinate of every pixel (the coordinate
+        transform's buffer, ms.rs:655-684)."""
+        out = np.empty((self.height, self.width, 3), np.uint32)
+        lib().ts_generated_coord_map(self._h, out.ctypes.data)
+        return out
+
+    def id_map(self):
+        """(patch id, map id) of every pixel (ms.rs:605-636)."""
+        out = np.empty((self.height, self.width, 2), np.uint32)
+        lib().ts_generated_id_map(self._h, out.ctypes.data)
+        return out
+
+    def resolved(self):
+        """The resolved list (flat pixel index) and first-resolve scores."""
+        n = lib().ts_generated_resolved_count(self._h)
+        flat = np.empty(n, np.uint32)
+        score = np.empty(n, np.float32)
+        lib().ts_generated_resolved(self._h, flat.ctypes.data, score.ctypes.data)
+        return flat, score
+
+    def stats(self):
+        st = RunStats()
+        lib().ts_generated_stats(self._h, C.byref(st))
+        return st.as_dict()
+
+
+def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0):
+    """A SessionBuilder for a workload spec dict (see workloads.py)."""
+    p = spec["params"]
+    b = Session.builder()
+    exs = spec["examples"]
+    ip = spec.get("inpaint_mask")
+    idx = spec.get("inpaint_index", -1)
+    for i, e in enumerate(exs):
+        ex = Example(e["image"])
+        if e.get("guide") is not None:
+            ex.with_guide(e["guide"])
+        s = e.get("sample", "all")
+        if s == "ignore":
+            ex.set_sample_method(SampleMethod.IGNORE)
+        elif s == "image":
+            ex.set_sample_method(SampleMethod.Image(e["mask"]))
+        if ip is not None and i == idx:
+            b.inpaint_example(ip, ex, Dims(spec["out_w"], spec["out_h"]))
+        else:
+            b.add_example(ex)
+    if spec.get("target_guide") is not None:
+        b.load_target_guide(spec["target_guide"])
+    b.output_size(Dims(spec["out_w"], spec["out_h"]))
+    b.nearest_neighbors(p["nearest_neighbors"]).random_sample_locations(p["random_sample_locations"])
+    b.cauchy_dispersion(p["cauchy_dispersion"]).backtrack_percent(p["backtrack_percent"])
+    b.backtrack_stages(p["backtrack_stages"]).seed(p["seed"]).guide_alpha(p["guide_alpha"])
+    b.tiling_mode(p["tiling_mode"])
+    if p.get("random_init") is not None:
+        b.random_init(p["random_init"])
+    b.batch_schedule(batch_divisor, max_batch).device(device)
+    return b
+
+
+def run_spec(spec, batch_divisor=8, max_batch=0, device=0):
+    """Build and run a workload spec; returns a dict shaped like the oracle's."""
+    g = builder_from_spec(spec, batch_divisor, max_batch, device).build().run()
+    flat, score = g.resolved()
+    st = g.stats()
+    return {"image": g.into_image(), "coord": g.coord_map(), "id": g.id_map(), "resolved": flat,
+            "scores": score, "evals": st["cost_evals"], "resolves": st["resolves"], "batches": st["batches"],
+            "stats": st}

@@ -1,0 +1,813 @@
+// ts_kernels.cu — sm_103a kernels of the texture-synthesis hot loop.
+//
+// One batch step of a synthesis stage is four launches:
+//   knn_walk        warp per work item: the k nearest resolved points under
+//                   the (d2, y, x) order, by walking a table of lattice offsets
+//                   sorted in that order and testing a resolved-point bitmap
+//                   (replaces TreeGrid::get_k_nearest_neighbors, ms.rs:1363-1530)
+//   knn_exhaustive  CTA per item the walk could not finish (sparse regions):
+//                   radix-select over the resolved list
+//   resolve         warp per item: distance weights (ms.rs:405-425,
+//                   1198-1203), coherence + random candidates (ms.rs:478-602),
+//                   own pattern (ms.rs:1151-1181), candidate cost and first-min
+//                   argmin (ms.rs:1184-1288), lanes over candidates
+//   commit          thread per item: update + flush_resolved (ms.rs:296-377)
+// Every item of a batch reads the state as it was when the batch started;
+// commit runs after all of them.  Per stage, random_candidates precomputes the
+// m random candidates of every item (they depend only on the seed), and
+// level_switch recolours the resolved pixels (ms.rs:687-700).
+//
+// Floating point follows the reference operation by operation: f32 sums are
+// sequential, multiplies and adds are never fused (the file is compiled with
+// --fmad=false and uses __fadd_rn/__fmul_rn where it matters), and the f64
+// distances use an explicit fused multiply-add exactly where ms.rs:415 calls
+// mul_add.
+#include <float.h>
+#include <stdint.h>
+
+#include "ts_common.h"
+#include "ts_kernels.cuh"
+
+namespace ts {
+
+namespace {
+
+constexpr int kWarp = 32;
+constexpr int kResolveWarps = 4;
+constexpr int kWalkWarps = 8;
+constexpr int kExhThreads = 256;
+constexpr int kExhCap = 2048;  // keys kept by the exhaustive k-NN at the cut distance
+constexpr uint32_t kMaxDraws = 1u << 22;
+
+__device__ __forceinline__ void set_err(int *err, int code) {
+  if (*err == 0) atomicCAS(err, 0, code);
+}
+
+__device__ __forceinline__ int off_dx(int32_t off) { return (int)(int16_t)(off & 0xffff); }
+__device__ __forceinline__ int off_dy(int32_t off) { return off >> 16; }
+__device__ __forceinline__ int32_t pack_off(int dx, int dy) { return (int32_t)((uint32_t)(dx & 0xffff) | ((uint32_t)dy << 16)); }
+
+__device__ __forceinline__ int modi(int a, int b) {
+  int r = a % b;
+  return r < 0 ? r + b : r;
+}
+
+// Tree membership of an output-plane point, tiling mirrors included
+// (flush_resolved, ms.rs:296-331).
+__device__ __forceinline__ bool occupied(const SessionDev &s, int x, int y) {
+  const bool inx = (unsigned)x < s.W, iny = (unsigned)y < s.H;
+  if (inx && iny) return (__ldg(&s.occ[(size_t)y * s.wpr + (x >> 5)]) >> (x & 31)) & 1u;
+  if (!s.tiling || (!inx && !iny)) return false;
+  int xs = x, ys = y;
+  if (!inx) {
+    if (x >= (int)s.W) {
+      xs = x - (int)s.W;
+      if (xs >= s.x_l) return false;
+    } else {
+      xs = x + (int)s.W;
+      if (xs < 0 || xs <= s.x_r) return false;
+    }
+  } else {
+    if (y >= (int)s.H) {
+      ys = y - (int)s.H;
+      if (ys >= s.y_b) return false;
+    } else {
+      ys = y + (int)s.H;
+      if (ys < 0 || ys <= s.y_t) return false;
+    }
+  }
+  return (__ldg(&s.mir[(size_t)ys * s.wpr + (xs >> 5)]) >> (xs & 31)) & 1u;
+}
+
+__device__ __forceinline__ bool mir_bit(const SessionDev &s, uint32_t x, uint32_t y) {
+  return (s.mir[(size_t)y * s.wpr + (x >> 5)] >> (x & 31)) & 1u;
+}
+
+// check_coord_validity (ms.rs:1534-1549)
+__device__ __forceinline__ bool coord_valid(const SessionDev &s, const MapDesc &md, int x, int y) {
+  if (x < 0 || y < 0 || x >= (int)md.w || y >= (int)md.h) return false;
+  if (md.mask_off < 0) return true;
+  return __ldg(&s.masks[md.mask_off + (size_t)y * md.w + x]) != 0;
+}
+
+// ---------------------------------------------------------------------------
+// Random candidates of every item of a stage (ms.rs:549-599): the stream is
+// Pcg32::seed_from_u64(stage_seed + item + 1); per candidate a map
+// (usize range), then (x, y) redrawn until valid.
+// ---------------------------------------------------------------------------
+__global__ void k_random_candidates(SessionDev s, StageDev st) {
+  const uint32_t item = blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= st.n_items) return;
+  Pcg32 g = pcg_from_u64(st.stage_seed + (uint64_t)item + 1ULL);
+  uint2 *out = st.rcand + (size_t)item * s.m;
+  for (uint32_t t = 0; t < s.m; ++t) {
+    uint64_t map64 = 0;
+    if (!gen_range_u64_bounded(g, s.n_maps, 256, map64)) {
+      set_err(s.err, kDevErrNoSample);
+      for (; t < s.m; ++t) out[t] = make_uint2(0u, 0u);  // keep every entry a valid texel
+      return;
+    }
+    const uint32_t map = (uint32_t)map64;
+    const MapDesc md = s.maps[map];
+    uint32_t x = 0, y = 0;
+    bool ok = false;
+    for (uint32_t tries = 0; tries < kMaxDraws; ++tries) {
+      if (!gen_range_u32_bounded(g, md.w, 256, x) || !gen_range_u32_bounded(g, md.h, 256, y)) break;
+      if (coord_valid(s, md, (int)x, (int)y)) {
+        ok = true;
+        break;
+      }
+    }
+    if (!ok) {
+      set_err(s.err, kDevErrNoSample);
+      for (; t < s.m; ++t) out[t] = make_uint2(0u, 0u);  // keep every entry a valid texel
+      return;
+    }
+    out[t] = make_uint2(x | (y << 16), map);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k-NN by walking the sorted offset table.  The table holds every lattice
+// offset with d2 <= its radius^2, in (d2, dy, dx) order, so the first k
+// occupied entries are exactly the k nearest points under the tie rule.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kWalkWarps *kWarp) k_knn_walk(SessionDev s, StageDev st, BatchDev b) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t nb = b.i1 - b.i0;
+  for (uint32_t local = blockIdx.x * kWalkWarps + (threadIdx.x >> 5); local < nb;
+       local += gridDim.x * kWalkWarps) {
+    const uint32_t pixel = st.items[b.i0 + local];
+    const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
+    int32_t *nbo = b.nbuf + (size_t)local * s.k;
+    uint32_t count = 0;
+    for (uint32_t c = 0; c < s.knn_tab_n; c += kWarp) {
+      const uint32_t idx = c + lane;
+      bool hit = false;
+      int32_t off = 0;
+      if (idx < s.knn_tab_n) {
+        off = __ldg(&s.knn_tab[idx]);
+        hit = occupied(s, px + off_dx(off), py + off_dy(off));
+      }
+      const uint32_t bal = __ballot_sync(0xffffffffu, hit);
+      const uint32_t rank = count + __popc(bal & lt);
+      if (hit && rank < s.k) nbo[rank] = off;
+      count += __popc(bal);
+      if (count >= s.k) break;
+    }
+    if (lane == 0) {
+      if (count >= s.k) {
+        b.ncnt[local] = s.k;
+      } else {
+        const uint32_t slot = atomicAdd(b.fb_count, 1u);
+        b.fb_list[slot] = local;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Exhaustive k-NN (one CTA per item): radix-select the k-th smallest d2 over
+// every resolved point and its mirrors, keep the points at or below it, sort
+// them by (d2, y, x) and emit the first k.
+// ---------------------------------------------------------------------------
+struct ExhShared {
+  uint32_t hist[256];
+  unsigned long long keys[kExhCap];
+  uint32_t nkeys;
+  uint32_t total;
+  uint32_t prefix;
+  uint32_t rank;
+  int overflow;
+};
+
+template <typename F>
+__device__ __forceinline__ void for_points(const SessionDev &s, uint32_t n_res, F &&f) {
+  for (uint32_t e = threadIdx.x; e < n_res; e += blockDim.x) {
+    const uint32_t p = s.resolved[e];
+    const int x = (int)(p % s.W), y = (int)(p / s.W);
+    f(x, y);
+    if (s.tiling && mir_bit(s, (uint32_t)x, (uint32_t)y)) {
+      if (x < s.x_l)
+        f(x + (int)s.W, y);
+      else if (x > s.x_r)
+        f(x - (int)s.W, y);
+      if (y < s.y_b)
+        f(x, y + (int)s.H);
+      else if (y > s.y_t)
+        f(x, y - (int)s.H);
+    }
+  }
+}
+
+__device__ __forceinline__ unsigned long long nb_key(uint32_t d2, int x, int y) {
+  return ((unsigned long long)d2 << 32) | ((uint32_t)(y + 32768) << 16) | (uint32_t)(x + 32768);
+}
+
+__device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
+                                    ExhShared &sh);
+
+__global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive(SessionDev s, StageDev st, BatchDev b,
+                                                                 int all_items) {
+  __shared__ ExhShared sh;
+  const uint32_t n = all_items ? b.i1 - b.i0 : *b.fb_count;
+  for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
+    const uint32_t local = all_items ? e : b.fb_list[e];
+    knn_exhaustive_item(s, st, b, local, sh);
+    __syncthreads();
+  }
+}
+
+__device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
+                                    ExhShared &sh) {
+  const uint32_t pixel = st.items[b.i0 + local];
+  const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
+  const uint32_t k = s.k;
+  const uint32_t n_res = b.n_res;
+  auto d2of = [&](int x, int y) -> uint32_t {
+    const int dx = x - px, dy = y - py;
+    return (uint32_t)(dx * dx + dy * dy);
+  };
+  if (threadIdx.x == 0) {
+    sh.nkeys = 0;
+    sh.total = 0;
+    sh.prefix = 0;
+    sh.rank = k;
+    sh.overflow = 0;
+  }
+  __syncthreads();
+  uint32_t mine = 0;
+  for_points(s, n_res, [&](int, int) { ++mine; });
+  atomicAdd(&sh.total, mine);
+  __syncthreads();
+  const uint32_t total = sh.total;
+  bool take_all = total <= k;
+  if (!take_all) {
+    for (int pass = 0; pass < 4; ++pass) {
+      const int shift = 24 - 8 * pass;
+      for (int i = threadIdx.x; i < 256; i += blockDim.x) sh.hist[i] = 0;
+      __syncthreads();
+      const uint32_t prefix = sh.prefix;
+      for_points(s, n_res, [&](int x, int y) {
+        const uint32_t d2 = d2of(x, y);
+        const bool match = pass == 0 || ((d2 ^ prefix) >> (shift + 8)) == 0;
+        if (match) atomicAdd(&sh.hist[(d2 >> shift) & 255u], 1u);
+      });
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        uint32_t cum = 0, rank = sh.rank;
+        for (int bk = 0; bk < 256; ++bk) {
+          const uint32_t h = sh.hist[bk];
+          if (cum + h >= rank) {
+            sh.prefix = prefix | ((uint32_t)bk << shift);
+            sh.rank = rank - cum;
+            break;
+          }
+          cum += h;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  const uint32_t D = take_all ? 0xffffffffu : sh.prefix;
+  for_points(s, n_res, [&](int x, int y) {
+    const uint32_t d2 = d2of(x, y);
+    if (d2 <= D) {
+      const uint32_t slot = atomicAdd(&sh.nkeys, 1u);
+      if (slot < (uint32_t)kExhCap)
+        sh.keys[slot] = nb_key(d2, x, y);
+      else
+        sh.overflow = 1;
+    }
+  });
+  __syncthreads();
+  if (sh.overflow) {
+    if (threadIdx.x == 0) {
+      set_err(s.err, kDevErrLimit);
+      b.ncnt[local] = 0;
+    }
+    return;
+  }
+  const uint32_t n = sh.nkeys;
+  uint32_t np2 = 1;
+  while (np2 < n) np2 <<= 1;
+  for (uint32_t i = n + threadIdx.x; i < np2; i += blockDim.x) sh.keys[i] = ~0ull;
+  __syncthreads();
+  // bitonic sort of np2 keys
+  for (uint32_t size = 2; size <= np2; size <<= 1) {
+    for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+      for (uint32_t i = threadIdx.x; i < np2; i += blockDim.x) {
+        const uint32_t j = i ^ stride;
+        if (j > i) {
+          const bool up = (i & size) == 0;
+          const unsigned long long a = sh.keys[i], c = sh.keys[j];
+          if ((a > c) == up) {
+            sh.keys[i] = c;
+            sh.keys[j] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  const uint32_t nout = n < k ? n : k;
+  int32_t *nbo = b.nbuf + (size_t)local * k;
+  for (uint32_t i = threadIdx.x; i < nout; i += blockDim.x) {
+    const unsigned long long key = sh.keys[i];
+    const int x = (int)(key & 0xffffu) - 32768, y = (int)((key >> 16) & 0xffffu) - 32768;
+    nbo[i] = pack_off(x - px, y - py);
+  }
+  if (threadIdx.x == 0) b.ncnt[local] = nout;
+}
+
+// ---------------------------------------------------------------------------
+// resolve: warp per item.
+// ---------------------------------------------------------------------------
+struct WarpSmem {
+  int32_t *nb;
+  uint32_t *pat, *gpat;
+  float *wt;
+  double *dist;
+  uint32_t *cxy, *caux;
+};
+
+__device__ __forceinline__ size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+__host__ __device__ __forceinline__ size_t warp_smem_bytes(uint32_t k, uint32_t m) {
+  const size_t kk = k ? k : 1;
+  size_t b = 0;
+  b += ((kk * 8 + 15) & ~(size_t)15);            // dist
+  b += ((kk * 4 + 15) & ~(size_t)15) * 4;        // nb, pat, gpat, wt
+  b += (((kk + m) * 4 + 15) & ~(size_t)15) * 2;  // cxy, caux
+  return b;
+}
+
+__device__ __forceinline__ WarpSmem carve(unsigned char *base, uint32_t k, uint32_t m) {
+  const size_t kk = k ? k : 1;
+  WarpSmem w;
+  unsigned char *p = base;
+  w.dist = (double *)p;
+  p += align16(kk * 8);
+  w.nb = (int32_t *)p;
+  p += align16(kk * 4);
+  w.pat = (uint32_t *)p;
+  p += align16(kk * 4);
+  w.gpat = (uint32_t *)p;
+  p += align16(kk * 4);
+  w.wt = (float *)p;
+  p += align16(kk * 4);
+  w.cxy = (uint32_t *)p;
+  p += align16((kk + m) * 4);
+  w.caux = (uint32_t *)p;
+  return w;
+}
+
+constexpr uint32_t kAuxNeg = 0x8000u;  // random candidate: neighbourhood c + (p - n)
+
+__device__ __forceinline__ uint32_t texel(const uint32_t *lv, const MapDesc &md, int x, int y) {
+  if ((unsigned)x < md.w && (unsigned)y < md.h) return __ldg(&lv[(size_t)y * md.w + x]);
+  return kOutside;
+}
+
+// Sum of the four channel LUT terms in channel order, starting from zero.
+__device__ __forceinline__ float lut4(const float *lut, uint32_t d, float acc) {
+  acc = __fadd_rn(acc, lut[d & 255u]);
+  acc = __fadd_rn(acc, lut[(d >> 8) & 255u]);
+  acc = __fadd_rn(acc, lut[(d >> 16) & 255u]);
+  acc = __fadd_rn(acc, lut[d >> 24]);
+  return acc;
+}
+
+// Cost of candidate c (better_match, ms.rs:1225-1288), abandoning as soon as
+// the partial sum reaches `bound`.  Returns false when abandoned.
+__device__ __forceinline__ bool candidate_cost(const SessionDev &s, const StageDev &st, const WarpSmem &w,
+                                               const float *lc, const float *lg, uint32_t nk, uint32_t cxy,
+                                               uint32_t aux, float bound, float &out) {
+  const uint32_t map = aux & 0x7fffu;
+  const bool neg = (aux & kAuxNeg) != 0;
+  const MapDesc md = s.maps[map];
+  const uint32_t *lv = s.levels + md.off + (size_t)st.level * md.w * md.h;
+  const int cx = (int)(cxy & 0xffffu), cy = (int)(cxy >> 16);
+  const uint32_t *gv = nullptr;
+  GuideDesc gd;
+  if (s.guided) {
+    gd = s.gdesc[map];
+    gv = s.guides + gd.off + (size_t)st.level * gd.w * gd.h;
+  }
+  float score = 0.0f;
+  for (uint32_t j = 0; j < nk; ++j) {
+    const int32_t off = w.nb[j];
+    int dx = off_dx(off), dy = off_dy(off);
+    if (neg) {
+      dx = -dx;
+      dy = -dy;
+    }
+    const int qx = cx + dx, qy = cy + dy;
+    const uint32_t t = texel(lv, md, qx, qy);
+    float nps = lut4(lc, __vabsdiffu4(w.pat[j], t), 0.0f);
+    if (s.guided) {
+      uint32_t gt = kOutside;
+      if ((unsigned)qx < gd.w && (unsigned)qy < gd.h) gt = __ldg(&gv[(size_t)qy * gd.w + qx]);
+      nps = lut4(lg, __vabsdiffu4(w.gpat[j], gt), nps);
+    }
+    score = __fadd_rn(score, __fmul_rn(nps, w.wt[j]));
+    if (score >= bound) return false;
+  }
+  out = score;
+  return true;
+}
+
+__global__ void __launch_bounds__(kResolveWarps *kWarp) k_resolve(SessionDev s, StageDev st, BatchDev b) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float *lc = (float *)smem;
+  float *lg = lc + 256;
+  for (int i = threadIdx.x; i < 512; i += blockDim.x) lc[i] = st.lut[i];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  const WarpSmem w = carve(smem + 2048 + (size_t)warp * warp_smem_bytes(s.k, s.m), s.k, s.m);
+  __syncthreads();
+  const uint32_t nb = b.i1 - b.i0;
+  const int W = (int)s.W, H = (int)s.H;
+  for (uint32_t local = blockIdx.x * kResolveWarps + warp; local < nb; local += gridDim.x * kResolveWarps) {
+    const uint32_t item = b.i0 + local;
+    const uint32_t pixel = st.items[item];
+    const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
+    const bool is_new = item >= st.redo;
+    const uint32_t nk = s.k ? b.ncnt[local] : 0u;
+    Result r;
+    r.pixel = pixel;
+    r.ncand = 0;
+    if (nk == 0) {
+      // no resolved neighbours: resolve_at_random with the stage seed, kept
+      // in the resolved list without tiling mirrors (ms.rs:1002-1010, 473)
+      if (lane == 0) {
+        Pcg32 g = pcg_from_u64(st.stage_seed);
+        uint64_t map64 = 0;
+        uint32_t x = 0, y = 0;
+        bool ok = gen_range_u64_bounded(g, s.n_maps, 256, map64);
+        const uint32_t map = ok ? (uint32_t)map64 : 0u;
+        const MapDesc md = s.maps[map];
+        g = pcg_from_u64(st.stage_seed);
+        ok = ok && gen_range_u32_bounded(g, md.w, 256, x);
+        g = pcg_from_u64(st.stage_seed);
+        ok = ok && gen_range_u32_bounded(g, md.h, 256, y);
+        if (!ok) set_err(s.err, kDevErrNoSample);
+        r.srcxy = x | (y << 16);
+        r.idp = pixel;
+        r.idm = map;
+        r.cmap = map;
+        r.flags = kResAppend;
+        r.score = 0.0f;
+        b.res[local] = r;
+      }
+      continue;
+    }
+    const int32_t *nbo = b.nbuf + (size_t)local * s.k;
+    const double x2 = s.xdiv[px + s.xdiv_off], y2 = s.ydiv[py + s.ydiv_off];
+    // neighbours: offsets, distances, own pattern, coherence candidates
+    uint32_t ncoh = 0;
+    bool bad_map = false;
+    for (uint32_t j0 = 0; j0 < nk; j0 += kWarp) {
+      const uint32_t j = j0 + lane;
+      bool valid = false;
+      uint32_t cxy = 0, aux = 0;
+      if (j < nk) {
+        const int32_t off = nbo[j];
+        w.nb[j] = off;
+        const int nx = px + off_dx(off), ny = py + off_dy(off);
+        const double ddx = __dsub_rn(s.xdiv[nx + s.xdiv_off], x2);
+        const double ddy = __dsub_rn(s.ydiv[ny + s.ydiv_off], y2);
+        w.dist[j] = __fma_rn(ddx, ddx, __dmul_rn(ddy, ddy));
+        int qx = nx, qy = ny;
+        if (s.tiling) {
+          qx = modi(nx, W);
+          qy = modi(ny, H);
+        }
+        w.pat[j] = ((unsigned)qx < s.W && (unsigned)qy < s.H) ? s.color[(size_t)qy * s.W + qx] : kOutside;
+        if (s.guided) {
+          w.gpat[j] = ((unsigned)qx < s.W && (unsigned)qy < s.H) ? __ldg(&s.tguide[(size_t)st.level * s.W * s.H +
+                                                                                   (size_t)qy * s.W + qx])
+                                                                  : kOutside;
+        }
+        const int wx = modi(nx, W), wy = modi(ny, H);
+        const uint4 sv = s.state[(size_t)wy * s.W + wx];
+        const uint32_t map = sv.z;
+        if (map >= s.n_maps) {
+          bad_map = true;
+        } else {
+          const int ccx = (int)(sv.x & 0xffffu) + (px - nx);
+          const int ccy = (int)(sv.x >> 16) + (py - ny);
+          const MapDesc md = s.maps[map];
+          if (coord_valid(s, md, ccx, ccy)) {
+            valid = true;
+            cxy = (uint32_t)ccx | ((uint32_t)ccy << 16);
+            aux = map | (j << 16);
+          }
+        }
+      }
+      const uint32_t bal = __ballot_sync(0xffffffffu, valid);
+      if (valid) {
+        const uint32_t slot = ncoh + __popc(bal & lt);
+        w.cxy[slot] = cxy;
+        w.caux[slot] = aux;
+      }
+      ncoh += __popc(bal);
+    }
+    if (__any_sync(0xffffffffu, bad_map)) {
+      // the reference panics on this index; record the error and leave the
+      // pixel untouched (commit skips results with an invalid map)
+      if (lane == 0) {
+        set_err(s.err, kDevErrIndex);
+        r.srcxy = 0;
+        r.idp = 0;
+        r.idm = 0;
+        r.cmap = 0xffffffffu;
+        r.flags = 0;
+        r.score = 0.0f;
+        b.res[local] = r;
+      }
+      continue;
+    }
+    // random candidates after the coherence ones
+    const uint2 *rc = st.rcand + (size_t)item * s.m;
+    for (uint32_t t = lane; t < s.m; t += kWarp) {
+      const uint2 v = rc[t];
+      w.cxy[ncoh + t] = v.x;
+      w.caux[ncoh + t] = v.y | kAuxNeg | (t << 16);
+    }
+    __syncwarp();
+    // weights: mean over the 4x-duplicated distance list, summed in order
+    double avg = 0.0;
+    if (lane == 0) {
+      double sum = 0.0;
+      for (uint32_t j = 0; j < nk; ++j) {
+        const double d = w.dist[j];
+        sum = __dadd_rn(sum, d);
+        sum = __dadd_rn(sum, d);
+        sum = __dadd_rn(sum, d);
+        sum = __dadd_rn(sum, d);
+      }
+      avg = __ddiv_rn(sum, (double)(nk * 4u));
+    }
+    avg = __shfl_sync(0xffffffffu, avg, 0);
+    bool nan_w = false;
+    for (uint32_t j = lane; j < nk; j += kWarp) {
+      const double d = __ddiv_rn(w.dist[j], avg);
+      const float wv = __double2float_rn(ts_exp64(-1.0 * d));
+      w.wt[j] = wv;
+      nan_w |= (wv != wv);
+    }
+    const bool slow = st.slow_lut || __any_sync(0xffffffffu, nan_w);
+    __syncwarp();
+    const uint32_t nc = ncoh + s.m;
+    float best_s = FLT_MAX;
+    uint32_t best_i = 0;
+    if (!slow) {
+      for (uint32_t base = 0; base < nc; base += kWarp) {
+        const uint32_t c = base + lane;
+        float sc = 0.0f;
+        bool alive = false;
+        if (c < nc) alive = candidate_cost(s, st, w, lc, lg, nk, w.cxy[c], w.caux[c], best_s, sc);
+        float v = alive ? sc : __int_as_float(0x7f800000);
+        uint32_t idx = alive ? c : 0xffffffffu;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+          const uint32_t oi = __shfl_xor_sync(0xffffffffu, idx, o);
+          if (ov < v || (ov == v && oi < idx)) {
+            v = ov;
+            idx = oi;
+          }
+        }
+        if (idx != 0xffffffffu && v < best_s) {
+          best_s = v;
+          best_i = idx;
+        }
+      }
+    } else if (lane == 0) {
+      // the reference's sequential find_best_match, for non-finite costs
+      for (uint32_t c = 0; c < nc; ++c) {
+        const uint32_t aux = w.caux[c];
+        const uint32_t map = aux & 0x7fffu;
+        const bool neg = (aux & kAuxNeg) != 0;
+        const MapDesc md = s.maps[map];
+        const uint32_t *lv = s.levels + md.off + (size_t)st.level * md.w * md.h;
+        const int cx = (int)(w.cxy[c] & 0xffffu), cy = (int)(w.cxy[c] >> 16);
+        float score = 0.0f;
+        bool better = true;
+        for (uint32_t j = 0; j < nk; ++j) {
+          int dx = off_dx(w.nb[j]), dy = off_dy(w.nb[j]);
+          if (neg) {
+            dx = -dx;
+            dy = -dy;
+          }
+          const int qx = cx + dx, qy = cy + dy;
+          float nps = lut4(lc, __vabsdiffu4(w.pat[j], texel(lv, md, qx, qy)), 0.0f);
+          if (s.guided) {
+            const GuideDesc gd = s.gdesc[map];
+            const uint32_t *gv = s.guides + gd.off + (size_t)st.level * gd.w * gd.h;
+            uint32_t gt = kOutside;
+            if ((unsigned)qx < gd.w && (unsigned)qy < gd.h) gt = gv[(size_t)qy * gd.w + qx];
+            nps = lut4(lg, __vabsdiffu4(w.gpat[j], gt), nps);
+          }
+          score = __fadd_rn(score, __fmul_rn(nps, w.wt[j]));
+          if (score >= best_s) {
+            better = false;
+            break;
+          }
+        }
+        if (better) {
+          best_s = score;
+          best_i = c;
+        }
+      }
+    }
+    if (lane == 0) {
+      const uint32_t aux = w.caux[best_i];
+      const uint32_t map = aux & 0x7fffu;
+      const uint32_t cxy = w.cxy[best_i];
+      uint32_t idp;
+      if (aux & kAuxNeg) {
+        idp = (cxy >> 16) * s.maps[map].w + (cxy & 0xffffu);
+      } else {
+        const uint32_t j = aux >> 16;
+        const int32_t off = w.nb[j];
+        const int wx = modi(px + off_dx(off), W), wy = modi(py + off_dy(off), H);
+        idp = s.state[(size_t)wy * s.W + wx].y;
+      }
+      r.srcxy = cxy;
+      r.idp = idp;
+      r.idm = map;
+      r.cmap = map;
+      r.flags = (is_new ? kResAppend : 0u) | kResMirrors;
+      r.score = best_s;
+      r.ncand = nc;
+      b.res[local] = r;
+    }
+  }
+}
+
+// update + flush_resolved for a batch (ms.rs:296-377).
+__global__ void k_commit(SessionDev s, StageDev st, BatchDev b) {
+  const uint32_t local = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nb = b.i1 - b.i0;
+  if (local >= nb) return;
+  const Result r = b.res[local];
+  const uint32_t p = r.pixel;
+  if (r.cmap >= s.n_maps || p >= s.W * s.H) {
+    set_err(s.err, kDevErrIndex);
+    return;
+  }
+  const MapDesc md = s.maps[r.cmap];
+  const uint32_t sx = r.srcxy & 0xffffu, sy = r.srcxy >> 16;
+  if (sx >= md.w || sy >= md.h) {
+    set_err(s.err, kDevErrIndex);
+    return;
+  }
+  s.state[p] = make_uint4(r.srcxy, r.idp, r.idm, r.cmap);
+  s.color[p] = s.levels[md.off + (size_t)st.level * md.w * md.h + (size_t)sy * md.w + sx];
+  if (r.ncand) atomicAdd(s.evals, (unsigned long long)r.ncand);
+  if (r.flags & kResAppend) {
+    const uint32_t item = b.i0 + local;
+    const uint32_t pos = b.n_res + (item - b.append_from);
+    s.resolved[pos] = p;
+    s.rscore[pos] = r.score;
+    const uint32_t x = p % s.W, y = p / s.W;
+    atomicOr(&s.occ[(size_t)y * s.wpr + (x >> 5)], 1u << (x & 31));
+    if (s.tiling && (r.flags & kResMirrors)) atomicOr(&s.mir[(size_t)y * s.wpr + (x >> 5)], 1u << (x & 31));
+  }
+}
+
+// next_pyramid_level (ms.rs:687-700)
+__global__ void k_level_switch(SessionDev s, uint32_t level, uint32_t n_res) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_res) return;
+  const uint32_t p = s.resolved[e];
+  const uint4 sv = s.state[p];
+  if (sv.w >= s.n_maps) {
+    set_err(s.err, kDevErrIndex);
+    return;
+  }
+  const MapDesc md = s.maps[sv.w];
+  const uint32_t x = sv.x & 0xffffu, y = sv.x >> 16;
+  if (x >= md.w || y >= md.h) {  // a coordinate drawn for another example (the reference panics)
+    set_err(s.err, kDevErrIndex);
+    return;
+  }
+  s.color[p] = s.levels[md.off + (size_t)level * md.w * md.h + (size_t)y * md.w + x];
+}
+
+// vertical_sample: u8 RGBA -> f32 RGBA, new height nh.
+__global__ void k_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uint32_t nh, const uint4 *taps,
+                           const float *wts) {
+  const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t oy = blockIdx.y;
+  if (x >= w || oy >= nh) return;
+  const uint4 t = taps[oy];
+  float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+  for (uint32_t i = 0; i < t.y; ++i) {
+    const uchar4 p = *(const uchar4 *)(src + ((size_t)(t.x + i) * w + x) * 4);
+    const float wt = wts[t.z + i];
+    a0 = __fadd_rn(a0, __fmul_rn((float)p.x, wt));
+    a1 = __fadd_rn(a1, __fmul_rn((float)p.y, wt));
+    a2 = __fadd_rn(a2, __fmul_rn((float)p.z, wt));
+    a3 = __fadd_rn(a3, __fmul_rn((float)p.w, wt));
+  }
+  *(float4 *)(tmp + ((size_t)oy * w + x) * 4) = make_float4(a0, a1, a2, a3);
+}
+
+__device__ __forceinline__ uint8_t to_u8(float v) {
+  v = v < 0.0f ? 0.0f : v;
+  v = v > 255.0f ? 255.0f : v;
+  return (uint8_t)roundf(v);
+}
+
+// horizontal_sample: f32 RGBA -> u8 RGBA (clamped, rounded half away from 0).
+__global__ void k_resize_h(const float *tmp, uint32_t w, uint32_t nh, uint8_t *dst, uint32_t nw, const uint4 *taps,
+                           const float *wts) {
+  const uint32_t ox = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t y = blockIdx.y;
+  if (ox >= nw || y >= nh) return;
+  const uint4 t = taps[ox];
+  float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+  for (uint32_t i = 0; i < t.y; ++i) {
+    const float4 p = *(const float4 *)(tmp + ((size_t)y * w + t.x + i) * 4);
+    const float wt = wts[t.z + i];
+    a0 = __fadd_rn(a0, __fmul_rn(p.x, wt));
+    a1 = __fadd_rn(a1, __fmul_rn(p.y, wt));
+    a2 = __fadd_rn(a2, __fmul_rn(p.z, wt));
+    a3 = __fadd_rn(a3, __fmul_rn(p.w, wt));
+  }
+  uchar4 o;
+  o.x = to_u8(a0);
+  o.y = to_u8(a1);
+  o.z = to_u8(a2);
+  o.w = to_u8(a3);
+  *(uchar4 *)(dst + ((size_t)y * nw + ox) * 4) = o;
+}
+
+inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+}  // namespace
+
+size_t resolve_smem_bytes(uint32_t k, uint32_t m, int) { return 2048 + (size_t)kResolveWarps * warp_smem_bytes(k, m); }
+
+cudaError_t configure_kernels(uint32_t k, uint32_t m) {
+  const size_t smem = resolve_smem_bytes(k, m, 0);
+  if (smem <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(k_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+void launch_random_candidates(const SessionDev &s, const StageDev &st, cudaStream_t stream) {
+  if (st.n_items == 0 || s.m == 0) return;
+  k_random_candidates<<<cdiv(st.n_items, 128), 128, 0, stream>>>(s, st);
+}
+
+void launch_knn_walk(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
+  const uint32_t n = b.i1 - b.i0;
+  if (n == 0) return;
+  k_knn_walk<<<cdiv(n, kWalkWarps), kWalkWarps * kWarp, 0, stream>>>(s, st, b);
+}
+
+void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchDev &b, bool all_items,
+                           cudaStream_t stream) {
+  const uint32_t n = b.i1 - b.i0;
+  if (n == 0) return;
+  const uint32_t grid = n < 1216u ? n : 1216u;  // 152 SMs x 8 CTAs, grid-stride beyond
+  k_knn_exhaustive<<<grid, kExhThreads, 0, stream>>>(s, st, b, all_items ? 1 : 0);
+}
+
+void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
+  const uint32_t n = b.i1 - b.i0;
+  if (n == 0) return;
+  const size_t smem = resolve_smem_bytes(s.k, s.m, s.guided);
+  k_resolve<<<cdiv(n, kResolveWarps), kResolveWarps * kWarp, smem, stream>>>(s, st, b);
+}
+
+void launch_commit(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
+  const uint32_t n = b.i1 - b.i0;
+  if (n == 0) return;
+  k_commit<<<cdiv(n, 256), 256, 0, stream>>>(s, st, b);
+}
+
+void launch_level_switch(const SessionDev &s, uint32_t level, uint32_t n_res, cudaStream_t stream) {
+  if (n_res == 0) return;
+  k_level_switch<<<cdiv(n_res, 256), 256, 0, stream>>>(s, level, n_res);
+}
+
+void launch_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uint32_t nh, const uint4 *taps,
+                     const float *wts, cudaStream_t stream) {
+  if (w == 0 || nh == 0) return;
+  dim3 grid(cdiv(w, 128), nh);
+  k_resize_v<<<grid, 128, 0, stream>>>(src, w, h, tmp, nh, taps, wts);
+}
+
+void launch_resize_h(const float *tmp, uint32_t w, uint32_t nh, uint8_t *dst, uint32_t nw, const uint4 *taps,
+                     const float *wts, cudaStream_t stream) {
+  if (nw == 0 || nh == 0) return;
+  dim3 grid(cdiv(nw, 128), nh);
+  k_resize_h<<<grid, 128, 0, stream>>>(tmp, w, nh, dst, nw, taps, wts);
+}
+
+}  // namespace ts

@@ -1,0 +1,118 @@
+// ts_kernels.cuh — device data layout and kernel launchers of the synthesis
+// hot loop (the internal interface between ts_session.cpp and ts_kernels.cu).
+//
+// Layout in device memory (one session):
+//   levels  u32[ ]   every non-ignored example's pyramid, packed RGBA8
+//                    (byte 0 = R); map f, level l at maps[f].off + l*w*h
+//   masks   u8[ ]    sample-mask bytes (1 = may be sampled), maps[f].mask_off
+//   guides  u32[ ]   example-guide pyramids, indexed by the unfiltered
+//                    example index (the reference indexes its guide list with
+//                    the filtered map id, ms.rs:1261-1266)
+//   tguide  u32[levels][W*H]  target-guide pyramid
+//   color   u32[W*H] output colour map
+//   state   uint4[W*H] {src x | y<<16, patch id, id-map id, coord-map id}
+//   occ/mir u32[H][ceil(W/32)] resolved-point bitmap / "has tiling mirrors"
+//   resolved u32[], rscore f32[]  the resolved list and first-resolve scores
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace ts {
+
+struct MapDesc {
+  uint32_t w, h;
+  uint64_t off;      // texel offset of level 0
+  int64_t mask_off;  // byte offset in the mask buffer, -1 = every texel valid
+};
+
+struct GuideDesc {
+  uint32_t w, h;
+  uint64_t off;
+};
+
+enum : uint32_t { kResAppend = 1u, kResMirrors = 2u };
+
+struct Result {
+  uint32_t pixel, srcxy, idp, idm;
+  uint32_t cmap, flags;
+  float score;
+  uint32_t ncand;
+};
+
+// Device status word values (0 = fine).
+enum : int { kDevOk = 0, kDevErrIndex = 1, kDevErrNoSample = 2, kDevErrLimit = 3 };
+
+struct SessionDev {
+  const uint32_t *levels;
+  const uint8_t *masks;
+  const MapDesc *maps;
+  uint32_t n_maps;
+  uint32_t n_levels;
+  const uint32_t *guides;
+  const GuideDesc *gdesc;
+  uint32_t n_guides;
+  int guided;
+  const uint32_t *tguide;
+  const double *xdiv;  // xdiv[x + xdiv_off] == (double)x / W
+  const double *ydiv;
+  int32_t xdiv_off, ydiv_off;
+  uint32_t *color;
+  uint4 *state;
+  uint32_t *occ;
+  uint32_t *mir;
+  uint32_t *resolved;
+  float *rscore;
+  const int32_t *knn_tab;  // offsets (dx & 0xffff) | (dy << 16), sorted by (d2, dy, dx)
+  uint32_t knn_tab_n;
+  int *err;
+  unsigned long long *evals;  // candidate-cost evaluations, summed by commit
+  uint32_t W, H, wpr;  // wpr: 32-bit words per bitmap row
+  int tiling;
+  int32_t x_l, x_r, y_b, y_t;
+  uint32_t k, m;
+};
+
+struct StageDev {
+  uint32_t level;
+  int slow_lut;            // LUT holds a non-finite value: exact sequential argmin
+  const float *lut;        // [2][256]: content, guide
+  uint64_t stage_seed;
+  const uint32_t *items;   // item -> pixel for this stage
+  uint32_t n_items;
+  uint32_t redo;
+  uint2 *rcand;            // [n_items][m] random candidates {x | y<<16, map}
+};
+
+struct BatchDev {
+  uint32_t i0, i1;       // stage items [i0, i1)
+  uint32_t n_res;        // resolved-list length at batch start
+  uint32_t append_from;  // items >= append_from append to the resolved list
+  int32_t *nbuf;         // [batch][k] neighbour offsets
+  uint32_t *ncnt;        // [batch] neighbour counts
+  uint32_t *fb_list;     // items needing the exhaustive k-NN
+  uint32_t *fb_count;
+  Result *res;           // [batch]
+};
+
+// Launchers (stream-ordered, no synchronisation).
+void launch_random_candidates(const SessionDev &s, const StageDev &st, cudaStream_t stream);
+void launch_knn_walk(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
+void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchDev &b, bool all_items,
+                           cudaStream_t stream);
+void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
+void launch_commit(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
+void launch_level_switch(const SessionDev &s, uint32_t level, uint32_t n_res, cudaStream_t stream);
+
+// Separable resize (image 0.23 imageops::resize): taps[o] = {left, count,
+// weight offset}; vertical pass u8 -> f32, horizontal pass f32 -> u8.
+void launch_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uint32_t nh, const uint4 *taps,
+                     const float *wts, cudaStream_t stream);
+void launch_resize_h(const float *tmp, uint32_t w, uint32_t nh, uint8_t *dst, uint32_t nw, const uint4 *taps,
+                     const float *wts, cudaStream_t stream);
+
+// Bytes of dynamic shared memory the resolve kernel needs per CTA.
+size_t resolve_smem_bytes(uint32_t k, uint32_t m, int guided);
+// Per-device kernel attributes for a (k, m) session (current device).
+cudaError_t configure_kernels(uint32_t k, uint32_t m);
+
+}  // namespace ts
