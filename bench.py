@@ -137,6 +137,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--once", action="store_true", help="build and run one session, print its stats (for profilers)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -151,6 +152,10 @@ def main():
 
     spec = workload()
     px = spec["out_w"] * spec["out_h"]
+    if args.once:
+        g = ts.builder_from_spec(spec).build().run()
+        print(json.dumps(g.stats()))
+        return
     # --- device-resident throughput: sessions built before the timed region
     for _ in range(args.warmup):
         ts.builder_from_spec(spec).build().run()
@@ -178,6 +183,22 @@ def main():
         e2e_t.append(time.perf_counter() - t1)
     e2e = px / (sum(e2e_t) / len(e2e_t)) / 1e6
     peak, peak_kind = _peaks()
+    # --- roofline of the dominant kernel: a separate pass with CUDA events
+    # around every launch on the launching stream
+    prof = ts.builder_from_spec(spec, profile=True).build().run().stats()
+    kern = prof["kernels"]
+    top = max(kern, key=lambda n: kern[n]["ms"])
+    res = kern["resolve"]
+    k = spec["params"]["nearest_neighbors"]
+    per_eval = 4 * k * (2 if spec.get("target_guide") is not None else 1)
+    alg_bytes = prof["cost_evals"] * per_eval  # example texels every candidate-cost evaluation reads
+    achieved = alg_bytes / (res["ms"] / 1e3) / 1e9
+    roofline = {"kernel": "k_resolve", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                "alg_bytes_per_launch": alg_bytes / max(1, res["launches"]),
+                "avg_launch_ms": res["ms"] / max(1, res["launches"]), "launches": res["launches"],
+                "kernel_share": {n: kern[n]["ms"] / max(1e-9, sum(v["ms"] for v in kern.values())) for n in kern},
+                "top_kernel": top}
     line = {
         "metric": "output Mpx/s", "value": value, "unit": "Mpx/s", "n_gpus": world, "steps": len(gpu_ms),
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -189,7 +210,7 @@ def main():
         "wall_ms_per_step": wall / len(gpu_ms) * 1e3,
         "clocks": clk.summary(),
         "e2e": {"value": e2e, "unit": "Mpx/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": None,
+        "roofline": roofline,
         "cpu_baseline": None,
     }
     if not args.no_cpu_baseline and rank == 0:

@@ -113,6 +113,18 @@ typedef struct ts_progress {
 } ts_progress;
 typedef void (*ts_progress_fn)(const ts_progress *update, void *user);
 
+/* Kernel kinds of a run, for per-kernel timings. */
+enum {
+  TS_KERNEL_RANDOM_CANDIDATES = 0,
+  TS_KERNEL_KNN_WALK = 1,
+  TS_KERNEL_KNN_EXHAUSTIVE = 2,
+  TS_KERNEL_RESOLVE = 3,
+  TS_KERNEL_COMMIT = 4,
+  TS_KERNEL_LEVEL_SWITCH = 5,
+  TS_KERNEL_MEAN = 6,
+  TS_KERNEL_KINDS = 7
+};
+
 /* Run statistics of a generated image. */
 typedef struct ts_run_stats {
   uint64_t resolves;      /* work items resolved in the stage loop */
@@ -122,6 +134,11 @@ typedef struct ts_run_stats {
   uint64_t kernel_launches;
   double gpu_ms;          /* device time of run (CUDA events) */
   double wall_ms;         /* host wall time of run */
+  /* Filled when the builder enabled ts_builder_profile_kernels: launches
+   * and summed device time (CUDA events around each launch) per kernel
+   * kind, indexed by TS_KERNEL_*. */
+  uint64_t kernel_count[8];
+  double kernel_ms[8];
 } ts_run_stats;
 
 const char *ts_status_str(int status);
@@ -181,6 +198,9 @@ int ts_builder_max_thread_count(ts_builder *b, uint64_t count);
 int ts_builder_batch_schedule(ts_builder *b, uint32_t batch_divisor, uint32_t max_batch);
 /* CUDA device ordinal (default 0). */
 int ts_builder_device(ts_builder *b, int32_t device);
+/* Time every kernel launch of run() with CUDA events (adds host overhead;
+ * for measurement runs only). */
+int ts_builder_profile_kernels(ts_builder *b, int32_t on);
 
 /* SessionBuilder::build (session.rs:336-448).  Consumes the builder on
  * success and on failure (as the Rust method takes self); the builder must

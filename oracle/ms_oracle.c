@@ -150,37 +150,67 @@ uint64_t tso_gen_range_u64(uint64_t seed, uint64_t n) {
 
 /* ------------------------------------------------------------------------ */
 /* exp for the neighbour weights (ms.rs:1198-1203 calls f64::exp).           */
-/* Cody & Waite range reduction x = n ln2 + r, |r| <= ln2/2, then the Taylor  */
-/* series of exp(r) to degree 13 by Horner's rule with fused multiply-adds,   */
-/* scaled by 2^n.  The GPU path evaluates the identical operation sequence,   */
-/* so both sides produce the same double; it is within a few ulp of the true  */
-/* exponential, and the weights are rounded to f32 afterwards.                */
+/* Table driven: x = (64 m + j) ln2/64 + r, |r| <= ln2/128 (Cody & Waite      */
+/* reduction, ln2/64 split in a high part with zero trailing bits and a low  */
+/* part), the Taylor series of e^r to degree 5 by Horner's rule with fused   */
+/* multiply-adds, times 2^(j/64) (nearest doubles) and 2^m.  The GPU path     */
+/* evaluates the identical operation sequence, so both sides produce the     */
+/* same double, within a few ulp of the true exponential; the weights are    */
+/* rounded to f32 afterwards.                                                */
 /* ------------------------------------------------------------------------ */
+static const double exp2_64[64] = {
+  0x1.0000000000000p+0, 0x1.02c9a3e778061p+0,
+  0x1.059b0d3158574p+0, 0x1.0874518759bc8p+0,
+  0x1.0b5586cf9890fp+0, 0x1.0e3ec32d3d1a2p+0,
+  0x1.11301d0125b51p+0, 0x1.1429aaea92de0p+0,
+  0x1.172b83c7d517bp+0, 0x1.1a35beb6fcb75p+0,
+  0x1.1d4873168b9aap+0, 0x1.2063b88628cd6p+0,
+  0x1.2387a6e756238p+0, 0x1.26b4565e27cddp+0,
+  0x1.29e9df51fdee1p+0, 0x1.2d285a6e4030bp+0,
+  0x1.306fe0a31b715p+0, 0x1.33c08b26416ffp+0,
+  0x1.371a7373aa9cbp+0, 0x1.3a7db34e59ff7p+0,
+  0x1.3dea64c123422p+0, 0x1.4160a21f72e2ap+0,
+  0x1.44e086061892dp+0, 0x1.486a2b5c13cd0p+0,
+  0x1.4bfdad5362a27p+0, 0x1.4f9b2769d2ca7p+0,
+  0x1.5342b569d4f82p+0, 0x1.56f4736b527dap+0,
+  0x1.5ab07dd485429p+0, 0x1.5e76f15ad2148p+0,
+  0x1.6247eb03a5585p+0, 0x1.6623882552225p+0,
+  0x1.6a09e667f3bcdp+0, 0x1.6dfb23c651a2fp+0,
+  0x1.71f75e8ec5f74p+0, 0x1.75feb564267c9p+0,
+  0x1.7a11473eb0187p+0, 0x1.7e2f336cf4e62p+0,
+  0x1.82589994cce13p+0, 0x1.868d99b4492edp+0,
+  0x1.8ace5422aa0dbp+0, 0x1.8f1ae99157736p+0,
+  0x1.93737b0cdc5e5p+0, 0x1.97d829fde4e50p+0,
+  0x1.9c49182a3f090p+0, 0x1.a0c667b5de565p+0,
+  0x1.a5503b23e255dp+0, 0x1.a9e6b5579fdbfp+0,
+  0x1.ae89f995ad3adp+0, 0x1.b33a2b84f15fbp+0,
+  0x1.b7f76f2fb5e47p+0, 0x1.bcc1e904bc1d2p+0,
+  0x1.c199bdd85529cp+0, 0x1.c67f12e57d14bp+0,
+  0x1.cb720dcef9069p+0, 0x1.d072d4a07897cp+0,
+  0x1.d5818dcfba487p+0, 0x1.da9e603db3285p+0,
+  0x1.dfc97337b9b5fp+0, 0x1.e502ee78b3ff6p+0,
+  0x1.ea4afa2a490dap+0, 0x1.efa1bee615a27p+0,
+  0x1.f50765b6e4540p+0, 0x1.fa7c1819e90d8p+0,
+};
+
 static double tso_exp(double x) {
   if (x != x) return x;
   if (x < -700.0) return 0.0; /* far below the smallest f32 after rounding */
   if (x > 700.0) return INFINITY;
-  const double inv_ln2 = 1.44269504088896338700e+00;
-  const double ln2_hi = 6.93147180369123816490e-01; /* 0x3fe62e42fee00000 */
-  const double ln2_lo = 1.90821492927058770002e-10; /* 0x3dea39ef35793c76 */
-  double n = rint(x * inv_ln2);
-  double r = x - n * ln2_hi;
-  r = r - n * ln2_lo;
-  double p = 1.0 / 6227020800.0; /* 1/13! */
-  p = fma(p, r, 1.0 / 479001600.0);
-  p = fma(p, r, 1.0 / 39916800.0);
-  p = fma(p, r, 1.0 / 3628800.0);
-  p = fma(p, r, 1.0 / 362880.0);
-  p = fma(p, r, 1.0 / 40320.0);
-  p = fma(p, r, 1.0 / 5040.0);
-  p = fma(p, r, 1.0 / 720.0);
-  p = fma(p, r, 1.0 / 120.0);
+  const double inv_step = 0x1.71547652b82fep+6;
+  const double step_hi = 0x1.62e42fee00000p-7;
+  const double step_lo = 0x1.a39ef35793c76p-39;
+  double k = rint(x * inv_step);
+  double r = fma(-k, step_hi, x);
+  r = fma(-k, step_lo, r);
+  double p = 1.0 / 120.0;
   p = fma(p, r, 1.0 / 24.0);
   p = fma(p, r, 1.0 / 6.0);
   p = fma(p, r, 0.5);
   p = fma(p, r, 1.0);
   p = fma(p, r, 1.0);
-  return ldexp(p, (int)n);
+  int ki = (int)k;
+  return ldexp(exp2_64[ki & 63] * p, ki >> 6);
 }
 double tso_exp_export(double x) { return tso_exp(x); }
 

@@ -68,13 +68,19 @@ class _Progress(C.Structure):
                 ("stage_current", C.c_uint64), ("stage_total", C.c_uint64)]
 
 
+KERNEL_KINDS = ("random_candidates", "knn_walk", "knn_exhaustive", "resolve", "commit", "level_switch", "mean")
+
+
 class RunStats(C.Structure):
     _fields_ = [("resolves", C.c_uint64), ("cost_evals", C.c_uint64), ("batches", C.c_uint64),
                 ("stages", C.c_uint64), ("kernel_launches", C.c_uint64), ("gpu_ms", C.c_double),
-                ("wall_ms", C.c_double)]
+                ("wall_ms", C.c_double), ("kernel_count", C.c_uint64 * 8), ("kernel_ms", C.c_double * 8)]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        d = {f: getattr(self, f) for f, _ in self._fields_ if not f.startswith("kernel_") or f == "kernel_launches"}
+        d["kernels"] = {name: {"launches": int(self.kernel_count[i]), "ms": float(self.kernel_ms[i])}
+                        for i, name in enumerate(KERNEL_KINDS)}
+        return d
 
 
 _PROGRESS_FN = C.CFUNCTYPE(None, C.POINTER(_Progress), C.c_void_p)
@@ -106,6 +112,7 @@ SIGNATURES = {
     "ts_builder_max_thread_count": (C.c_int, [C.c_void_p, C.c_uint64]),
     "ts_builder_batch_schedule": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
     "ts_builder_device": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ts_builder_profile_kernels": (C.c_int, [C.c_void_p, C.c_int32]),
     "ts_builder_build": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "ts_session_run": (C.c_int, [C.c_void_p, _PROGRESS_FN, C.c_void_p, C.POINTER(C.c_void_p)]),
     "ts_session_free": (None, [C.c_void_p]),
@@ -320,6 +327,10 @@ class SessionBuilder:
     def device(self, ordinal):
         return self._check(lib().ts_builder_device(self._h, int(ordinal)))
 
+    def profile_kernels(self, on=True):
+        """Time every kernel launch with CUDA events (measurement runs)."""
+        return self._check(lib().ts_builder_profile_kernels(self._h, 1 if on else 0))
+
     def build(self):
         out = C.c_void_p()
         rc = lib().ts_builder_build(self._h, C.byref(out))
@@ -407,7 +418,7 @@ class GeneratedImage:
         return st.as_dict()
 
 
-def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0):
+def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0, profile=False):
     """A SessionBuilder for a workload spec dict (see workloads.py)."""
     p = spec["params"]
     b = Session.builder()
@@ -437,6 +448,8 @@ def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0):
     if p.get("random_init") is not None:
         b.random_init(p["random_init"])
     b.batch_schedule(batch_divisor, max_batch).device(device)
+    if profile:
+        b.profile_kernels(True)
     return b
 
 

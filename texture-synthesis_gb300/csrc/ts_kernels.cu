@@ -1,16 +1,23 @@
 // ts_kernels.cu — sm_103a kernels of the texture-synthesis hot loop.
 //
-// One batch step of a synthesis stage is four launches:
+// One batch step of a synthesis stage is five launches:
 //   knn_walk        warp per work item: the k nearest resolved points under
 //                   the (d2, y, x) order, by walking a table of lattice offsets
 //                   sorted in that order and testing a resolved-point bitmap
 //                   (replaces TreeGrid::get_k_nearest_neighbors, ms.rs:1363-1530)
 //   knn_exhaustive  CTA per item the walk could not finish (sparse regions):
 //                   radix-select over the resolved list
-//   resolve         warp per item: distance weights (ms.rs:405-425,
-//                   1198-1203), coherence + random candidates (ms.rs:478-602),
-//                   own pattern (ms.rs:1151-1181), candidate cost and first-min
+//   mean            thread per item: the mean of the 4x-duplicated distance
+//                   list (ms.rs:417-423), the in-order f64 sum; one item per
+//                   lane, because an f64 warp instruction costs the same
+//                   whatever its active-lane count
+//   resolve         warp per item: neighbour weights (ms.rs:1198-1203) in
+//                   double-f32 arithmetic with an exact f64 fallback,
+//                   coherence + random candidates (ms.rs:478-602), own
+//                   pattern (ms.rs:1151-1181), candidate cost and first-min
 //                   argmin (ms.rs:1184-1288), lanes over candidates
+// The k-NN kernels also write each neighbour's exact squared normalised
+// distance (ms.rs:410-415), one f64 fused multiply-add from per-pixel tables.
 //   commit          thread per item: update + flush_resolved (ms.rs:296-377)
 // Every item of a batch reads the state as it was when the batch started;
 // commit runs after all of them.  Per stage, random_candidates precomputes the
@@ -38,6 +45,9 @@ constexpr int kWalkWarps = 8;
 constexpr int kExhThreads = 256;
 constexpr int kExhCap = 2048;  // keys kept by the exhaustive k-NN at the cut distance
 constexpr uint32_t kMaxDraws = 1u << 22;
+
+__device__ const double g_exp2_64[64] = {TS_EXP2_TABLE_VALUES};
+__device__ const float g_exp2_ff[128] = {TS_EXP2_FF_TABLE_VALUES};
 
 __device__ __forceinline__ void set_err(int *err, int code) {
   if (*err == 0) atomicCAS(err, 0, code);
@@ -127,12 +137,25 @@ __global__ void k_random_candidates(SessionDev s, StageDev st) {
   }
 }
 
+// Exact squared normalised distance of a neighbour at offset (dx, dy).
+__device__ __forceinline__ double neighbour_dist(const SessionDev &s, int px, int py, int dx, int dy, double x2,
+                                                  double y2) {
+  const int R = s.dtab_r;
+  if (dx >= -R && dx <= R && dy >= -R && dy <= R) {
+    const double ddx = __ldg(&s.dxt[(size_t)px * (2 * R + 1) + dx + R]);
+    return __fma_rn(ddx, ddx, __ldg(&s.dy2t[(size_t)py * (2 * R + 1) + dy + R]));
+  }
+  const double ddx = __dsub_rn(s.xdiv[px + dx + s.xdiv_off], x2);
+  const double ddy = __dsub_rn(s.ydiv[py + dy + s.ydiv_off], y2);
+  return __fma_rn(ddx, ddx, __dmul_rn(ddy, ddy));
+}
+
 // ---------------------------------------------------------------------------
 // k-NN by walking the sorted offset table.  The table holds every lattice
 // offset with d2 <= its radius^2, in (d2, dy, dx) order, so the first k
 // occupied entries are exactly the k nearest points under the tie rule.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kWalkWarps *kWarp) k_knn_walk(SessionDev s, StageDev st, BatchDev b) {
+__global__ void __launch_bounds__(kWalkWarps *kWarp, 4) k_knn_walk(SessionDev s, StageDev st, BatchDev b) {
   const int lane = threadIdx.x & 31;
   const uint32_t lt = (1u << lane) - 1u;
   const uint32_t nb = b.i1 - b.i0;
@@ -140,6 +163,7 @@ __global__ void __launch_bounds__(kWalkWarps *kWarp) k_knn_walk(SessionDev s, St
        local += gridDim.x * kWalkWarps) {
     const uint32_t pixel = st.items[b.i0 + local];
     const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
+    const double x2 = s.xdiv[px + s.xdiv_off], y2 = s.ydiv[py + s.ydiv_off];
     int32_t *nbo = b.nbuf + (size_t)local * s.k;
     uint32_t count = 0;
     for (uint32_t c = 0; c < s.knn_tab_n; c += kWarp) {
@@ -152,7 +176,10 @@ __global__ void __launch_bounds__(kWalkWarps *kWarp) k_knn_walk(SessionDev s, St
       }
       const uint32_t bal = __ballot_sync(0xffffffffu, hit);
       const uint32_t rank = count + __popc(bal & lt);
-      if (hit && rank < s.k) nbo[rank] = off;
+      if (hit && rank < s.k) {
+        nbo[rank] = off;
+        b.dist[(size_t)rank * nb + local] = neighbour_dist(s, px, py, off_dx(off), off_dy(off), x2, y2);
+      }
       count += __popc(bal);
       if (count >= s.k) break;
     }
@@ -313,12 +340,40 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
   }
   const uint32_t nout = n < k ? n : k;
   int32_t *nbo = b.nbuf + (size_t)local * k;
+  const uint32_t nb = b.i1 - b.i0;
+  const double x2 = s.xdiv[px + s.xdiv_off], y2 = s.ydiv[py + s.ydiv_off];
   for (uint32_t i = threadIdx.x; i < nout; i += blockDim.x) {
     const unsigned long long key = sh.keys[i];
     const int x = (int)(key & 0xffffu) - 32768, y = (int)((key >> 16) & 0xffffu) - 32768;
     nbo[i] = pack_off(x - px, y - py);
+    b.dist[(size_t)i * nb + local] = neighbour_dist(s, px, py, x - px, y - py, x2, y2);
   }
   if (threadIdx.x == 0) b.ncnt[local] = nout;
+}
+
+// ---------------------------------------------------------------------------
+// mean: thread per item (get_distances_to_k_neighs, ms.rs:417-423): the sum
+// of the 4x-duplicated distance list in order, then / (4k).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_mean(SessionDev s, StageDev st, BatchDev b) {
+  const uint32_t nb = b.i1 - b.i0;
+  const uint32_t local = blockIdx.x * blockDim.x + threadIdx.x;
+  if (local >= nb) return;
+  const uint32_t nk = b.ncnt[local];
+  if (nk == 0) return;
+  // one item per lane: 32 chains share each f64 warp instruction
+  double sum = 0.0;
+#pragma unroll 4
+  for (uint32_t j = 0; j < nk; ++j) {
+    const double d = b.dist[(size_t)j * nb + local];
+    sum = __dadd_rn(sum, d);
+    sum = __dadd_rn(sum, d);
+    sum = __dadd_rn(sum, d);
+    sum = __dadd_rn(sum, d);
+  }
+  const double avg = __ddiv_rn(sum, (double)(nk * 4u));
+  b.mean[local] = avg;
+  b.minv[local] = __drcp_rn(avg);
 }
 
 // ---------------------------------------------------------------------------
@@ -328,7 +383,6 @@ struct WarpSmem {
   int32_t *nb;
   uint32_t *pat, *gpat;
   float *wt;
-  double *dist;
   uint32_t *cxy, *caux;
 };
 
@@ -337,7 +391,6 @@ __device__ __forceinline__ size_t align16(size_t v) { return (v + 15) & ~(size_t
 __host__ __device__ __forceinline__ size_t warp_smem_bytes(uint32_t k, uint32_t m) {
   const size_t kk = k ? k : 1;
   size_t b = 0;
-  b += ((kk * 8 + 15) & ~(size_t)15);            // dist
   b += ((kk * 4 + 15) & ~(size_t)15) * 4;        // nb, pat, gpat, wt
   b += (((kk + m) * 4 + 15) & ~(size_t)15) * 2;  // cxy, caux
   return b;
@@ -347,8 +400,6 @@ __device__ __forceinline__ WarpSmem carve(unsigned char *base, uint32_t k, uint3
   const size_t kk = k ? k : 1;
   WarpSmem w;
   unsigned char *p = base;
-  w.dist = (double *)p;
-  p += align16(kk * 8);
   w.nb = (int32_t *)p;
   p += align16(kk * 4);
   w.pat = (uint32_t *)p;
@@ -420,9 +471,13 @@ __device__ __forceinline__ bool candidate_cost(const SessionDev &s, const StageD
 
 __global__ void __launch_bounds__(kResolveWarps *kWarp) k_resolve(SessionDev s, StageDev st, BatchDev b) {
   extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double tab[64];
+  __shared__ float tab_ff[128];
   float *lc = (float *)smem;
   float *lg = lc + 256;
   for (int i = threadIdx.x; i < 512; i += blockDim.x) lc[i] = st.lut[i];
+  if (threadIdx.x < 64) tab[threadIdx.x] = g_exp2_64[threadIdx.x];
+  tab_ff[threadIdx.x] = g_exp2_ff[threadIdx.x];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t lt = (1u << lane) - 1u;
   const WarpSmem w = carve(smem + 2048 + (size_t)warp * warp_smem_bytes(s.k, s.m), s.k, s.m);
@@ -464,8 +519,9 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp) k_resolve(SessionDev s, 
       continue;
     }
     const int32_t *nbo = b.nbuf + (size_t)local * s.k;
-    const double x2 = s.xdiv[px + s.xdiv_off], y2 = s.ydiv[py + s.ydiv_off];
-    // neighbours: offsets, distances, own pattern, coherence candidates
+    const double avg = b.mean[local], inv = b.minv[local];
+    // neighbours: offsets, weights, own pattern, coherence candidates
+    bool nan_w = false;
     uint32_t ncoh = 0;
     bool bad_map = false;
     for (uint32_t j0 = 0; j0 < nk; j0 += kWarp) {
@@ -475,10 +531,14 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp) k_resolve(SessionDev s, 
       if (j < nk) {
         const int32_t off = nbo[j];
         w.nb[j] = off;
+        // weight (find_best_match, ms.rs:1198-1203): w = (f32) exp(-(d / mean))
+        const double dj = b.dist[(size_t)j * nb + local];
+        float wv;
+        if (!ts_weight_ff(dj, avg, tab_ff, wv))
+          wv = __double2float_rn(ts_exp64(-1.0 * ts_div_markstein(dj, avg, inv), tab));
+        w.wt[j] = wv;
+        nan_w |= (wv != wv);
         const int nx = px + off_dx(off), ny = py + off_dy(off);
-        const double ddx = __dsub_rn(s.xdiv[nx + s.xdiv_off], x2);
-        const double ddy = __dsub_rn(s.ydiv[ny + s.ydiv_off], y2);
-        w.dist[j] = __fma_rn(ddx, ddx, __dmul_rn(ddy, ddy));
         int qx = nx, qy = ny;
         if (s.tiling) {
           qx = modi(nx, W);
@@ -535,28 +595,6 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp) k_resolve(SessionDev s, 
       const uint2 v = rc[t];
       w.cxy[ncoh + t] = v.x;
       w.caux[ncoh + t] = v.y | kAuxNeg | (t << 16);
-    }
-    __syncwarp();
-    // weights: mean over the 4x-duplicated distance list, summed in order
-    double avg = 0.0;
-    if (lane == 0) {
-      double sum = 0.0;
-      for (uint32_t j = 0; j < nk; ++j) {
-        const double d = w.dist[j];
-        sum = __dadd_rn(sum, d);
-        sum = __dadd_rn(sum, d);
-        sum = __dadd_rn(sum, d);
-        sum = __dadd_rn(sum, d);
-      }
-      avg = __ddiv_rn(sum, (double)(nk * 4u));
-    }
-    avg = __shfl_sync(0xffffffffu, avg, 0);
-    bool nan_w = false;
-    for (uint32_t j = lane; j < nk; j += kWarp) {
-      const double d = __ddiv_rn(w.dist[j], avg);
-      const float wv = __double2float_rn(ts_exp64(-1.0 * d));
-      w.wt[j] = wv;
-      nan_w |= (wv != wv);
     }
     const bool slow = st.slow_lut || __any_sync(0xffffffffu, nan_w);
     __syncwarp();
@@ -776,6 +814,12 @@ void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchD
   if (n == 0) return;
   const uint32_t grid = n < 1216u ? n : 1216u;  // 152 SMs x 8 CTAs, grid-stride beyond
   k_knn_exhaustive<<<grid, kExhThreads, 0, stream>>>(s, st, b, all_items ? 1 : 0);
+}
+
+void launch_mean(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
+  const uint32_t n = b.i1 - b.i0;
+  if (n == 0 || s.k == 0) return;
+  k_mean<<<cdiv(n, 128), 128, 0, stream>>>(s, st, b);
 }
 
 void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {

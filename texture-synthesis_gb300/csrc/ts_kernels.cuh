@@ -56,6 +56,11 @@ struct SessionDev {
   const double *xdiv;  // xdiv[x + xdiv_off] == (double)x / W
   const double *ydiv;
   int32_t xdiv_off, ydiv_off;
+  // dxt[px * (2R+1) + dx + R] == xdiv[px + dx] - xdiv[px] and
+  // dy2t[py * (2R+1) + dy + R] == dy * dy (dy likewise), for |dx|, |dy| <= R
+  const double *dxt;
+  const double *dy2t;
+  int32_t dtab_r;
   uint32_t *color;
   uint4 *state;
   uint32_t *occ;
@@ -91,6 +96,9 @@ struct BatchDev {
   uint32_t *ncnt;        // [batch] neighbour counts
   uint32_t *fb_list;     // items needing the exhaustive k-NN
   uint32_t *fb_count;
+  double *dist;          // [k][batch] squared normalised distances
+  double *mean;          // [batch] mean of the 4x-duplicated distance list
+  double *minv;          // [batch] RN(1 / mean)
   Result *res;           // [batch]
 };
 
@@ -99,6 +107,7 @@ void launch_random_candidates(const SessionDev &s, const StageDev &st, cudaStrea
 void launch_knn_walk(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
 void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchDev &b, bool all_items,
                            cudaStream_t stream);
+void launch_mean(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
 void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
 void launch_commit(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
 void launch_level_switch(const SessionDev &s, uint32_t level, uint32_t n_res, cudaStream_t stream);

@@ -39,6 +39,7 @@ constexpr uint32_t kMaxExamples = 256;
 constexpr uint32_t kMaxSide = 16384;
 constexpr float kTilingBoundary = 0.05f;  // TILING_BOUNDARY_PERCENTAGE, ms.rs:15
 constexpr int kKnnTabRadius = 36;
+constexpr int kDistTabRadius = 64;  // offsets the weight tables cover
 constexpr uint64_t kRcandBudget = 64ull << 20;  // random-candidate entries held at once
 
 struct Image {
@@ -82,6 +83,7 @@ struct Params {
   uint32_t batch_divisor = 8;
   uint32_t max_batch = 0;
   int device = 0;
+  bool profile = false;
 };
 
 std::string fmt_float(float v) {
@@ -470,6 +472,11 @@ int ts_builder_device(ts_builder *b, int32_t device) {
   b->prm.device = device;
   return TS_OK;
 }
+int ts_builder_profile_kernels(ts_builder *b, int32_t on) {
+  BUILDER_GUARD(b);
+  b->prm.profile = on != 0;
+  return TS_OK;
+}
 
 }  // extern "C"
 
@@ -723,6 +730,45 @@ std::vector<int32_t> knn_table(int radius) {
 
 }  // namespace
 
+namespace {
+
+// Per-launch CUDA event pairs, recorded only when profiling is on.
+struct LaunchTimer {
+  bool on = false;
+  cudaStream_t st = 0;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev;
+  ~LaunchTimer() {
+    for (auto &e : ev) {
+      cudaEventDestroy(e.second.first);
+      cudaEventDestroy(e.second.second);
+    }
+  }
+  template <typename F>
+  void run(int kind, F &&f) {
+    if (!on) {
+      f();
+      return;
+    }
+    cudaEvent_t a, b;
+    CUDA_TRY(cudaEventCreate(&a));
+    CUDA_TRY(cudaEventCreate(&b));
+    CUDA_TRY(cudaEventRecord(a, st));
+    f();
+    CUDA_TRY(cudaEventRecord(b, st));
+    ev.push_back({kind, {a, b}});
+  }
+  void collect(ts_run_stats &out) {
+    for (auto &e : ev) {
+      float ms = 0.0f;
+      CUDA_TRY(cudaEventElapsedTime(&ms, e.second.first, e.second.second));
+      out.kernel_count[e.first] += 1;
+      out.kernel_ms[e.first] += ms;
+    }
+  }
+};
+
+}  // namespace
+
 extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user, ts_generated **out) {
   if (!s || !out) return TS_ERR_NULL;
   *out = nullptr;
@@ -895,7 +941,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     DevBuf<uint32_t> d_color, d_occ, d_mir, d_res, d_items, d_ncnt, d_fbl, d_fbc;
     DevBuf<uint4> d_state;
     DevBuf<float> d_rscore, d_lut;
-    DevBuf<double> d_xdiv, d_ydiv;
+    DevBuf<double> d_xdiv, d_ydiv, d_dist, d_dxt, d_dy2t, d_mean, d_minv;
     DevBuf<int32_t> d_tab, d_nbuf;
     DevBuf<uint2> d_rcand;
     DevBuf<Result> d_result;
@@ -915,6 +961,9 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     CUDA_TRY(d_tab.alloc(tab.size()));
     CUDA_TRY(d_nbuf.alloc((size_t)max_batch_items * std::max<uint32_t>(k, 1)));
     CUDA_TRY(d_ncnt.alloc(max_batch_items));
+    CUDA_TRY(d_dist.alloc((size_t)max_batch_items * std::max<uint32_t>(k, 1)));
+    CUDA_TRY(d_mean.alloc(max_batch_items));
+    CUDA_TRY(d_minv.alloc(max_batch_items));
     CUDA_TRY(d_fbl.alloc(max_batch_items));
     CUDA_TRY(d_fbc.alloc(n_batches));
     CUDA_TRY(d_result.alloc(max_batch_items));
@@ -928,6 +977,21 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     for (size_t i = 0; i < ydiv.size(); ++i) ydiv[i] = (double)((int64_t)i - yo) / (double)H;
     CUDA_TRY(d_xdiv.alloc(xdiv.size()));
     CUDA_TRY(d_ydiv.alloc(ydiv.size()));
+    // per-pixel tables of the normalised offsets the weights use: dx and
+    // dy * dy for |offset| <= kDistTabRadius, the same IEEE operations as
+    // get_distances_to_k_neighs (ms.rs:410-415)
+    const int32_t R = kDistTabRadius;
+    std::vector<double> dxt((size_t)W * (2 * R + 1)), dy2t((size_t)H * (2 * R + 1));
+    for (uint32_t x = 0; x < W; ++x)
+      for (int32_t o = -R; o <= R; ++o)
+        dxt[(size_t)x * (2 * R + 1) + o + R] = (double)((int64_t)x + o) / (double)W - (double)x / (double)W;
+    for (uint32_t y = 0; y < H; ++y)
+      for (int32_t o = -R; o <= R; ++o) {
+        const double dy = (double)((int64_t)y + o) / (double)H - (double)y / (double)H;
+        dy2t[(size_t)y * (2 * R + 1) + o + R] = dy * dy;
+      }
+    CUDA_TRY(d_dxt.alloc(dxt.size()));
+    CUDA_TRY(d_dy2t.alloc(dy2t.size()));
     // the tree is rebuilt from the resolved list, mirrors included (ms.rs:747-779)
     std::vector<uint32_t> occ((size_t)wpr * H, 0), mir((size_t)wpr * H, 0);
     for (size_t i = 0; i < locked; ++i) {
@@ -958,6 +1022,8 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     CUDA_TRY(cudaMemcpyAsync(d_tab.p, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_xdiv.p, xdiv.data(), xdiv.size() * 8, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_ydiv.p, ydiv.data(), ydiv.size() * 8, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_dxt.p, dxt.data(), dxt.size() * 8, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_dy2t.p, dy2t.data(), dy2t.size() * 8, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemsetAsync(d_fbc.p, 0, n_batches * 4, st));
     CUDA_TRY(cudaMemsetAsync(d_err.p, 0, sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(d_evals.p, 0, sizeof(unsigned long long), st));
@@ -977,6 +1043,9 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     sd.ydiv = d_ydiv.p;
     sd.xdiv_off = xo;
     sd.ydiv_off = yo;
+    sd.dxt = d_dxt.p;
+    sd.dy2t = d_dy2t.p;
+    sd.dtab_r = R;
     sd.color = d_color.p;
     sd.state = d_state.p;
     sd.occ = d_occ.p;
@@ -998,6 +1067,9 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     sd.k = k;
     sd.m = m;
     uint64_t launches = 0, batches = 0, resolves = 0;
+    LaunchTimer lt;
+    lt.on = p.profile;
+    lt.st = st;
     size_t fb_index = 0;
     uint64_t overall_total = 0, overall_current = 0;
     for (auto &sp : plan) overall_total += sp.n_items;
@@ -1005,7 +1077,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     for (size_t si = 0; si < plan.size(); ++si) {
       const StagePlan &sp = plan[si];
       if (sp.level_switch) {
-        launch_level_switch(sd, sp.level, sp.n_res_start, st);
+        lt.run(TS_KERNEL_LEVEL_SWITCH, [&] { launch_level_switch(sd, sp.level, sp.n_res_start, st); });
         ++launches;
       }
       StageDev sdv{};
@@ -1028,7 +1100,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
         chunk.stage_seed = sp.seed + c0;  // item i's stream is seeded with stage_seed + i + 1
         chunk.rcand = d_rcand.p;
         chunk.redo = sp.redo > c0 ? sp.redo - c0 : 0;
-        launch_random_candidates(sd, chunk, st);
+        lt.run(TS_KERNEL_RANDOM_CANDIDATES, [&] { launch_random_candidates(sd, chunk, st); });
         ++launches;
         chunk.stage_seed = sp.seed;  // resolve_at_random uses the stage seed itself
         for (size_t bk = bi; bk < bj; ++bk) {
@@ -1042,19 +1114,26 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
           bd.ncnt = d_ncnt.p;
           bd.fb_list = d_fbl.p;
           bd.fb_count = d_fbc.p + fb_index++;
+          bd.dist = d_dist.p;
+          bd.mean = d_mean.p;
+          bd.minv = d_minv.p;
           bd.res = d_result.p;
           if (k > 0) {
             if (bp.exhaustive) {
-              launch_knn_exhaustive(sd, chunk, bd, true, st);
+              lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, chunk, bd, true, st); });
               ++launches;
             } else {
-              launch_knn_walk(sd, chunk, bd, st);
-              launch_knn_exhaustive(sd, chunk, bd, false, st);
+              lt.run(TS_KERNEL_KNN_WALK, [&] { launch_knn_walk(sd, chunk, bd, st); });
+              lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, chunk, bd, false, st); });
               launches += 2;
             }
           }
-          launch_resolve(sd, chunk, bd, st);
-          launch_commit(sd, chunk, bd, st);
+          if (k > 0) {
+            lt.run(TS_KERNEL_MEAN, [&] { launch_mean(sd, chunk, bd, st); });
+            ++launches;
+          }
+          lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve(sd, chunk, bd, st); });
+          lt.run(TS_KERNEL_COMMIT, [&] { launch_commit(sd, chunk, bd, st); });
           launches += 2;
           ++batches;
           resolves += bp.i1 - bp.i0;
@@ -1117,6 +1196,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     g->stats.stages = plan.size();
     g->stats.kernel_launches = launches;
     g->stats.gpu_ms = ms;
+    lt.collect(g->stats);
     g->stats.cost_evals = evals;
   } catch (const Failure &f) {
     s->err = f.msg;
