@@ -196,6 +196,10 @@ int ts_builder_max_thread_count(ts_builder *b, uint64_t count);
  * 0 gives batches of one item, the reference's single-thread semantics.
  * max_batch caps a batch (0 = no cap). */
 int ts_builder_batch_schedule(ts_builder *b, uint32_t batch_divisor, uint32_t max_batch);
+/* Batches of at most `team_max_batch` work items resolve with one CTA per
+ * item (lowest latency); larger batches with one warp per item (highest
+ * throughput).  Both give identical results. */
+int ts_builder_resolve_team(ts_builder *b, uint32_t team_max_batch);
 /* CUDA device ordinal (default 0). */
 int ts_builder_device(ts_builder *b, int32_t device);
 /* Time every kernel launch of run() with CUDA events (adds host overhead;

@@ -113,6 +113,7 @@ SIGNATURES = {
     "ts_builder_batch_schedule": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
     "ts_builder_device": (C.c_int, [C.c_void_p, C.c_int32]),
     "ts_builder_profile_kernels": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ts_builder_resolve_team": (C.c_int, [C.c_void_p, C.c_uint32]),
     "ts_builder_build": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "ts_session_run": (C.c_int, [C.c_void_p, _PROGRESS_FN, C.c_void_p, C.POINTER(C.c_void_p)]),
     "ts_session_free": (None, [C.c_void_p]),
@@ -327,6 +328,11 @@ class SessionBuilder:
     def device(self, ordinal):
         return self._check(lib().ts_builder_device(self._h, int(ordinal)))
 
+    def resolve_team(self, max_batch):
+        """Batches of at most max_batch items resolve with one CTA per item;
+        larger ones with one warp per item (identical results)."""
+        return self._check(lib().ts_builder_resolve_team(self._h, int(max_batch)))
+
     def profile_kernels(self, on=True):
         """Time every kernel launch with CUDA events (measurement runs)."""
         return self._check(lib().ts_builder_profile_kernels(self._h, 1 if on else 0))
@@ -418,7 +424,7 @@ class GeneratedImage:
         return st.as_dict()
 
 
-def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0, profile=False):
+def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0, profile=False, team_max_batch=None):
     """A SessionBuilder for a workload spec dict (see workloads.py)."""
     p = spec["params"]
     b = Session.builder()
@@ -450,12 +456,14 @@ def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0, profile=Fals
     b.batch_schedule(batch_divisor, max_batch).device(device)
     if profile:
         b.profile_kernels(True)
+    if team_max_batch is not None:
+        b.resolve_team(team_max_batch)
     return b
 
 
-def run_spec(spec, batch_divisor=8, max_batch=0, device=0):
+def run_spec(spec, batch_divisor=8, max_batch=0, device=0, team_max_batch=None):
     """Build and run a workload spec; returns a dict shaped like the oracle's."""
-    g = builder_from_spec(spec, batch_divisor, max_batch, device).build().run()
+    g = builder_from_spec(spec, batch_divisor, max_batch, device, team_max_batch=team_max_batch).build().run()
     flat, score = g.resolved()
     st = g.stats()
     return {"image": g.into_image(), "coord": g.coord_map(), "id": g.id_map(), "resolved": flat,

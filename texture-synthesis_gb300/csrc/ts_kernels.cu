@@ -32,6 +32,8 @@
 #include <float.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "ts_common.h"
 #include "ts_kernels.cuh"
 
@@ -43,6 +45,7 @@ constexpr int kWarp = 32;
 constexpr int kResolveWarps = 4;
 constexpr int kWalkWarps = 8;
 constexpr int kExhThreads = 256;
+constexpr int kTeamThreads = 128;
 constexpr int kExhCap = 2048;  // keys kept by the exhaustive k-NN at the cut distance
 constexpr uint32_t kMaxDraws = 1u << 22;
 
@@ -379,10 +382,11 @@ __global__ void __launch_bounds__(128) k_mean(SessionDev s, StageDev st, BatchDe
 // ---------------------------------------------------------------------------
 // resolve: warp per item.
 // ---------------------------------------------------------------------------
+// Per-warp shared memory: one 16-byte record per neighbour
+// {offset, own pattern texel, target-guide texel, weight bits}, then the
+// candidates {x | y<<16} and {map | neg flag | source index << 16}.
 struct WarpSmem {
-  int32_t *nb;
-  uint32_t *pat, *gpat;
-  float *wt;
+  uint4 *nbr;
   uint32_t *cxy, *caux;
 };
 
@@ -390,8 +394,7 @@ __device__ __forceinline__ size_t align16(size_t v) { return (v + 15) & ~(size_t
 
 __host__ __device__ __forceinline__ size_t warp_smem_bytes(uint32_t k, uint32_t m) {
   const size_t kk = k ? k : 1;
-  size_t b = 0;
-  b += ((kk * 4 + 15) & ~(size_t)15) * 4;        // nb, pat, gpat, wt
+  size_t b = kk * 16;                            // nbr
   b += (((kk + m) * 4 + 15) & ~(size_t)15) * 2;  // cxy, caux
   return b;
 }
@@ -400,14 +403,8 @@ __device__ __forceinline__ WarpSmem carve(unsigned char *base, uint32_t k, uint3
   const size_t kk = k ? k : 1;
   WarpSmem w;
   unsigned char *p = base;
-  w.nb = (int32_t *)p;
-  p += align16(kk * 4);
-  w.pat = (uint32_t *)p;
-  p += align16(kk * 4);
-  w.gpat = (uint32_t *)p;
-  p += align16(kk * 4);
-  w.wt = (float *)p;
-  p += align16(kk * 4);
+  w.nbr = (uint4 *)p;
+  p += kk * 16;
   w.cxy = (uint32_t *)p;
   p += align16((kk + m) * 4);
   w.caux = (uint32_t *)p;
@@ -421,7 +418,7 @@ __device__ __forceinline__ uint32_t texel(const uint32_t *lv, const MapDesc &md,
   return kOutside;
 }
 
-// Sum of the four channel LUT terms in channel order, starting from zero.
+// Sum of the four channel LUT terms in channel order, starting from acc.
 __device__ __forceinline__ float lut4(const float *lut, uint32_t d, float acc) {
   acc = __fadd_rn(acc, lut[d & 255u]);
   acc = __fadd_rn(acc, lut[(d >> 8) & 255u]);
@@ -431,7 +428,8 @@ __device__ __forceinline__ float lut4(const float *lut, uint32_t d, float acc) {
 }
 
 // Cost of candidate c (better_match, ms.rs:1225-1288), abandoning as soon as
-// the partial sum reaches `bound`.  Returns false when abandoned.
+// the partial sum reaches `bound`; bounds-checked gathers.  Returns false
+// when abandoned.
 __device__ __forceinline__ bool candidate_cost(const SessionDev &s, const StageDev &st, const WarpSmem &w,
                                                const float *lc, const float *lg, uint32_t nk, uint32_t cxy,
                                                uint32_t aux, float bound, float &out) {
@@ -448,28 +446,238 @@ __device__ __forceinline__ bool candidate_cost(const SessionDev &s, const StageD
   }
   float score = 0.0f;
   for (uint32_t j = 0; j < nk; ++j) {
-    const int32_t off = w.nb[j];
-    int dx = off_dx(off), dy = off_dy(off);
+    const uint4 nr = w.nbr[j];
+    int dx = off_dx((int32_t)nr.x), dy = off_dy((int32_t)nr.x);
     if (neg) {
       dx = -dx;
       dy = -dy;
     }
     const int qx = cx + dx, qy = cy + dy;
     const uint32_t t = texel(lv, md, qx, qy);
-    float nps = lut4(lc, __vabsdiffu4(w.pat[j], t), 0.0f);
+    float nps = lut4(lc, __vabsdiffu4(nr.y, t), 0.0f);
     if (s.guided) {
       uint32_t gt = kOutside;
       if ((unsigned)qx < gd.w && (unsigned)qy < gd.h) gt = __ldg(&gv[(size_t)qy * gd.w + qx]);
-      nps = lut4(lg, __vabsdiffu4(w.gpat[j], gt), nps);
+      nps = lut4(lg, __vabsdiffu4(nr.z, gt), nps);
     }
-    score = __fadd_rn(score, __fmul_rn(nps, w.wt[j]));
+    score = __fadd_rn(score, __fmul_rn(nps, __uint_as_float(nr.w)));
     if (score >= bound) return false;
   }
   out = score;
   return true;
 }
 
-__global__ void __launch_bounds__(kResolveWarps *kWarp) k_resolve(SessionDev s, StageDev st, BatchDev b) {
+// The same on the padded images, for items whose neighbour offsets all lie
+// within kPad: no bounds checks, gathers issued four neighbours ahead.
+template <bool kGuided>
+__device__ __forceinline__ bool candidate_cost_padded(const SessionDev &s, const StageDev &st, const WarpSmem &w,
+                                                      const float *lc, const float *lg, uint32_t nk, uint32_t cxy,
+                                                      uint32_t aux, float bound, float &out) {
+  const uint32_t map = aux & 0x7fffu;
+  const int sg = (aux & kAuxNeg) ? -1 : 1;
+  const MapDesc md = s.maps[map];
+  const int cx = (int)(cxy & 0xffffu), cy = (int)(cxy >> 16);
+  const int pw = (int)md.pw;
+  const uint32_t *base = s.plevels + md.poff + (size_t)st.level * md.pw * md.ph +
+                         (size_t)(cy + kPad) * md.pw + (cx + kPad);
+  const uint32_t *gbase = nullptr;
+  if (kGuided) {
+    const GuideDesc gd = s.gdesc[map];
+    gbase = s.pguides + gd.poff + (size_t)st.level * gd.pw * gd.ph + (size_t)(cy + kPad) * gd.pw + (cx + kPad);
+  }
+  float score = 0.0f;
+  uint32_t j = 0;
+  for (; j + 4 <= nk; j += 4) {
+    uint4 nr[4];
+    uint32_t t[4], gt[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      nr[u] = w.nbr[j + u];
+      const int lin = sg * (off_dy((int32_t)nr[u].x) * pw + off_dx((int32_t)nr[u].x));
+      t[u] = __ldg(base + lin);
+      if (kGuided) gt[u] = __ldg(gbase + lin);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      float nps = lut4(lc, __vabsdiffu4(nr[u].y, t[u]), 0.0f);
+      if (kGuided) nps = lut4(lg, __vabsdiffu4(nr[u].z, gt[u]), nps);
+      score = __fadd_rn(score, __fmul_rn(nps, __uint_as_float(nr[u].w)));
+      if (score >= bound) return false;
+    }
+  }
+  for (; j < nk; ++j) {
+    const uint4 nr = w.nbr[j];
+    const int lin = sg * (off_dy((int32_t)nr.x) * pw + off_dx((int32_t)nr.x));
+    float nps = lut4(lc, __vabsdiffu4(nr.y, __ldg(base + lin)), 0.0f);
+    if (kGuided) nps = lut4(lg, __vabsdiffu4(nr.z, __ldg(gbase + lin)), nps);
+    score = __fadd_rn(score, __fmul_rn(nps, __uint_as_float(nr.w)));
+    if (score >= bound) return false;
+  }
+  out = score;
+  return true;
+}
+
+// Per-neighbour set-up of an item: weight (find_best_match, ms.rs:1198-1203,
+// w = (f32) exp(-(d / mean))), own pattern texel and target-guide texel
+// (ms.rs:1151-1181, wrapped when tiling), the record in shared memory, and
+// the neighbour's coherence candidate (ms.rs:497-547): its source plus the
+// shift to the centre, kept if valid.  Returns true for a valid candidate.
+__device__ __forceinline__ bool neighbour_setup(const SessionDev &s, const StageDev &st, const BatchDev &b,
+                                                uint32_t local, uint32_t nb, int px, int py, uint32_t j, int32_t off,
+                                                double avg, double inv, const double *tab, const float *tab_ff,
+                                                const WarpSmem &w, uint32_t &cxy, uint32_t &aux, bool &nan_w,
+                                                int &maxoff, bool &bad_map) {
+  const int W = (int)s.W, H = (int)s.H;
+  const double dj = b.dist[(size_t)j * nb + local];
+  float wv;
+  if (!ts_weight_ff(dj, avg, tab_ff, wv)) wv = __double2float_rn(ts_exp64(-1.0 * ts_div_markstein(dj, avg, inv), tab));
+  nan_w |= (wv != wv);
+  maxoff = max(maxoff, max(abs(off_dx(off)), abs(off_dy(off))));
+  const int nx = px + off_dx(off), ny = py + off_dy(off);
+  int qx = nx, qy = ny;
+  if (s.tiling) {
+    qx = modi(nx, W);
+    qy = modi(ny, H);
+  }
+  const bool inb = (unsigned)qx < s.W && (unsigned)qy < s.H;
+  const uint32_t pat = inb ? s.color[(size_t)qy * s.W + qx] : kOutside;
+  uint32_t gpat = 0;
+  if (s.guided) gpat = inb ? __ldg(&s.tguide[(size_t)st.level * s.W * s.H + (size_t)qy * s.W + qx]) : kOutside;
+  w.nbr[j] = make_uint4((uint32_t)off, pat, gpat, __float_as_uint(wv));
+  const int wx = modi(nx, W), wy = modi(ny, H);
+  const uint4 sv = s.state[(size_t)wy * s.W + wx];
+  const uint32_t map = sv.z;
+  if (map >= s.n_maps) {
+    bad_map = true;
+    return false;
+  }
+  const int ccx = (int)(sv.x & 0xffffu) + (px - nx);
+  const int ccy = (int)(sv.x >> 16) + (py - ny);
+  if (!coord_valid(s, s.maps[map], ccx, ccy)) return false;
+  cxy = (uint32_t)ccx | ((uint32_t)ccy << 16);
+  aux = map | (j << 16);
+  return true;
+}
+
+// The reference's sequential find_best_match (ms.rs:1184-1221), for stages or
+// items with non-finite costs, where early exit and argmin need its exact
+// comparison sequence.  One thread.
+__device__ void sequential_best(const SessionDev &s, const StageDev &st, const WarpSmem &w, const float *lc,
+                                const float *lg, uint32_t nk, uint32_t nc, float &best_s, uint32_t &best_i) {
+  best_s = FLT_MAX;
+  best_i = 0;
+  for (uint32_t c = 0; c < nc; ++c) {
+    const uint32_t aux = w.caux[c];
+    const uint32_t map = aux & 0x7fffu;
+    const bool neg = (aux & kAuxNeg) != 0;
+    const MapDesc md = s.maps[map];
+    const uint32_t *lv = s.levels + md.off + (size_t)st.level * md.w * md.h;
+    const int cx = (int)(w.cxy[c] & 0xffffu), cy = (int)(w.cxy[c] >> 16);
+    float score = 0.0f;
+    bool better = true;
+    for (uint32_t j = 0; j < nk; ++j) {
+      const uint4 nr = w.nbr[j];
+      int dx = off_dx((int32_t)nr.x), dy = off_dy((int32_t)nr.x);
+      if (neg) {
+        dx = -dx;
+        dy = -dy;
+      }
+      const int qx = cx + dx, qy = cy + dy;
+      float nps = lut4(lc, __vabsdiffu4(nr.y, texel(lv, md, qx, qy)), 0.0f);
+      if (s.guided) {
+        const GuideDesc gd = s.gdesc[map];
+        const uint32_t *gv = s.guides + gd.off + (size_t)st.level * gd.w * gd.h;
+        uint32_t gt = kOutside;
+        if ((unsigned)qx < gd.w && (unsigned)qy < gd.h) gt = gv[(size_t)qy * gd.w + qx];
+        nps = lut4(lg, __vabsdiffu4(nr.z, gt), nps);
+      }
+      score = __fadd_rn(score, __fmul_rn(nps, __uint_as_float(nr.w)));
+      if (score >= best_s) {
+        better = false;
+        break;
+      }
+    }
+    if (better) {
+      best_s = score;
+      best_i = c;
+    }
+  }
+}
+
+// The winning candidate as an update (ms.rs:976-1001): source coordinate and
+// map, patch id (the neighbour's for coherence candidates, the example flat
+// index for random ones), score.
+__device__ void write_result(const SessionDev &s, const WarpSmem &w, const BatchDev &b, uint32_t local,
+                             uint32_t pixel, int px, int py, bool is_new, uint32_t nc, float best_s,
+                             uint32_t best_i) {
+  const uint32_t aux = w.caux[best_i];
+  const uint32_t map = aux & 0x7fffu;
+  const uint32_t cxy = w.cxy[best_i];
+  uint32_t idp;
+  if (aux & kAuxNeg) {
+    idp = (cxy >> 16) * s.maps[map].w + (cxy & 0xffffu);
+  } else {
+    const uint32_t j = aux >> 16;
+    const int32_t off = (int32_t)w.nbr[j].x;
+    const int wx = modi(px + off_dx(off), (int)s.W), wy = modi(py + off_dy(off), (int)s.H);
+    idp = s.state[(size_t)wy * s.W + wx].y;
+  }
+  Result r;
+  r.pixel = pixel;
+  r.srcxy = cxy;
+  r.idp = idp;
+  r.idm = map;
+  r.cmap = map;
+  r.flags = (is_new ? kResAppend : 0u) | kResMirrors;
+  r.score = best_s;
+  r.ncand = nc;
+  b.res[local] = r;
+}
+
+// Result for an item with no resolved neighbour: resolve_at_random with the
+// stage seed, appended without tiling mirrors (ms.rs:1002-1010, 473).
+__device__ void write_random_result(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
+                                    uint32_t pixel) {
+  Pcg32 g = pcg_from_u64(st.stage_seed);
+  uint64_t map64 = 0;
+  uint32_t x = 0, y = 0;
+  bool ok = gen_range_u64_bounded(g, s.n_maps, 256, map64);
+  const uint32_t map = ok ? (uint32_t)map64 : 0u;
+  const MapDesc md = s.maps[map];
+  g = pcg_from_u64(st.stage_seed);
+  ok = ok && gen_range_u32_bounded(g, md.w, 256, x);
+  g = pcg_from_u64(st.stage_seed);
+  ok = ok && gen_range_u32_bounded(g, md.h, 256, y);
+  if (!ok) set_err(s.err, kDevErrNoSample);
+  Result r;
+  r.pixel = pixel;
+  r.srcxy = x | (y << 16);
+  r.idp = pixel;
+  r.idm = map;
+  r.cmap = map;
+  r.flags = kResAppend;
+  r.score = 0.0f;
+  r.ncand = 0;
+  b.res[local] = r;
+}
+
+// A result that commit skips (an invalid map id was met; the reference
+// panics there).
+__device__ void write_bad_result(const SessionDev &s, const BatchDev &b, uint32_t local, uint32_t pixel) {
+  set_err(s.err, kDevErrIndex);
+  Result r;
+  r.pixel = pixel;
+  r.srcxy = 0;
+  r.idp = 0;
+  r.idm = 0;
+  r.cmap = 0xffffffffu;
+  r.flags = 0;
+  r.score = 0.0f;
+  r.ncand = 0;
+  b.res[local] = r;
+}
+
+__global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve(SessionDev s, StageDev st, BatchDev b) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double tab[64];
   __shared__ float tab_ff[128];
@@ -496,76 +704,23 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp) k_resolve(SessionDev s, 
     if (nk == 0) {
       // no resolved neighbours: resolve_at_random with the stage seed, kept
       // in the resolved list without tiling mirrors (ms.rs:1002-1010, 473)
-      if (lane == 0) {
-        Pcg32 g = pcg_from_u64(st.stage_seed);
-        uint64_t map64 = 0;
-        uint32_t x = 0, y = 0;
-        bool ok = gen_range_u64_bounded(g, s.n_maps, 256, map64);
-        const uint32_t map = ok ? (uint32_t)map64 : 0u;
-        const MapDesc md = s.maps[map];
-        g = pcg_from_u64(st.stage_seed);
-        ok = ok && gen_range_u32_bounded(g, md.w, 256, x);
-        g = pcg_from_u64(st.stage_seed);
-        ok = ok && gen_range_u32_bounded(g, md.h, 256, y);
-        if (!ok) set_err(s.err, kDevErrNoSample);
-        r.srcxy = x | (y << 16);
-        r.idp = pixel;
-        r.idm = map;
-        r.cmap = map;
-        r.flags = kResAppend;
-        r.score = 0.0f;
-        b.res[local] = r;
-      }
+      if (lane == 0) write_random_result(s, st, b, local, pixel);
       continue;
     }
     const int32_t *nbo = b.nbuf + (size_t)local * s.k;
     const double avg = b.mean[local], inv = b.minv[local];
     // neighbours: offsets, weights, own pattern, coherence candidates
     bool nan_w = false;
+    int maxoff = 0;
     uint32_t ncoh = 0;
     bool bad_map = false;
     for (uint32_t j0 = 0; j0 < nk; j0 += kWarp) {
       const uint32_t j = j0 + lane;
       bool valid = false;
       uint32_t cxy = 0, aux = 0;
-      if (j < nk) {
-        const int32_t off = nbo[j];
-        w.nb[j] = off;
-        // weight (find_best_match, ms.rs:1198-1203): w = (f32) exp(-(d / mean))
-        const double dj = b.dist[(size_t)j * nb + local];
-        float wv;
-        if (!ts_weight_ff(dj, avg, tab_ff, wv))
-          wv = __double2float_rn(ts_exp64(-1.0 * ts_div_markstein(dj, avg, inv), tab));
-        w.wt[j] = wv;
-        nan_w |= (wv != wv);
-        const int nx = px + off_dx(off), ny = py + off_dy(off);
-        int qx = nx, qy = ny;
-        if (s.tiling) {
-          qx = modi(nx, W);
-          qy = modi(ny, H);
-        }
-        w.pat[j] = ((unsigned)qx < s.W && (unsigned)qy < s.H) ? s.color[(size_t)qy * s.W + qx] : kOutside;
-        if (s.guided) {
-          w.gpat[j] = ((unsigned)qx < s.W && (unsigned)qy < s.H) ? __ldg(&s.tguide[(size_t)st.level * s.W * s.H +
-                                                                                   (size_t)qy * s.W + qx])
-                                                                  : kOutside;
-        }
-        const int wx = modi(nx, W), wy = modi(ny, H);
-        const uint4 sv = s.state[(size_t)wy * s.W + wx];
-        const uint32_t map = sv.z;
-        if (map >= s.n_maps) {
-          bad_map = true;
-        } else {
-          const int ccx = (int)(sv.x & 0xffffu) + (px - nx);
-          const int ccy = (int)(sv.x >> 16) + (py - ny);
-          const MapDesc md = s.maps[map];
-          if (coord_valid(s, md, ccx, ccy)) {
-            valid = true;
-            cxy = (uint32_t)ccx | ((uint32_t)ccy << 16);
-            aux = map | (j << 16);
-          }
-        }
-      }
+      if (j < nk)
+        valid = neighbour_setup(s, st, b, local, nb, px, py, j, nbo[j], avg, inv, tab, tab_ff, w, cxy, aux, nan_w,
+                                maxoff, bad_map);
       const uint32_t bal = __ballot_sync(0xffffffffu, valid);
       if (valid) {
         const uint32_t slot = ncoh + __popc(bal & lt);
@@ -577,16 +732,7 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp) k_resolve(SessionDev s, 
     if (__any_sync(0xffffffffu, bad_map)) {
       // the reference panics on this index; record the error and leave the
       // pixel untouched (commit skips results with an invalid map)
-      if (lane == 0) {
-        set_err(s.err, kDevErrIndex);
-        r.srcxy = 0;
-        r.idp = 0;
-        r.idm = 0;
-        r.cmap = 0xffffffffu;
-        r.flags = 0;
-        r.score = 0.0f;
-        b.res[local] = r;
-      }
+      if (lane == 0) write_bad_result(s, b, local, pixel);
       continue;
     }
     // random candidates after the coherence ones
@@ -597,6 +743,9 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp) k_resolve(SessionDev s, 
       w.caux[ncoh + t] = v.y | kAuxNeg | (t << 16);
     }
     const bool slow = st.slow_lut || __any_sync(0xffffffffu, nan_w);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) maxoff = max(maxoff, __shfl_xor_sync(0xffffffffu, maxoff, o));
+    const bool padded = maxoff <= kPad && !s.guide_dims_differ;
     __syncwarp();
     const uint32_t nc = ncoh + s.m;
     float best_s = FLT_MAX;
@@ -606,7 +755,14 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp) k_resolve(SessionDev s, 
         const uint32_t c = base + lane;
         float sc = 0.0f;
         bool alive = false;
-        if (c < nc) alive = candidate_cost(s, st, w, lc, lg, nk, w.cxy[c], w.caux[c], best_s, sc);
+        if (c < nc) {
+          if (!padded)
+            alive = candidate_cost(s, st, w, lc, lg, nk, w.cxy[c], w.caux[c], best_s, sc);
+          else if (s.guided)
+            alive = candidate_cost_padded<true>(s, st, w, lc, lg, nk, w.cxy[c], w.caux[c], best_s, sc);
+          else
+            alive = candidate_cost_padded<false>(s, st, w, lc, lg, nk, w.cxy[c], w.caux[c], best_s, sc);
+        }
         float v = alive ? sc : __int_as_float(0x7f800000);
         uint32_t idx = alive ? c : 0xffffffffu;
 #pragma unroll
@@ -624,65 +780,189 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp) k_resolve(SessionDev s, 
         }
       }
     } else if (lane == 0) {
-      // the reference's sequential find_best_match, for non-finite costs
-      for (uint32_t c = 0; c < nc; ++c) {
-        const uint32_t aux = w.caux[c];
-        const uint32_t map = aux & 0x7fffu;
-        const bool neg = (aux & kAuxNeg) != 0;
+      sequential_best(s, st, w, lc, lg, nk, nc, best_s, best_i);
+    }
+    if (lane == 0) write_result(s, w, b, local, pixel, px, py, is_new, nc, best_s, best_i);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// resolve, team form: one CTA of T threads per item, one candidate per
+// thread.  Candidate 0's exact score is computed first (its neighbour terms
+// in parallel, their in-order sum on one thread); every other candidate then
+// runs against min(S_0, its thread's earlier results) and stops as soon as
+// its partial sum reaches that bound; a block-wide first-index argmin picks
+// the winner.  The first strict minimum of the reference never stops early
+// (every bound it meets is larger, or equal with a later index), so the
+// result is the reference's.  Latency per item is about one candidate's
+// evaluation, which suits batches too small to fill the GPU with warps.
+// ---------------------------------------------------------------------------
+template <int T>
+__global__ void __launch_bounds__(T) k_resolve_team(SessionDev s, StageDev st, BatchDev b) {
+  constexpr int NW = T / 32;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double tab[64];
+  __shared__ float tab_ff[128];
+  __shared__ uint32_t wcnt[NW];
+  __shared__ float red_s[NW];
+  __shared__ uint32_t red_i[NW];
+  __shared__ int sh_flags, sh_maxoff;
+  __shared__ float sh_s0;
+  float *lc = (float *)smem;
+  float *lg = lc + 256;
+  for (int i = threadIdx.x; i < 512; i += T) lc[i] = st.lut[i];
+  for (int i = threadIdx.x; i < 64; i += T) tab[i] = g_exp2_64[i];
+  for (int i = threadIdx.x; i < 128; i += T) tab_ff[i] = g_exp2_ff[i];
+  const WarpSmem w = carve(smem + 2048, s.k, s.m);
+  float *term = (float *)(smem + 2048 + warp_smem_bytes(s.k, s.m));
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t nb = b.i1 - b.i0;
+  __syncthreads();
+  for (uint32_t local = blockIdx.x; local < nb; local += gridDim.x) {
+    const uint32_t item = b.i0 + local;
+    const uint32_t pixel = st.items[item];
+    const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
+    const bool is_new = item >= st.redo;
+    const uint32_t nk = s.k ? b.ncnt[local] : 0u;
+    if (nk == 0) {
+      if (tid == 0) write_random_result(s, st, b, local, pixel);
+      continue;
+    }
+    if (tid == 0) {
+      sh_flags = 0;
+      sh_maxoff = 0;
+    }
+    __syncthreads();
+    const int32_t *nbo = b.nbuf + (size_t)local * s.k;
+    const double avg = b.mean[local], inv = b.minv[local];
+    bool nan_w = false, bad_map = false;
+    int maxoff = 0;
+    uint32_t ncoh = 0;
+    for (uint32_t j0 = 0; j0 < nk; j0 += T) {
+      const uint32_t j = j0 + tid;
+      bool valid = false;
+      uint32_t cxy = 0, aux = 0;
+      if (j < nk)
+        valid = neighbour_setup(s, st, b, local, nb, px, py, j, nbo[j], avg, inv, tab, tab_ff, w, cxy, aux, nan_w,
+                                maxoff, bad_map);
+      // order-preserving compaction of the valid coherence candidates
+      const uint32_t bal = __ballot_sync(0xffffffffu, valid);
+      if (lane == 0) wcnt[warp] = __popc(bal);
+      __syncthreads();
+      uint32_t base = ncoh, total = 0;
+#pragma unroll
+      for (int i = 0; i < NW; ++i) {
+        if (i < warp) base += wcnt[i];
+        total += wcnt[i];
+      }
+      if (valid) {
+        const uint32_t slot = base + __popc(bal & lt);
+        w.cxy[slot] = cxy;
+        w.caux[slot] = aux;
+      }
+      ncoh += total;
+      __syncthreads();
+    }
+    if (nan_w) atomicOr(&sh_flags, 1);
+    if (bad_map) atomicOr(&sh_flags, 2);
+    if (maxoff) atomicMax(&sh_maxoff, maxoff);
+    const uint2 *rc = st.rcand + (size_t)item * s.m;
+    for (uint32_t t = tid; t < s.m; t += T) {
+      const uint2 v = rc[t];
+      w.cxy[ncoh + t] = v.x;
+      w.caux[ncoh + t] = v.y | kAuxNeg | (t << 16);
+    }
+    __syncthreads();
+    if (sh_flags & 2) {
+      if (tid == 0) write_bad_result(s, b, local, pixel);
+      __syncthreads();
+      continue;
+    }
+    const bool slow = st.slow_lut || (sh_flags & 1);
+    const bool padded = sh_maxoff <= kPad && !s.guide_dims_differ;
+    const uint32_t nc = ncoh + s.m;
+    float best_s = FLT_MAX;
+    uint32_t best_i = 0;
+    if (!slow) {
+      // S_0: candidate 0's terms nps_j * w_j in parallel, summed in order
+      {
+        const uint32_t cxy0 = w.cxy[0], aux0 = w.caux[0];
+        const uint32_t map = aux0 & 0x7fffu;
+        const bool neg = (aux0 & kAuxNeg) != 0;
         const MapDesc md = s.maps[map];
         const uint32_t *lv = s.levels + md.off + (size_t)st.level * md.w * md.h;
-        const int cx = (int)(w.cxy[c] & 0xffffu), cy = (int)(w.cxy[c] >> 16);
-        float score = 0.0f;
-        bool better = true;
-        for (uint32_t j = 0; j < nk; ++j) {
-          int dx = off_dx(w.nb[j]), dy = off_dy(w.nb[j]);
+        const int cx = (int)(cxy0 & 0xffffu), cy = (int)(cxy0 >> 16);
+        for (uint32_t j = tid; j < nk; j += T) {
+          const uint4 nr = w.nbr[j];
+          int dx = off_dx((int32_t)nr.x), dy = off_dy((int32_t)nr.x);
           if (neg) {
             dx = -dx;
             dy = -dy;
           }
           const int qx = cx + dx, qy = cy + dy;
-          float nps = lut4(lc, __vabsdiffu4(w.pat[j], texel(lv, md, qx, qy)), 0.0f);
+          float nps = lut4(lc, __vabsdiffu4(nr.y, texel(lv, md, qx, qy)), 0.0f);
           if (s.guided) {
             const GuideDesc gd = s.gdesc[map];
             const uint32_t *gv = s.guides + gd.off + (size_t)st.level * gd.w * gd.h;
             uint32_t gt = kOutside;
-            if ((unsigned)qx < gd.w && (unsigned)qy < gd.h) gt = gv[(size_t)qy * gd.w + qx];
-            nps = lut4(lg, __vabsdiffu4(w.gpat[j], gt), nps);
+            if ((unsigned)qx < gd.w && (unsigned)qy < gd.h) gt = __ldg(&gv[(size_t)qy * gd.w + qx]);
+            nps = lut4(lg, __vabsdiffu4(nr.z, gt), nps);
           }
-          score = __fadd_rn(score, __fmul_rn(nps, w.wt[j]));
-          if (score >= best_s) {
-            better = false;
-            break;
-          }
+          term[j] = __fmul_rn(nps, __uint_as_float(nr.w));
         }
-        if (better) {
-          best_s = score;
-          best_i = c;
+        __syncthreads();
+        if (tid == 0) {
+          float sc = 0.0f;
+          for (uint32_t j = 0; j < nk; ++j) sc = __fadd_rn(sc, term[j]);
+          sh_s0 = sc;
+        }
+        __syncthreads();
+      }
+      float my_s = sh_s0;
+      uint32_t my_i = 0;
+      for (uint32_t c = 1 + tid; c < nc; c += T) {
+        float sc;
+        bool alive;
+        if (!padded)
+          alive = candidate_cost(s, st, w, lc, lg, nk, w.cxy[c], w.caux[c], my_s, sc);
+        else if (s.guided)
+          alive = candidate_cost_padded<true>(s, st, w, lc, lg, nk, w.cxy[c], w.caux[c], my_s, sc);
+        else
+          alive = candidate_cost_padded<false>(s, st, w, lc, lg, nk, w.cxy[c], w.caux[c], my_s, sc);
+        if (alive) {
+          my_s = sc;
+          my_i = c;
         }
       }
-    }
-    if (lane == 0) {
-      const uint32_t aux = w.caux[best_i];
-      const uint32_t map = aux & 0x7fffu;
-      const uint32_t cxy = w.cxy[best_i];
-      uint32_t idp;
-      if (aux & kAuxNeg) {
-        idp = (cxy >> 16) * s.maps[map].w + (cxy & 0xffffu);
-      } else {
-        const uint32_t j = aux >> 16;
-        const int32_t off = w.nb[j];
-        const int wx = modi(px + off_dx(off), W), wy = modi(py + off_dy(off), H);
-        idp = s.state[(size_t)wy * s.W + wx].y;
+      // first index of the minimum over the block
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, my_s, o);
+        const uint32_t oi = __shfl_xor_sync(0xffffffffu, my_i, o);
+        if (ov < my_s || (ov == my_s && oi < my_i)) {
+          my_s = ov;
+          my_i = oi;
+        }
       }
-      r.srcxy = cxy;
-      r.idp = idp;
-      r.idm = map;
-      r.cmap = map;
-      r.flags = (is_new ? kResAppend : 0u) | kResMirrors;
-      r.score = best_s;
-      r.ncand = nc;
-      b.res[local] = r;
+      if (lane == 0) {
+        red_s[warp] = my_s;
+        red_i[warp] = my_i;
+      }
+      __syncthreads();
+      best_s = red_s[0];
+      best_i = red_i[0];
+      for (int i = 1; i < NW; ++i) {
+        if (red_s[i] < best_s || (red_s[i] == best_s && red_i[i] < best_i)) {
+          best_s = red_s[i];
+          best_i = red_i[i];
+        }
+      }
+    } else if (tid == 0) {
+      sequential_best(s, st, w, lc, lg, nk, nc, best_s, best_i);
     }
+    if (tid == 0) write_result(s, w, b, local, pixel, px, py, is_new, nc, best_s, best_i);
+    __syncthreads();
   }
 }
 
@@ -785,16 +1065,35 @@ __global__ void k_resize_h(const float *tmp, uint32_t w, uint32_t nh, uint8_t *d
   *(uchar4 *)(dst + ((size_t)y * nw + ox) * 4) = o;
 }
 
+// Padded copy: dst[l][y + kPad][x + kPad] = src[l][y][x], border = kOutside.
+__global__ void k_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, uint32_t *dst) {
+  const uint32_t pw = w + 2 * kPad, ph = h + 2 * kPad;
+  const size_t n = (size_t)pw * ph * levels;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t l = i / ((size_t)pw * ph);
+    const uint32_t r = (uint32_t)(i - l * pw * ph);
+    const int y = (int)(r / pw) - kPad, x = (int)(r % pw) - kPad;
+    dst[i] = ((unsigned)x < w && (unsigned)y < h) ? src[l * w * h + (size_t)y * w + x] : kOutside;
+  }
+}
+
 inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
 }  // namespace
 
 size_t resolve_smem_bytes(uint32_t k, uint32_t m, int) { return 2048 + (size_t)kResolveWarps * warp_smem_bytes(k, m); }
+static size_t team_smem_bytes(uint32_t k, uint32_t m) { return 2048 + warp_smem_bytes(k, m) + (size_t)(k ? k : 1) * 4; }
 
 cudaError_t configure_kernels(uint32_t k, uint32_t m) {
   const size_t smem = resolve_smem_bytes(k, m, 0);
-  if (smem <= 48 * 1024) return cudaSuccess;
-  return cudaFuncSetAttribute(k_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  const size_t tsm = team_smem_bytes(k, m);
+  if (tsm > 48 * 1024)
+    return cudaFuncSetAttribute(k_resolve_team<kTeamThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm);
+  return cudaSuccess;
 }
 
 void launch_random_candidates(const SessionDev &s, const StageDev &st, cudaStream_t stream) {
@@ -829,6 +1128,13 @@ void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, 
   k_resolve<<<cdiv(n, kResolveWarps), kResolveWarps * kWarp, smem, stream>>>(s, st, b);
 }
 
+void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
+  const uint32_t n = b.i1 - b.i0;
+  if (n == 0) return;
+  const uint32_t grid = n < 152u * 16u ? n : 152u * 16u;
+  k_resolve_team<kTeamThreads><<<grid, kTeamThreads, team_smem_bytes(s.k, s.m), stream>>>(s, st, b);
+}
+
 void launch_commit(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
   const uint32_t n = b.i1 - b.i0;
   if (n == 0) return;
@@ -838,6 +1144,12 @@ void launch_commit(const SessionDev &s, const StageDev &st, const BatchDev &b, c
 void launch_level_switch(const SessionDev &s, uint32_t level, uint32_t n_res, cudaStream_t stream) {
   if (n_res == 0) return;
   k_level_switch<<<cdiv(n_res, 256), 256, 0, stream>>>(s, level, n_res);
+}
+
+void launch_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, uint32_t *dst, cudaStream_t stream) {
+  const size_t n = (size_t)(w + 2 * kPad) * (h + 2 * kPad) * levels;
+  if (n == 0) return;
+  k_pad<<<(uint32_t)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, stream>>>(src, w, h, levels, dst);
 }
 
 void launch_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uint32_t nh, const uint4 *taps,

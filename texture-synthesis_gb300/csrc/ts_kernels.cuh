@@ -19,15 +19,25 @@
 
 namespace ts {
 
+// Padded level images: each level is also stored with a border of
+// kPad texels of the out-of-bounds colour Rgba(0,0,0,255) (ms.rs:1139-1148),
+// pitch pw = w + 2 kPad, so that a neighbourhood within kPad of an in-bounds
+// centre reads the same values without bounds checks.
+constexpr int kPad = 32;
+
 struct MapDesc {
   uint32_t w, h;
   uint64_t off;      // texel offset of level 0
   int64_t mask_off;  // byte offset in the mask buffer, -1 = every texel valid
+  uint64_t poff;     // texel offset of level 0's padded image (its (-kPad, -kPad) corner)
+  uint32_t pw, ph;   // padded pitch and height
 };
 
 struct GuideDesc {
   uint32_t w, h;
   uint64_t off;
+  uint64_t poff;
+  uint32_t pw, ph;
 };
 
 enum : uint32_t { kResAppend = 1u, kResMirrors = 2u };
@@ -44,6 +54,8 @@ enum : int { kDevOk = 0, kDevErrIndex = 1, kDevErrNoSample = 2, kDevErrLimit = 3
 
 struct SessionDev {
   const uint32_t *levels;
+  const uint32_t *plevels;  // padded copies of levels
+  const uint32_t *pguides;  // padded copies of guides
   const uint8_t *masks;
   const MapDesc *maps;
   uint32_t n_maps;
@@ -71,6 +83,7 @@ struct SessionDev {
   uint32_t knn_tab_n;
   int *err;
   unsigned long long *evals;  // candidate-cost evaluations, summed by commit
+  int guide_dims_differ;  // some example guide differs in size from its map
   uint32_t W, H, wpr;  // wpr: 32-bit words per bitmap row
   int tiling;
   int32_t x_l, x_r, y_b, y_t;
@@ -109,6 +122,7 @@ void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchD
                            cudaStream_t stream);
 void launch_mean(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
 void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
+void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
 void launch_commit(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
 void launch_level_switch(const SessionDev &s, uint32_t level, uint32_t n_res, cudaStream_t stream);
 
@@ -118,6 +132,9 @@ void launch_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uin
                      const float *wts, cudaStream_t stream);
 void launch_resize_h(const float *tmp, uint32_t w, uint32_t nh, uint8_t *dst, uint32_t nw, const uint4 *taps,
                      const float *wts, cudaStream_t stream);
+
+// Padded copy of `levels` images of w x h texels (see kPad).
+void launch_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, uint32_t *dst, cudaStream_t stream);
 
 // Bytes of dynamic shared memory the resolve kernel needs per CTA.
 size_t resolve_smem_bytes(uint32_t k, uint32_t m, int guided);

@@ -84,6 +84,7 @@ struct Params {
   uint32_t max_batch = 0;
   int device = 0;
   bool profile = false;
+  uint32_t team_max_batch = 8192;
 };
 
 std::string fmt_float(float v) {
@@ -246,7 +247,8 @@ struct ts_session {
   uint32_t inpaint_index = 0;
   Image inpaint_colors;
   std::vector<uint8_t> inpaint_mask;         // W*H: 1 = to synthesise
-  DevBuf<uint32_t> levels, guides, tguide;
+  DevBuf<uint32_t> levels, guides, tguide, plevels, pguides;
+  bool guide_dims_differ = false;
   DevBuf<uint8_t> masks;
   DevBuf<MapDesc> d_maps;
   DevBuf<GuideDesc> d_gdesc;
@@ -472,6 +474,11 @@ int ts_builder_device(ts_builder *b, int32_t device) {
   b->prm.device = device;
   return TS_OK;
 }
+int ts_builder_resolve_team(ts_builder *b, uint32_t team_max_batch) {
+  BUILDER_GUARD(b);
+  b->prm.team_max_batch = team_max_batch;
+  return TS_OK;
+}
 int ts_builder_profile_kernels(ts_builder *b, int32_t on) {
   BUILDER_GUARD(b);
   b->prm.profile = on != 0;
@@ -625,7 +632,7 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
       s->inpaint_colors = imgs[s->inpaint_index];
     }
     // filtered maps and their device pyramids
-    uint64_t texels = 0, mask_bytes = 0;
+    uint64_t texels = 0, ptexels = 0, mask_bytes = 0;
     for (uint32_t e = 0; e < s->n_ex; ++e) {
       if (b->examples[e].method == TS_SAMPLE_IGNORE) continue;
       MapDesc md;
@@ -633,7 +640,11 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
       md.h = imgs[e].h;
       md.off = texels;
       md.mask_off = -1;
+      md.pw = md.w + 2 * kPad;
+      md.ph = md.h + 2 * kPad;
+      md.poff = ptexels;
       texels += (uint64_t)md.w * md.h * s->n_levels;
+      ptexels += (uint64_t)md.pw * md.ph * s->n_levels;
       if (b->examples[e].method == TS_SAMPLE_IMAGE) {
         bool any = false;
         for (size_t i = 0; i < (size_t)md.w * md.h && !any; ++i) any = masks[e].px[4 * i] != 0;
@@ -656,20 +667,38 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
         CUDA_TRY(cudaMemcpy(s->masks.p + s->maps[f].mask_off, mb.data(), mb.size(), cudaMemcpyHostToDevice));
       }
     }
+    CUDA_TRY(s->plevels.alloc(ptexels));
+    for (uint32_t f = 0; f < s->n_maps; ++f)
+      launch_pad(s->levels.p + s->maps[f].off, s->maps[f].w, s->maps[f].h, s->n_levels,
+                 s->plevels.p + s->maps[f].poff, st);
+    CUDA_TRY(cudaGetLastError());
     CUDA_TRY(s->d_maps.alloc(s->n_maps));
     CUDA_TRY(cudaMemcpy(s->d_maps.p, s->maps.data(), s->n_maps * sizeof(MapDesc), cudaMemcpyHostToDevice));
     // guides: every example (unfiltered order) plus the target guide
     std::vector<GuideDesc> gd(std::max<uint32_t>(s->n_ex, 1));
     if (s->guided) {
-      uint64_t gtex = 0;
+      uint64_t gtex = 0, pgtex = 0;
       for (uint32_t e = 0; e < s->n_ex; ++e) {
         gd[e].w = guides[e].w;
         gd[e].h = guides[e].h;
         gd[e].off = gtex;
+        gd[e].pw = gd[e].w + 2 * kPad;
+        gd[e].ph = gd[e].h + 2 * kPad;
+        gd[e].poff = pgtex;
         gtex += (uint64_t)guides[e].w * guides[e].h * s->n_levels;
+        pgtex += (uint64_t)gd[e].pw * gd[e].ph * s->n_levels;
       }
+      // the guide of map f is example f's guide (unfiltered index); the
+      // padded fast path needs its size to equal the map's
+      for (uint32_t f = 0; f < s->n_maps; ++f)
+        if (f >= s->n_ex || gd[f].w != s->maps[f].w || gd[f].h != s->maps[f].h) s->guide_dims_differ = true;
       CUDA_TRY(s->guides.alloc(gtex));
-      for (uint32_t e = 0; e < s->n_ex; ++e) device_pyramid(guides[e], p.backtrack_stages, s->guides.p + gd[e].off, st);
+      CUDA_TRY(s->pguides.alloc(pgtex));
+      for (uint32_t e = 0; e < s->n_ex; ++e) {
+        device_pyramid(guides[e], p.backtrack_stages, s->guides.p + gd[e].off, st);
+        launch_pad(s->guides.p + gd[e].off, gd[e].w, gd[e].h, s->n_levels, s->pguides.p + gd[e].poff, st);
+      }
+      CUDA_TRY(cudaGetLastError());
       Image tg = load_image(b->target, true, W, H, st);
       CUDA_TRY(s->tguide.alloc((size_t)W * H * s->n_levels));
       device_pyramid(tg, p.backtrack_stages, s->tguide.p, st);
@@ -1030,6 +1059,9 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
 
     SessionDev sd{};
     sd.levels = s->levels.p;
+    sd.plevels = s->plevels.p;
+    sd.pguides = s->pguides.p;
+    sd.guide_dims_differ = s->guide_dims_differ ? 1 : 0;
     sd.masks = s->masks.p;
     sd.maps = s->d_maps.p;
     sd.n_maps = s->n_maps;
@@ -1132,7 +1164,10 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
             lt.run(TS_KERNEL_MEAN, [&] { launch_mean(sd, chunk, bd, st); });
             ++launches;
           }
-          lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve(sd, chunk, bd, st); });
+          if (bp.i1 - bp.i0 <= p.team_max_batch)
+            lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve_team(sd, chunk, bd, st); });
+          else
+            lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve(sd, chunk, bd, st); });
           lt.run(TS_KERNEL_COMMIT, [&] { launch_commit(sd, chunk, bd, st); });
           launches += 2;
           ++batches;
