@@ -196,10 +196,12 @@ int ts_builder_max_thread_count(ts_builder *b, uint64_t count);
  * 0 gives batches of one item, the reference's single-thread semantics.
  * max_batch caps a batch (0 = no cap). */
 int ts_builder_batch_schedule(ts_builder *b, uint32_t batch_divisor, uint32_t max_batch);
-/* Batches of at most `team_max_batch` work items resolve with one CTA per
- * item (lowest latency); larger batches with one warp per item (highest
- * throughput).  Both give identical results. */
-int ts_builder_resolve_team(ts_builder *b, uint32_t team_max_batch);
+/* Kernel forms of the resolve step, all with identical results: batches of
+ * at most `full_max_batch` items score every candidate of an item with one
+ * CTA (lowest latency); up to `team_max_batch` items, one CTA per item with
+ * early exit; larger batches, one warp per item (highest throughput).
+ * Defaults 8192 and 1024. */
+int ts_builder_resolve_team(ts_builder *b, uint32_t team_max_batch, uint32_t full_max_batch);
 /* CUDA device ordinal (default 0). */
 int ts_builder_device(ts_builder *b, int32_t device);
 /* Time every kernel launch of run() with CUDA events (adds host overhead;
@@ -239,6 +241,17 @@ int ts_generated_id_map(const ts_generated *g, uint32_t *out_pm);
 uint64_t ts_generated_resolved_count(const ts_generated *g);
 int ts_generated_resolved(const ts_generated *g, uint32_t *out_flat, float *out_score);
 void ts_generated_stats(const ts_generated *g, ts_run_stats *out);
+/* One timed kernel launch of a profiled run (ts_builder_profile_kernels). */
+typedef struct ts_launch_record {
+  int32_t kind;         /* TS_KERNEL_* */
+  int32_t stage;        /* p_stage (backtrack stage), -1 outside the stage loop */
+  uint32_t batch_items; /* work items of the batch (stage items for per-stage kernels) */
+  float ms;             /* device time between CUDA events around the launch */
+} ts_launch_record;
+/* Number of launch records, and the records themselves (`out` holds at
+ * least that many). */
+uint64_t ts_generated_launch_count(const ts_generated *g);
+int ts_generated_launches(const ts_generated *g, ts_launch_record *out);
 void ts_generated_free(ts_generated *g);
 
 #ifdef __cplusplus

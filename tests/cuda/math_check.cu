@@ -4,6 +4,8 @@
 //  - ts_exp64 stays within 2 ulp of CUDA's exp()
 //  - the double-f32 weight (ts_weight_ff), when it decides, equals the
 //    exact f64 weight, and decides for almost every input
+//  - the integer mean (ts_add4_rn chain, ts_div_int_rn) of a 50-entry
+//    distance list equals the __dadd_rn chain divided by __ddiv_rn
 // Prints one JSON line of mismatch counts; exit status 0.
 #include <cstdio>
 #include <cstdint>
@@ -42,6 +44,21 @@ __global__ void k_check(const double *a, const double *b, const double *x, size_
     q_ref[i] = __ddiv_rn(a[i], b[i]);
     e_dev[i] = ts::ts_exp64(x[i], tab);
     e_cuda[i] = exp(x[i]);
+  }
+}
+
+// means of 50-entry lists: integer chain vs f64 chain
+__global__ void k_mean_check(const double *d, size_t lists, double *m_int, double *m_ref) {
+  for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < lists; l += (size_t)gridDim.x * blockDim.x) {
+    uint64_t acc = 0;
+    double ref = 0.0;
+    for (int j = 0; j < 50; ++j) {
+      const double v = d[l * 50 + j];
+      acc = ts::ts_add4_rn(acc, ts::dbl_bits(v));
+      for (int r = 0; r < 4; ++r) ref = __dadd_rn(ref, v);
+    }
+    m_int[l] = ts::bits_dbl(ts::ts_div_int_rn(acc, 200u));
+    m_ref[l] = __ddiv_rn(ref, 200.0);
   }
 }
 
@@ -118,6 +135,8 @@ int main() {
   cudaMemcpy(da, wd.data(), n * 8, cudaMemcpyHostToDevice);
   cudaMemcpy(db, wm.data(), n * 8, cudaMemcpyHostToDevice);
   k_weight<<<1216, 256>>>(da, db, n, wf, dec, we);
+  const size_t lists = n / 50;
+  k_mean_check<<<1216, 256>>>(da, lists, q1, q2);
   err = cudaDeviceSynchronize();
   if (err != cudaSuccess) { printf("{\"cuda_error\": \"%s\"}\n", cudaGetErrorString(err)); return 1; }
   std::vector<float> hwf(n), hwe(n);
@@ -125,6 +144,11 @@ int main() {
   cudaMemcpy(hwf.data(), wf, n * 4, cudaMemcpyDeviceToHost);
   cudaMemcpy(hwe.data(), we, n * 4, cudaMemcpyDeviceToHost);
   cudaMemcpy(hdec.data(), dec, n * 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(hq1.data(), q1, lists * 8, cudaMemcpyDeviceToHost);
+  cudaMemcpy(hq2.data(), q2, lists * 8, cudaMemcpyDeviceToHost);
+  size_t mean_bad = 0;
+  for (size_t l = 0; l < lists; ++l)
+    if (bits(hq1[l]) != bits(hq2[l])) ++mean_bad;
   size_t w_bad = 0, w_undecided = 0;
   for (size_t i = 0; i < n; ++i) {
     if (!hdec[i]) { ++w_undecided; continue; }
@@ -134,7 +158,7 @@ int main() {
   }
   printf("{\"n\": %zu, \"div_mismatch\": %zu, \"host_div_mismatch\": %zu, \"exp_host_device_mismatch\": %zu, "
          "\"exp_over_2ulp\": %zu, \"exp_max_ulp\": %.3f, \"exp_f32_differs_from_cuda\": %zu, "
-         "\"weight_mismatch\": %zu, \"weight_undecided\": %zu}\n",
-         n, div_bad, host_div_bad, exp_host_bad, exp_ulp_bad, max_ulp, f32_bad, w_bad, w_undecided);
+         "\"weight_mismatch\": %zu, \"weight_undecided\": %zu, \"mean_mismatch\": %zu}\n",
+         n, div_bad, host_div_bad, exp_host_bad, exp_ulp_bad, max_ulp, f32_bad, w_bad, w_undecided, mean_bad);
   return 0;
 }

@@ -27,6 +27,12 @@ def host(tmp_path_factory):
     L.host_exp.argtypes = [C.c_double]
     L.host_div.restype = C.c_double
     L.host_div.argtypes = [C.c_double, C.c_double]
+    L.host_sum4_int.restype = C.c_double
+    L.host_sum4_int.argtypes = [C.c_void_p, C.c_int]
+    L.host_div_int.restype = C.c_double
+    L.host_div_int.argtypes = [C.c_double, C.c_uint32]
+    L.host_add_rn.restype = C.c_double
+    L.host_add_rn.argtypes = [C.c_double, C.c_double]
     L.host_weight_ff.restype = C.c_int
     L.host_weight_ff.argtypes = [C.c_double, C.c_double, C.POINTER(C.c_float)]
     L.host_weight_exact.restype = C.c_float
@@ -70,6 +76,53 @@ def _distances(rng, n, W, H):
         # fused multiply-add: exact rational arithmetic, one rounding
         out.append(float(Fraction(dx) * Fraction(dx) + Fraction(dy * dy)))
     return np.array(out, np.float64)
+
+
+def test_integer_addition(host):
+    """ts_add_rn equals IEEE double addition (non-negative operands)."""
+    rng = np.random.default_rng(10)
+    a = np.concatenate([rng.random(100000) * 8.0, 2.0 ** rng.integers(-40, 14, 50000) * rng.random(50000)])
+    b = np.concatenate([rng.random(100000) * 8.0, 2.0 ** rng.integers(-40, 14, 50000) * rng.random(50000)])
+    a[:1000] = 0.0
+    for x, y in zip(a, b):
+        assert host.host_add_rn(float(x), float(y)) == float(x) + float(y), (x, y)
+    # ties: y exactly half an ulp of x, and odd / even x
+    for t in range(20000):
+        x = float(rng.integers(1 << 52, 1 << 53)) * 2.0 ** int(rng.integers(-60, 0))
+        y = math.ulp(x) / 2 * float(rng.integers(1, 4))
+        assert host.host_add_rn(x, y) == x + y, (x, y)
+
+
+def test_integer_division(host):
+    """ts_div_int_rn(s, n) equals IEEE s / n for the mean's divisors."""
+    rng = np.random.default_rng(12)
+    s = np.concatenate([rng.random(100000) * 4096.0, 2.0 ** rng.integers(-40, 13, 50000) * rng.random(50000)])
+    for i, x in enumerate(s):
+        n = int(rng.integers(1, 1025)) if i % 2 else 4 * int(rng.integers(1, 257))
+        assert host.host_div_int(float(x), n) == float(x) / n, (x, n)
+    assert host.host_div_int(0.0, 200) == 0.0
+
+
+def test_integer_sum4(host):
+    """The 4x-duplicated in-order sum through ts_add4_rn equals the f64 chain."""
+    rng = np.random.default_rng(11)
+    for t in range(4000):
+        n = int(rng.integers(1, 257))
+        if t % 3 == 0:
+            d = rng.random(n) * 4.0
+        elif t % 3 == 1:
+            W, H = int(rng.integers(8, 16385)), int(rng.integers(8, 16385))
+            d = _distances(rng, n, W, H)
+        else:  # grid-aligned values that produce exact ties
+            base = float(rng.integers(1, 1 << 20)) * 2.0 ** -40
+            d = np.array([base * (1 + float(rng.integers(0, 8)) / 8) for _ in range(n)])
+        d[rng.random(n) < 0.05] = 0.0
+        ref = 0.0
+        for v in d:
+            for _ in range(4):
+                ref += float(v)
+        got = host.host_sum4_int(d.ctypes.data, n)
+        assert got == ref, (t, got, ref)
 
 
 def test_fast_weight_matches_exact(host):

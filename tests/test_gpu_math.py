@@ -9,7 +9,9 @@ the product header and checks, over 4M inputs:
   - ts_exp64 on the device equals ts_exp64 on the host bit for bit,
   - ts_exp64 is within 2 ulp of CUDA's exp(),
   - the double-f32 weight, when it decides, equals the exact f64 weight
-    (and decides for more than 99.9% of inputs).
+    (and decides for more than 99.9% of inputs),
+  - the integer mean (ts_add4_rn, ts_div_int_rn) equals the __dadd_rn chain
+    divided by __ddiv_rn.
 """
 import json
 import os
@@ -36,3 +38,4 @@ def test_weight_math(tmp_path):
     assert r["exp_over_2ulp"] == 0, r
     assert r["weight_mismatch"] == 0, r
     assert r["weight_undecided"] < r["n"] // 1000, r
+    assert r["mean_mismatch"] == 0, r

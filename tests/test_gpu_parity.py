@@ -31,18 +31,20 @@ def assert_same(got, ref, label=""):
     assert got["evals"] == ref["evals"], "%s evals %d != %d" % (label, got["evals"], ref["evals"])
 
 
-def run_both(ts, oracle, spec, divisor=8, max_batch=0, team=None):
-    got = ts.run_spec(spec, batch_divisor=divisor, max_batch=max_batch, team_max_batch=team)
+def run_both(ts, oracle, spec, divisor=8, max_batch=0, team=None, full=1024):
+    got = ts.run_spec(spec, batch_divisor=divisor, max_batch=max_batch, team_max_batch=team,
+                      team_full_max_batch=full)
     ref = oracle.run(spec, batch_divisor=divisor, max_batch=max_batch, nthreads=4)
     return got, ref
 
 
-@pytest.mark.parametrize("team", [0, 1 << 30])
-def test_resolve_forms(ts, oracle, wl, team):
-    """Warp-per-item (team 0) and CTA-per-item (every batch) resolve kernels."""
+@pytest.mark.parametrize("team,full", [(0, 0), (1 << 30, 0), (1 << 30, 1 << 30)])
+def test_resolve_forms(ts, oracle, wl, team, full):
+    """Resolve kernel forms on every batch: warp per item; CTA per item with
+    early exit; CTA per item scoring every candidate."""
     for spec in (wl.config0(out=64, ex=32), wl.config1(out=64, ex=32), wl.config2(out=64, ex=32)):
-        got, ref = run_both(ts, oracle, spec, team=team)
-        assert_same(got, ref, "%s team=%d" % (spec["name"], team))
+        got, ref = run_both(ts, oracle, spec, team=team, full=full)
+        assert_same(got, ref, "%s team=%d full=%d" % (spec["name"], team, full))
 
 
 @pytest.mark.parametrize("divisor", [8, 2, 1])

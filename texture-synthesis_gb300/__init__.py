@@ -83,6 +83,10 @@ class RunStats(C.Structure):
         return d
 
 
+class _LaunchRecord(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("stage", C.c_int32), ("batch_items", C.c_uint32), ("ms", C.c_float)]
+
+
 _PROGRESS_FN = C.CFUNCTYPE(None, C.POINTER(_Progress), C.c_void_p)
 
 # every function tsgpu.h declares: name -> (restype, argtypes)
@@ -113,7 +117,7 @@ SIGNATURES = {
     "ts_builder_batch_schedule": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
     "ts_builder_device": (C.c_int, [C.c_void_p, C.c_int32]),
     "ts_builder_profile_kernels": (C.c_int, [C.c_void_p, C.c_int32]),
-    "ts_builder_resolve_team": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "ts_builder_resolve_team": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
     "ts_builder_build": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "ts_session_run": (C.c_int, [C.c_void_p, _PROGRESS_FN, C.c_void_p, C.POINTER(C.c_void_p)]),
     "ts_session_free": (None, [C.c_void_p]),
@@ -126,6 +130,8 @@ SIGNATURES = {
     "ts_generated_resolved": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "ts_generated_stats": (None, [C.c_void_p, C.POINTER(RunStats)]),
     "ts_generated_free": (None, [C.c_void_p]),
+    "ts_generated_launch_count": (C.c_uint64, [C.c_void_p]),
+    "ts_generated_launches": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
 
 
@@ -328,10 +334,11 @@ class SessionBuilder:
     def device(self, ordinal):
         return self._check(lib().ts_builder_device(self._h, int(ordinal)))
 
-    def resolve_team(self, max_batch):
-        """Batches of at most max_batch items resolve with one CTA per item;
-        larger ones with one warp per item (identical results)."""
-        return self._check(lib().ts_builder_resolve_team(self._h, int(max_batch)))
+    def resolve_team(self, max_batch, full_max_batch=1024):
+        """Resolve kernel forms by batch size (identical results): up to
+        full_max_batch items, one CTA scores every candidate of an item; up to
+        max_batch, one CTA per item with early exit; above, a warp per item."""
+        return self._check(lib().ts_builder_resolve_team(self._h, int(max_batch), int(full_max_batch)))
 
     def profile_kernels(self, on=True):
         """Time every kernel launch with CUDA events (measurement runs)."""
@@ -423,8 +430,18 @@ class GeneratedImage:
         lib().ts_generated_stats(self._h, C.byref(st))
         return st.as_dict()
 
+    def launches(self):
+        """Per-launch timings of a profiled run: dicts of kernel, stage,
+        batch_items, ms."""
+        n = lib().ts_generated_launch_count(self._h)
+        arr = (_LaunchRecord * max(1, n))()
+        lib().ts_generated_launches(self._h, arr)
+        return [{"kernel": KERNEL_KINDS[r.kind], "stage": r.stage, "batch_items": r.batch_items, "ms": r.ms}
+                for r in arr[:n]]
 
-def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0, profile=False, team_max_batch=None):
+
+def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0, profile=False, team_max_batch=None,
+                      team_full_max_batch=1024):
     """A SessionBuilder for a workload spec dict (see workloads.py)."""
     p = spec["params"]
     b = Session.builder()
@@ -457,13 +474,14 @@ def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0, profile=Fals
     if profile:
         b.profile_kernels(True)
     if team_max_batch is not None:
-        b.resolve_team(team_max_batch)
+        b.resolve_team(team_max_batch, team_full_max_batch)
     return b
 
 
-def run_spec(spec, batch_divisor=8, max_batch=0, device=0, team_max_batch=None):
+def run_spec(spec, batch_divisor=8, max_batch=0, device=0, team_max_batch=None, team_full_max_batch=1024):
     """Build and run a workload spec; returns a dict shaped like the oracle's."""
-    g = builder_from_spec(spec, batch_divisor, max_batch, device, team_max_batch=team_max_batch).build().run()
+    g = builder_from_spec(spec, batch_divisor, max_batch, device, team_max_batch=team_max_batch,
+                          team_full_max_batch=team_full_max_batch).build().run()
     flat, score = g.resolved()
     st = g.stats()
     return {"image": g.into_image(), "coord": g.coord_map(), "id": g.id_map(), "resolved": flat,

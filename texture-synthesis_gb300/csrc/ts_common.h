@@ -258,6 +258,133 @@ TS_HD float bits_flt(uint32_t u) {
 }
 
 // ---------------------------------------------------------------------------
+// IEEE round-to-nearest-even addition of non-negative doubles in integer
+// arithmetic, for the in-order sum of the 4x-duplicated distance list
+// (ms.rs:417-421).  GB300's f64 adds have long latency; this dependent chain
+// of 4k additions runs on the integer pipes instead.  Operands are the bit
+// patterns of finite doubles >= 0 (zero or normal).
+// ---------------------------------------------------------------------------
+constexpr uint64_t kFrac52 = (1ULL << 52) - 1;
+
+// RN(x + y): align with guard, round and sticky bits, add, renormalise once,
+// round to nearest even.
+TS_HD uint64_t ts_add_rn(uint64_t bx, uint64_t by) {
+  if (bx < by) {
+    const uint64_t t = bx;
+    bx = by;
+    by = t;
+  }
+  if (by == 0) return bx;
+  uint32_t ex = (uint32_t)(bx >> 52);
+  const uint32_t ey = (uint32_t)(by >> 52);
+  const uint64_t mx = (bx & kFrac52) | (1ULL << 52);
+  const uint64_t my = (by & kFrac52) | (1ULL << 52);
+  const uint32_t sh = ex - ey;
+  uint64_t y;
+  if (sh >= 58) {
+    y = 1;  // only the sticky bit survives
+  } else {
+    const uint64_t y3 = my << 3;
+    y = (y3 >> sh) | ((y3 & ((1ULL << sh) - 1)) != 0 ? 1u : 0u);
+  }
+  uint64_t z = (mx << 3) + y;
+  if (z >> 56) {
+    z = (z >> 1) | (z & 1u);
+    ++ex;
+  }
+  uint64_t m = z >> 3;
+  const uint32_t low = (uint32_t)(z & 7u);
+  if (low > 4u || (low == 4u && (m & 1u))) ++m;
+  if (m >> 53) {
+    m >>= 1;
+    ++ex;
+  }
+  return ((uint64_t)ex << 52) | (m & kFrac52);
+}
+
+// RN(RN(RN(RN(s + d) + d) + d) + d).  When all four sums stay in s's binade,
+// s is on that binade's grid u and every step adds d rounded to u: the bit
+// pattern advances by 4 * round(d / u) (exact ties alternate by parity).
+TS_HD uint64_t ts_add4_rn(uint64_t bs, uint64_t bd) {
+  if (bd == 0) return bs;
+  if (bs != 0 && bs > bd) {
+    const uint32_t es = (uint32_t)(bs >> 52), ed = (uint32_t)(bd >> 52);
+    const uint32_t sh = es - ed;
+    uint64_t a, rem, half;
+    if (sh >= 54) {
+      a = 0;
+      rem = 1;  // below half an ulp: rounds down
+      half = 2;
+    } else if (sh >= 1) {
+      const uint64_t md = (bd & kFrac52) | (1ULL << 52);
+      a = md >> sh;
+      rem = md & ((1ULL << sh) - 1);
+      half = 1ULL << (sh - 1);
+    } else {
+      a = 0;
+      rem = 0;
+      half = 0;  // same binade: not this path
+    }
+    if (sh >= 1) {
+      const bool tie = rem == half;
+      const uint64_t step = a + (rem > half ? 1u : 0u);
+      if ((bs & kFrac52) + 4 * (a + 1) < (1ULL << 52)) {
+        if (!tie) return bs + 4 * step;
+        uint64_t b = bs;
+        for (int i = 0; i < 4; ++i) {
+          b += a;
+          b += b & 1u;  // the tie goes to the even neighbour
+        }
+        return b;
+      }
+    }
+  }
+  bs = ts_add_rn(bs, bd);
+  bs = ts_add_rn(bs, bd);
+  bs = ts_add_rn(bs, bd);
+  return ts_add_rn(bs, bd);
+}
+
+// RN(s / n) for a double s >= 0 (zero or normal) and an integer 1 <= n < 2^20,
+// in integer arithmetic: a 96-bit quotient from two 64-by-32 divisions,
+// normalised to 53 bits plus guard bits and a sticky bit, rounded to nearest
+// even.
+TS_HD uint64_t ts_div_int_rn(uint64_t bs, uint32_t n) {
+  if (bs == 0) return 0;
+  const uint32_t e = (uint32_t)(bs >> 52);
+  const uint64_t m = (bs & kFrac52) | (1ULL << 52);
+  const uint64_t num = m << 11;  // [2^63, 2^64)
+  const uint64_t q1 = num / n, r1 = num - q1 * n;
+  const uint64_t n2 = r1 << 32;  // < 2^52
+  const uint64_t q2 = n2 / n, r2 = n2 - q2 * n;
+  // quotient Q = q1 * 2^32 + q2 (value = Q * 2^(e - 1118)), sticky = r2 != 0
+  uint64_t hi = q1 >> 32, lo = (q1 << 32) | q2;
+  bool sticky = r2 != 0;
+  const uint32_t bl = hi ? 128u - clz64(hi) : 64u - clz64(lo);
+  const uint32_t t = bl - 56;  // keep 56 bits: 53 + guard, round, sticky
+  uint64_t z;
+  if (t == 0) {
+    z = lo;
+  } else if (t < 64) {
+    sticky = sticky || (lo & ((1ULL << t) - 1)) != 0;
+    z = (lo >> t) | (hi << (64 - t));
+  } else {
+    sticky = sticky || lo != 0 || (hi & ((1ULL << (t - 64)) - 1)) != 0;
+    z = hi >> (t - 64);
+  }
+  z |= sticky ? 1u : 0u;
+  uint64_t mq = z >> 3;
+  uint32_t ee = e - 40 + t;
+  const uint32_t low = (uint32_t)(z & 7u);
+  if (low > 4u || (low == 4u && (mq & 1u))) ++mq;
+  if (mq >> 53) {
+    mq >>= 1;
+    ++ee;
+  }
+  return ((uint64_t)ee << 52) | (mq & kFrac52);
+}
+
+// ---------------------------------------------------------------------------
 // Neighbour weight w = (f32) exp(-(d / mean)) without f64 arithmetic on the
 // common path (GB300's f64 rate is a small fraction of its f32 rate).
 //

@@ -8,9 +8,10 @@
 //   knn_exhaustive  CTA per item the walk could not finish (sparse regions):
 //                   radix-select over the resolved list
 //   mean            thread per item: the mean of the 4x-duplicated distance
-//                   list (ms.rs:417-423), the in-order f64 sum; one item per
-//                   lane, because an f64 warp instruction costs the same
-//                   whatever its active-lane count
+//                   list (ms.rs:417-423), the in-order f64 sum, one item per
+//                   lane (large batches); for whole small batches the
+//                   exhaustive k-NN computes it on one thread in integer
+//                   arithmetic, whose dependent chain is shorter than f64's
 //   resolve         warp per item: neighbour weights (ms.rs:1198-1203) in
 //                   double-f32 arithmetic with an exact f64 fallback,
 //                   coherence + random candidates (ms.rs:478-602), own
@@ -46,7 +47,8 @@ constexpr int kResolveWarps = 4;
 constexpr int kWalkWarps = 8;
 constexpr int kExhThreads = 256;
 constexpr int kTeamThreads = 128;
-constexpr int kExhCap = 2048;  // keys kept by the exhaustive k-NN at the cut distance
+constexpr int kExhCap = 2048;      // keys kept by the exhaustive k-NN at the cut distance
+constexpr int kExhAllKeys = 8192;  // keys the exhaustive k-NN sorts in shared memory directly
 constexpr uint32_t kMaxDraws = 1u << 22;
 
 __device__ const double g_exp2_64[64] = {TS_EXP2_TABLE_VALUES};
@@ -203,6 +205,7 @@ __global__ void __launch_bounds__(kWalkWarps *kWarp, 4) k_knn_walk(SessionDev s,
 // them by (d2, y, x) and emit the first k.
 // ---------------------------------------------------------------------------
 struct ExhShared {
+  double dist[256];  // the item's neighbour distances, when the kernel also computes the mean
   uint32_t hist[256];
   unsigned long long keys[kExhCap];
   uint32_t nkeys;
@@ -236,21 +239,46 @@ __device__ __forceinline__ unsigned long long nb_key(uint32_t d2, int x, int y) 
 }
 
 __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
-                                    ExhShared &sh);
+                                    ExhShared &sh, unsigned long long *all, bool with_mean);
 
+// One CTA per item.  `all` (dynamic shared memory, kExhAllKeys entries)
+// receives every point's key in one pass over the resolved list; when they
+// fit, a bitonic sort of them gives the answer directly, otherwise a
+// radix select over further passes finds the cut distance first.
 __global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive(SessionDev s, StageDev st, BatchDev b,
                                                                  int all_items) {
   __shared__ ExhShared sh;
+  extern __shared__ unsigned long long all_keys[];
   const uint32_t n = all_items ? b.i1 - b.i0 : *b.fb_count;
   for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
     const uint32_t local = all_items ? e : b.fb_list[e];
-    knn_exhaustive_item(s, st, b, local, sh);
+    knn_exhaustive_item(s, st, b, local, sh, all_keys, all_items != 0);
     __syncthreads();
   }
 }
 
+// Bitonic sort of keys[0, np2) ascending (np2 a power of two), whole CTA.
+__device__ __forceinline__ void block_bitonic(unsigned long long *keys, uint32_t np2) {
+  for (uint32_t size = 2; size <= np2; size <<= 1) {
+    for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+      for (uint32_t i = threadIdx.x; i < np2; i += blockDim.x) {
+        const uint32_t j = i ^ stride;
+        if (j > i) {
+          const bool up = (i & size) == 0;
+          const unsigned long long a = keys[i], c = keys[j];
+          if ((a > c) == up) {
+            keys[i] = c;
+            keys[j] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
 __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
-                                    ExhShared &sh) {
+                                    ExhShared &sh, unsigned long long *all, bool with_mean) {
   const uint32_t pixel = st.items[b.i0 + local];
   const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
   const uint32_t k = s.k;
@@ -267,13 +295,147 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
     sh.overflow = 0;
   }
   __syncthreads();
-  uint32_t mine = 0;
-  for_points(s, n_res, [&](int, int) { ++mine; });
-  atomicAdd(&sh.total, mine);
+  // pass 1: every key into shared memory while it fits, and the count; one
+  // shared atomic per warp and round
+  const int lane = threadIdx.x & 31;
+  for (uint32_t e0 = 0; e0 < n_res; e0 += blockDim.x) {
+    const uint32_t e = e0 + threadIdx.x;
+    int xs[3], ys[3];
+    uint32_t cnt = 0;
+    if (e < n_res) {
+      const uint32_t p = s.resolved[e];
+      const int x = (int)(p % s.W), y = (int)(p / s.W);
+      xs[0] = x;
+      ys[0] = y;
+      cnt = 1;
+      if (s.tiling && mir_bit(s, (uint32_t)x, (uint32_t)y)) {
+        if (x < s.x_l) {
+          xs[cnt] = x + (int)s.W;
+          ys[cnt++] = y;
+        } else if (x > s.x_r) {
+          xs[cnt] = x - (int)s.W;
+          ys[cnt++] = y;
+        }
+        if (y < s.y_b) {
+          xs[cnt] = x;
+          ys[cnt++] = y + (int)s.H;
+        } else if (y > s.y_t) {
+          xs[cnt] = x;
+          ys[cnt++] = y - (int)s.H;
+        }
+      }
+    }
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    uint32_t base = 0;
+    if (lane == 31) base = atomicAdd(&sh.total, incl);
+    base = __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
+    uint32_t dor = 0;
+    for (uint32_t i = 0; i < cnt; ++i) {
+      const uint32_t d2 = d2of(xs[i], ys[i]);
+      dor |= d2;
+      if (base + i < (uint32_t)kExhAllKeys) all[base + i] = nb_key(d2, xs[i], ys[i]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dor |= __shfl_xor_sync(0xffffffffu, dor, o);
+    if (lane == 0 && dor) atomicOr(&sh.prefix, dor);  // prefix holds the OR of all d2 until the select
+  }
   __syncthreads();
   const uint32_t total = sh.total;
-  bool take_all = total <= k;
-  if (!take_all) {
+  const unsigned long long *sorted;
+  uint32_t n;
+  if (total <= k || total <= (uint32_t)kExhAllKeys) {
+    // radix select of the k-th smallest d2 over the shared keys, digits of
+    // 8 bits from the highest significant bit down
+    const uint32_t dor_all = sh.prefix;
+    const int bits = dor_all ? 32 - __clz(dor_all) : 1;
+    uint32_t D = 0xffffffffu;
+    if (total > k) {
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        sh.prefix = 0;
+        sh.rank = k;
+      }
+      for (int shift = ((bits - 1) / 8) * 8; shift >= 0; shift -= 8) {
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) sh.hist[i] = 0;
+        __syncthreads();
+        const uint32_t prefix = sh.prefix;
+        for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) {
+          const uint32_t d2 = (uint32_t)(all[i] >> 32);
+          if (shift == 24 || ((d2 ^ prefix) >> (shift + 8)) == 0) atomicAdd(&sh.hist[(d2 >> shift) & 255u], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+          // warp 0: inclusive scan of 256 bins, 8 per lane
+          uint32_t v[8], acc = 0;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            acc += sh.hist[lane * 8 + q];
+            v[q] = acc;
+          }
+          uint32_t off = acc;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, off, o);
+            if (lane >= o) off += t;
+          }
+          off -= acc;  // exclusive prefix of this lane's 8 bins
+          const uint32_t rank = sh.rank;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const uint32_t lo = off + (q ? v[q - 1] : 0u), hi = off + v[q];
+            if (lo < rank && rank <= hi) {
+              sh.prefix = prefix | ((uint32_t)(lane * 8 + q) << shift);
+              sh.rank = rank - lo;
+            }
+          }
+        }
+        __syncthreads();
+      }
+      D = sh.prefix;
+      // keys at or below the cut, into the small buffer
+      if (threadIdx.x == 0) sh.nkeys = 0;
+      __syncthreads();
+      for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) {
+        const unsigned long long key = all[i];
+        if ((uint32_t)(key >> 32) <= D) {
+          const uint32_t slot = atomicAdd(&sh.nkeys, 1u);
+          if (slot < (uint32_t)kExhCap)
+            sh.keys[slot] = key;
+          else
+            sh.overflow = 1;
+        }
+      }
+    } else {
+      if (threadIdx.x == 0) sh.nkeys = total;
+      for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) sh.keys[i] = all[i];
+    }
+    __syncthreads();
+    if (sh.overflow) {
+      if (threadIdx.x == 0) {
+        set_err(s.err, kDevErrLimit);
+        b.ncnt[local] = 0;
+      }
+      return;
+    }
+    n = sh.nkeys;
+    uint32_t np2 = 1;
+    while (np2 < n) np2 <<= 1;
+    for (uint32_t i = n + threadIdx.x; i < np2; i += blockDim.x) sh.keys[i] = ~0ull;
+    __syncthreads();
+    block_bitonic(sh.keys, np2);
+    sorted = sh.keys;
+  } else {
+    if (threadIdx.x == 0) {
+      sh.prefix = 0;
+      sh.rank = k;
+    }
+    __syncthreads();
+    // radix select of the k-th smallest d2 over further passes
     for (int pass = 0; pass < 4; ++pass) {
       const int shift = 24 - 8 * pass;
       for (int i = threadIdx.x; i < 256; i += blockDim.x) sh.hist[i] = 0;
@@ -299,57 +461,52 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
       }
       __syncthreads();
     }
-  }
-  const uint32_t D = take_all ? 0xffffffffu : sh.prefix;
-  for_points(s, n_res, [&](int x, int y) {
-    const uint32_t d2 = d2of(x, y);
-    if (d2 <= D) {
-      const uint32_t slot = atomicAdd(&sh.nkeys, 1u);
-      if (slot < (uint32_t)kExhCap)
-        sh.keys[slot] = nb_key(d2, x, y);
-      else
-        sh.overflow = 1;
-    }
-  });
-  __syncthreads();
-  if (sh.overflow) {
-    if (threadIdx.x == 0) {
-      set_err(s.err, kDevErrLimit);
-      b.ncnt[local] = 0;
-    }
-    return;
-  }
-  const uint32_t n = sh.nkeys;
-  uint32_t np2 = 1;
-  while (np2 < n) np2 <<= 1;
-  for (uint32_t i = n + threadIdx.x; i < np2; i += blockDim.x) sh.keys[i] = ~0ull;
-  __syncthreads();
-  // bitonic sort of np2 keys
-  for (uint32_t size = 2; size <= np2; size <<= 1) {
-    for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-      for (uint32_t i = threadIdx.x; i < np2; i += blockDim.x) {
-        const uint32_t j = i ^ stride;
-        if (j > i) {
-          const bool up = (i & size) == 0;
-          const unsigned long long a = sh.keys[i], c = sh.keys[j];
-          if ((a > c) == up) {
-            sh.keys[i] = c;
-            sh.keys[j] = a;
-          }
-        }
+    const uint32_t D = sh.prefix;
+    for_points(s, n_res, [&](int x, int y) {
+      const uint32_t d2 = d2of(x, y);
+      if (d2 <= D) {
+        const uint32_t slot = atomicAdd(&sh.nkeys, 1u);
+        if (slot < (uint32_t)kExhCap)
+          sh.keys[slot] = nb_key(d2, x, y);
+        else
+          sh.overflow = 1;
       }
-      __syncthreads();
+    });
+    __syncthreads();
+    if (sh.overflow) {
+      if (threadIdx.x == 0) {
+        set_err(s.err, kDevErrLimit);
+        b.ncnt[local] = 0;
+      }
+      return;
     }
+    n = sh.nkeys;
+    uint32_t np2 = 1;
+    while (np2 < n) np2 <<= 1;
+    for (uint32_t i = n + threadIdx.x; i < np2; i += blockDim.x) sh.keys[i] = ~0ull;
+    __syncthreads();
+    block_bitonic(sh.keys, np2);
+    sorted = sh.keys;
   }
   const uint32_t nout = n < k ? n : k;
   int32_t *nbo = b.nbuf + (size_t)local * k;
   const uint32_t nb = b.i1 - b.i0;
   const double x2 = s.xdiv[px + s.xdiv_off], y2 = s.ydiv[py + s.ydiv_off];
   for (uint32_t i = threadIdx.x; i < nout; i += blockDim.x) {
-    const unsigned long long key = sh.keys[i];
+    const unsigned long long key = sorted[i];
     const int x = (int)(key & 0xffffu) - 32768, y = (int)((key >> 16) & 0xffffu) - 32768;
     nbo[i] = pack_off(x - px, y - py);
-    b.dist[(size_t)i * nb + local] = neighbour_dist(s, px, py, x - px, y - py, x2, y2);
+    const double d = neighbour_dist(s, px, py, x - px, y - py, x2, y2);
+    b.dist[(size_t)i * nb + local] = d;
+    if (with_mean) sh.dist[i] = d;
+  }
+  if (with_mean) {
+    __syncthreads();
+    if (threadIdx.x == 0 && nout > 0) {  // the mean (ms.rs:417-423), as k_mean computes it
+      uint64_t acc = 0;
+      for (uint32_t i = 0; i < nout; ++i) acc = ts_add4_rn(acc, dbl_bits(sh.dist[i]));
+      b.mean[local] = bits_dbl(ts_div_int_rn(acc, nout * 4u));
+    }
   }
   if (threadIdx.x == 0) b.ncnt[local] = nout;
 }
@@ -364,9 +521,10 @@ __global__ void __launch_bounds__(128) k_mean(SessionDev s, StageDev st, BatchDe
   if (local >= nb) return;
   const uint32_t nk = b.ncnt[local];
   if (nk == 0) return;
-  // one item per lane: 32 chains share each f64 warp instruction
+  // one item per lane: 32 chains share each f64 warp instruction, which on
+  // GB300 costs the same whatever its active-lane count
   double sum = 0.0;
-#pragma unroll 4
+#pragma unroll 8
   for (uint32_t j = 0; j < nk; ++j) {
     const double d = b.dist[(size_t)j * nb + local];
     sum = __dadd_rn(sum, d);
@@ -374,9 +532,7 @@ __global__ void __launch_bounds__(128) k_mean(SessionDev s, StageDev st, BatchDe
     sum = __dadd_rn(sum, d);
     sum = __dadd_rn(sum, d);
   }
-  const double avg = __ddiv_rn(sum, (double)(nk * 4u));
-  b.mean[local] = avg;
-  b.minv[local] = __drcp_rn(avg);
+  b.mean[local] = __ddiv_rn(sum, (double)(nk * 4u));
 }
 
 // ---------------------------------------------------------------------------
@@ -428,13 +584,14 @@ __device__ __forceinline__ float lut4(const float *lut, uint32_t d, float acc) {
 }
 
 // Cost of candidate c (better_match, ms.rs:1225-1288), abandoning as soon as
-// the partial sum reaches `bound`; bounds-checked gathers.  Returns false
+// the partial sum reaches `bound`; bounds-checked gathers (out-of-bounds
+// texels read Rgba(0,0,0,255)), issued four neighbours ahead.  Returns false
 // when abandoned.
 __device__ __forceinline__ bool candidate_cost(const SessionDev &s, const StageDev &st, const WarpSmem &w,
                                                const float *lc, const float *lg, uint32_t nk, uint32_t cxy,
                                                uint32_t aux, float bound, float &out) {
   const uint32_t map = aux & 0x7fffu;
-  const bool neg = (aux & kAuxNeg) != 0;
+  const int sg = (aux & kAuxNeg) ? -1 : 1;
   const MapDesc md = s.maps[map];
   const uint32_t *lv = s.levels + md.off + (size_t)st.level * md.w * md.h;
   const int cx = (int)(cxy & 0xffffu), cy = (int)(cxy >> 16);
@@ -445,23 +602,28 @@ __device__ __forceinline__ bool candidate_cost(const SessionDev &s, const StageD
     gv = s.guides + gd.off + (size_t)st.level * gd.w * gd.h;
   }
   float score = 0.0f;
-  for (uint32_t j = 0; j < nk; ++j) {
-    const uint4 nr = w.nbr[j];
-    int dx = off_dx((int32_t)nr.x), dy = off_dy((int32_t)nr.x);
-    if (neg) {
-      dx = -dx;
-      dy = -dy;
+  for (uint32_t j0 = 0; j0 < nk; j0 += 4) {
+    uint4 nr[4];
+    uint32_t t[4], gt[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      t[u] = kOutside;
+      gt[u] = kOutside;
+      if (j0 + u < nk) {
+        nr[u] = w.nbr[j0 + u];
+        const int qx = cx + sg * off_dx((int32_t)nr[u].x), qy = cy + sg * off_dy((int32_t)nr[u].x);
+        if ((unsigned)qx < md.w && (unsigned)qy < md.h) t[u] = __ldg(&lv[(size_t)qy * md.w + qx]);
+        if (s.guided && (unsigned)qx < gd.w && (unsigned)qy < gd.h) gt[u] = __ldg(&gv[(size_t)qy * gd.w + qx]);
+      }
     }
-    const int qx = cx + dx, qy = cy + dy;
-    const uint32_t t = texel(lv, md, qx, qy);
-    float nps = lut4(lc, __vabsdiffu4(nr.y, t), 0.0f);
-    if (s.guided) {
-      uint32_t gt = kOutside;
-      if ((unsigned)qx < gd.w && (unsigned)qy < gd.h) gt = __ldg(&gv[(size_t)qy * gd.w + qx]);
-      nps = lut4(lg, __vabsdiffu4(nr.z, gt), nps);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (j0 + u >= nk) break;
+      float nps = lut4(lc, __vabsdiffu4(nr[u].y, t[u]), 0.0f);
+      if (s.guided) nps = lut4(lg, __vabsdiffu4(nr[u].z, gt[u]), nps);
+      score = __fadd_rn(score, __fmul_rn(nps, __uint_as_float(nr[u].w)));
+      if (score >= bound) return false;
     }
-    score = __fadd_rn(score, __fmul_rn(nps, __uint_as_float(nr.w)));
-    if (score >= bound) return false;
   }
   out = score;
   return true;
@@ -524,13 +686,14 @@ __device__ __forceinline__ bool candidate_cost_padded(const SessionDev &s, const
 // shift to the centre, kept if valid.  Returns true for a valid candidate.
 __device__ __forceinline__ bool neighbour_setup(const SessionDev &s, const StageDev &st, const BatchDev &b,
                                                 uint32_t local, uint32_t nb, int px, int py, uint32_t j, int32_t off,
-                                                double avg, double inv, const double *tab, const float *tab_ff,
+                                                double avg, const double *tab, const float *tab_ff,
                                                 const WarpSmem &w, uint32_t &cxy, uint32_t &aux, bool &nan_w,
                                                 int &maxoff, bool &bad_map) {
   const int W = (int)s.W, H = (int)s.H;
   const double dj = b.dist[(size_t)j * nb + local];
   float wv;
-  if (!ts_weight_ff(dj, avg, tab_ff, wv)) wv = __double2float_rn(ts_exp64(-1.0 * ts_div_markstein(dj, avg, inv), tab));
+  if (!ts_weight_ff(dj, avg, tab_ff, wv))
+    wv = __double2float_rn(ts_exp64(-1.0 * ts_div_markstein(dj, avg, __drcp_rn(avg)), tab));
   nan_w |= (wv != wv);
   maxoff = max(maxoff, max(abs(off_dx(off)), abs(off_dy(off))));
   const int nx = px + off_dx(off), ny = py + off_dy(off);
@@ -708,7 +871,7 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve(SessionDev 
       continue;
     }
     const int32_t *nbo = b.nbuf + (size_t)local * s.k;
-    const double avg = b.mean[local], inv = b.minv[local];
+    const double avg = b.mean[local];
     // neighbours: offsets, weights, own pattern, coherence candidates
     bool nan_w = false;
     int maxoff = 0;
@@ -719,7 +882,7 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve(SessionDev 
       bool valid = false;
       uint32_t cxy = 0, aux = 0;
       if (j < nk)
-        valid = neighbour_setup(s, st, b, local, nb, px, py, j, nbo[j], avg, inv, tab, tab_ff, w, cxy, aux, nan_w,
+        valid = neighbour_setup(s, st, b, local, nb, px, py, j, nbo[j], avg, tab, tab_ff, w, cxy, aux, nan_w,
                                 maxoff, bad_map);
       const uint32_t bal = __ballot_sync(0xffffffffu, valid);
       if (valid) {
@@ -797,7 +960,7 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve(SessionDev 
 // result is the reference's.  Latency per item is about one candidate's
 // evaluation, which suits batches too small to fill the GPU with warps.
 // ---------------------------------------------------------------------------
-template <int T>
+template <int T, bool kFull>
 __global__ void __launch_bounds__(T) k_resolve_team(SessionDev s, StageDev st, BatchDev b) {
   constexpr int NW = T / 32;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -835,7 +998,7 @@ __global__ void __launch_bounds__(T) k_resolve_team(SessionDev s, StageDev st, B
     }
     __syncthreads();
     const int32_t *nbo = b.nbuf + (size_t)local * s.k;
-    const double avg = b.mean[local], inv = b.minv[local];
+    const double avg = b.mean[local];
     bool nan_w = false, bad_map = false;
     int maxoff = 0;
     uint32_t ncoh = 0;
@@ -844,7 +1007,7 @@ __global__ void __launch_bounds__(T) k_resolve_team(SessionDev s, StageDev st, B
       bool valid = false;
       uint32_t cxy = 0, aux = 0;
       if (j < nk)
-        valid = neighbour_setup(s, st, b, local, nb, px, py, j, nbo[j], avg, inv, tab, tab_ff, w, cxy, aux, nan_w,
+        valid = neighbour_setup(s, st, b, local, nb, px, py, j, nbo[j], avg, tab, tab_ff, w, cxy, aux, nan_w,
                                 maxoff, bad_map);
       // order-preserving compaction of the valid coherence candidates
       const uint32_t bal = __ballot_sync(0xffffffffu, valid);
@@ -884,7 +1047,78 @@ __global__ void __launch_bounds__(T) k_resolve_team(SessionDev s, StageDev st, B
     const uint32_t nc = ncoh + s.m;
     float best_s = FLT_MAX;
     uint32_t best_i = 0;
-    if (!slow) {
+    if (!slow && kFull) {
+      // every term nps(c, j) * w_j in parallel (consecutive threads take
+      // consecutive neighbours of one candidate), then each candidate's
+      // in-order sum on one thread: the reference's scores, all of them
+      uint32_t c = tid / nk, j = tid - c * nk;
+      const uint32_t dc = T / nk, dj = T - dc * nk;
+      for (uint32_t i = tid; i < nc * nk; i += T) {
+        const uint32_t cxy = w.cxy[c], aux = w.caux[c];
+        const uint32_t map = aux & 0x7fffu;
+        const int sg = (aux & kAuxNeg) ? -1 : 1;
+        const MapDesc md = s.maps[map];
+        const uint4 nr = w.nbr[j];
+        const int qx = (int)(cxy & 0xffffu) + sg * off_dx((int32_t)nr.x);
+        const int qy = (int)(cxy >> 16) + sg * off_dy((int32_t)nr.x);
+        uint32_t t = kOutside;
+        if ((unsigned)qx < md.w && (unsigned)qy < md.h)
+          t = __ldg(&s.levels[md.off + (size_t)st.level * md.w * md.h + (size_t)qy * md.w + qx]);
+        float nps = lut4(lc, __vabsdiffu4(nr.y, t), 0.0f);
+        if (s.guided) {
+          const GuideDesc gd = s.gdesc[map];
+          uint32_t gt = kOutside;
+          if ((unsigned)qx < gd.w && (unsigned)qy < gd.h)
+            gt = __ldg(&s.guides[gd.off + (size_t)st.level * gd.w * gd.h + (size_t)qy * gd.w + qx]);
+          nps = lut4(lg, __vabsdiffu4(nr.z, gt), nps);
+        }
+        term[i] = __fmul_rn(nps, __uint_as_float(nr.w));
+        c += dc;
+        j += dj;
+        if (j >= nk) {
+          j -= nk;
+          ++c;
+        }
+      }
+      __syncthreads();
+      float my_s = FLT_MAX;
+      uint32_t my_i = 0xffffffffu;
+      for (uint32_t cc = tid; cc < nc; cc += T) {
+        float sc = 0.0f;
+        const float *tc = term + (size_t)cc * nk;
+        for (uint32_t jj = 0; jj < nk; ++jj) sc = __fadd_rn(sc, tc[jj]);
+        if (sc < my_s) {  // first strict minimum among this thread's candidates
+          my_s = sc;
+          my_i = cc;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, my_s, o);
+        const uint32_t oi = __shfl_xor_sync(0xffffffffu, my_i, o);
+        if (ov < my_s || (ov == my_s && oi < my_i)) {
+          my_s = ov;
+          my_i = oi;
+        }
+      }
+      if (lane == 0) {
+        red_s[warp] = my_s;
+        red_i[warp] = my_i;
+      }
+      __syncthreads();
+      best_s = red_s[0];
+      best_i = red_i[0];
+      for (int i = 1; i < NW; ++i) {
+        if (red_s[i] < best_s || (red_s[i] == best_s && red_i[i] < best_i)) {
+          best_s = red_s[i];
+          best_i = red_i[i];
+        }
+      }
+      if (best_i == 0xffffffffu) {  // no score below f32::MAX: the reference keeps candidate 0
+        best_s = FLT_MAX;
+        best_i = 0;
+      }
+    } else if (!slow) {
       // S_0: candidate 0's terms nps_j * w_j in parallel, summed in order
       {
         const uint32_t cxy0 = w.cxy[0], aux0 = w.caux[0];
@@ -1083,6 +1317,11 @@ inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b
 
 size_t resolve_smem_bytes(uint32_t k, uint32_t m, int) { return 2048 + (size_t)kResolveWarps * warp_smem_bytes(k, m); }
 static size_t team_smem_bytes(uint32_t k, uint32_t m) { return 2048 + warp_smem_bytes(k, m) + (size_t)(k ? k : 1) * 4; }
+// the full-evaluation team form keeps every (candidate, neighbour) term
+static size_t team_full_smem_bytes(uint32_t k, uint32_t m) {
+  return 2048 + warp_smem_bytes(k, m) + (size_t)(k ? k : 1) * (k + m) * 4;
+}
+constexpr size_t kTeamFullMaxSmem = 96 * 1024;
 
 cudaError_t configure_kernels(uint32_t k, uint32_t m) {
   const size_t smem = resolve_smem_bytes(k, m, 0);
@@ -1090,9 +1329,19 @@ cudaError_t configure_kernels(uint32_t k, uint32_t m) {
     cudaError_t e = cudaFuncSetAttribute(k_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
+  cudaError_t e = cudaFuncSetAttribute(k_knn_exhaustive, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       kExhAllKeys * 8);
+  if (e != cudaSuccess) return e;
   const size_t tsm = team_smem_bytes(k, m);
-  if (tsm > 48 * 1024)
-    return cudaFuncSetAttribute(k_resolve_team<kTeamThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm);
+  if (tsm > 48 * 1024) {
+    e = cudaFuncSetAttribute(k_resolve_team<kTeamThreads, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tsm);
+    if (e != cudaSuccess) return e;
+  }
+  const size_t fsm = team_full_smem_bytes(k, m);
+  if (fsm > 48 * 1024 && fsm <= kTeamFullMaxSmem)
+    return cudaFuncSetAttribute(k_resolve_team<kTeamThreads, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)fsm);
   return cudaSuccess;
 }
 
@@ -1111,8 +1360,8 @@ void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchD
                            cudaStream_t stream) {
   const uint32_t n = b.i1 - b.i0;
   if (n == 0) return;
-  const uint32_t grid = n < 1216u ? n : 1216u;  // 152 SMs x 8 CTAs, grid-stride beyond
-  k_knn_exhaustive<<<grid, kExhThreads, 0, stream>>>(s, st, b, all_items ? 1 : 0);
+  const uint32_t grid = n < 608u ? n : 608u;  // 152 SMs x 4 CTAs, grid-stride beyond
+  k_knn_exhaustive<<<grid, kExhThreads, (size_t)kExhAllKeys * 8, stream>>>(s, st, b, all_items ? 1 : 0);
 }
 
 void launch_mean(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
@@ -1128,11 +1377,15 @@ void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, 
   k_resolve<<<cdiv(n, kResolveWarps), kResolveWarps * kWarp, smem, stream>>>(s, st, b);
 }
 
-void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
+void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev &b, bool full,
+                         cudaStream_t stream) {
   const uint32_t n = b.i1 - b.i0;
   if (n == 0) return;
   const uint32_t grid = n < 152u * 16u ? n : 152u * 16u;
-  k_resolve_team<kTeamThreads><<<grid, kTeamThreads, team_smem_bytes(s.k, s.m), stream>>>(s, st, b);
+  if (full && team_full_smem_bytes(s.k, s.m) <= kTeamFullMaxSmem)
+    k_resolve_team<kTeamThreads, true><<<grid, kTeamThreads, team_full_smem_bytes(s.k, s.m), stream>>>(s, st, b);
+  else
+    k_resolve_team<kTeamThreads, false><<<grid, kTeamThreads, team_smem_bytes(s.k, s.m), stream>>>(s, st, b);
 }
 
 void launch_commit(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {

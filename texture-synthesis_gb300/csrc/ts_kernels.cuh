@@ -111,18 +111,22 @@ struct BatchDev {
   uint32_t *fb_count;
   double *dist;          // [k][batch] squared normalised distances
   double *mean;          // [batch] mean of the 4x-duplicated distance list
-  double *minv;          // [batch] RN(1 / mean)
   Result *res;           // [batch]
 };
 
 // Launchers (stream-ordered, no synchronisation).
 void launch_random_candidates(const SessionDev &s, const StageDev &st, cudaStream_t stream);
 void launch_knn_walk(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
+// all_items: every item of the batch (and the mean too); otherwise the items
+// the walk left in fb_list.
 void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchDev &b, bool all_items,
                            cudaStream_t stream);
 void launch_mean(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
 void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
-void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
+// One CTA per item; `full` scores every candidate completely (lowest latency,
+// for batches far too small to fill the GPU), otherwise candidate 0 first
+// and the rest with early exit.
+void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev &b, bool full, cudaStream_t stream);
 void launch_commit(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
 void launch_level_switch(const SessionDev &s, uint32_t level, uint32_t n_res, cudaStream_t stream);
 

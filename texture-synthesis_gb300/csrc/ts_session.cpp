@@ -85,6 +85,7 @@ struct Params {
   int device = 0;
   bool profile = false;
   uint32_t team_max_batch = 8192;
+  uint32_t team_full_max_batch = 1024;
 };
 
 std::string fmt_float(float v) {
@@ -264,6 +265,7 @@ struct ts_generated {
   std::vector<uint32_t> resolved;
   std::vector<float> scores;
   ts_run_stats stats{};
+  std::vector<ts_launch_record> launches;
 };
 
 extern "C" {
@@ -474,9 +476,10 @@ int ts_builder_device(ts_builder *b, int32_t device) {
   b->prm.device = device;
   return TS_OK;
 }
-int ts_builder_resolve_team(ts_builder *b, uint32_t team_max_batch) {
+int ts_builder_resolve_team(ts_builder *b, uint32_t team_max_batch, uint32_t full_max_batch) {
   BUILDER_GUARD(b);
   b->prm.team_max_batch = team_max_batch;
+  b->prm.team_full_max_batch = full_max_batch;
   return TS_OK;
 }
 int ts_builder_profile_kernels(ts_builder *b, int32_t on) {
@@ -763,13 +766,20 @@ namespace {
 
 // Per-launch CUDA event pairs, recorded only when profiling is on.
 struct LaunchTimer {
+  struct Rec {
+    int kind, stage;
+    uint32_t items;
+    cudaEvent_t a, b;
+  };
   bool on = false;
   cudaStream_t st = 0;
-  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev;
+  int stage = -1;
+  uint32_t items = 0;
+  std::vector<Rec> ev;
   ~LaunchTimer() {
     for (auto &e : ev) {
-      cudaEventDestroy(e.second.first);
-      cudaEventDestroy(e.second.second);
+      cudaEventDestroy(e.a);
+      cudaEventDestroy(e.b);
     }
   }
   template <typename F>
@@ -778,20 +788,21 @@ struct LaunchTimer {
       f();
       return;
     }
-    cudaEvent_t a, b;
-    CUDA_TRY(cudaEventCreate(&a));
-    CUDA_TRY(cudaEventCreate(&b));
-    CUDA_TRY(cudaEventRecord(a, st));
+    Rec r{kind, stage, items, nullptr, nullptr};
+    CUDA_TRY(cudaEventCreate(&r.a));
+    CUDA_TRY(cudaEventCreate(&r.b));
+    CUDA_TRY(cudaEventRecord(r.a, st));
     f();
-    CUDA_TRY(cudaEventRecord(b, st));
-    ev.push_back({kind, {a, b}});
+    CUDA_TRY(cudaEventRecord(r.b, st));
+    ev.push_back(r);
   }
-  void collect(ts_run_stats &out) {
+  void collect(ts_run_stats &out, std::vector<ts_launch_record> &recs) {
     for (auto &e : ev) {
       float ms = 0.0f;
-      CUDA_TRY(cudaEventElapsedTime(&ms, e.second.first, e.second.second));
-      out.kernel_count[e.first] += 1;
-      out.kernel_ms[e.first] += ms;
+      CUDA_TRY(cudaEventElapsedTime(&ms, e.a, e.b));
+      out.kernel_count[e.kind] += 1;
+      out.kernel_ms[e.kind] += ms;
+      recs.push_back(ts_launch_record{e.kind, e.stage, e.items, ms});
     }
   }
 };
@@ -970,7 +981,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     DevBuf<uint32_t> d_color, d_occ, d_mir, d_res, d_items, d_ncnt, d_fbl, d_fbc;
     DevBuf<uint4> d_state;
     DevBuf<float> d_rscore, d_lut;
-    DevBuf<double> d_xdiv, d_ydiv, d_dist, d_dxt, d_dy2t, d_mean, d_minv;
+    DevBuf<double> d_xdiv, d_ydiv, d_dist, d_dxt, d_dy2t, d_mean;
     DevBuf<int32_t> d_tab, d_nbuf;
     DevBuf<uint2> d_rcand;
     DevBuf<Result> d_result;
@@ -992,7 +1003,6 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     CUDA_TRY(d_ncnt.alloc(max_batch_items));
     CUDA_TRY(d_dist.alloc((size_t)max_batch_items * std::max<uint32_t>(k, 1)));
     CUDA_TRY(d_mean.alloc(max_batch_items));
-    CUDA_TRY(d_minv.alloc(max_batch_items));
     CUDA_TRY(d_fbl.alloc(max_batch_items));
     CUDA_TRY(d_fbc.alloc(n_batches));
     CUDA_TRY(d_result.alloc(max_batch_items));
@@ -1108,6 +1118,8 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     std::vector<uint8_t> prog_img;
     for (size_t si = 0; si < plan.size(); ++si) {
       const StagePlan &sp = plan[si];
+      lt.stage = sp.p_stage;
+      lt.items = sp.n_items;
       if (sp.level_switch) {
         lt.run(TS_KERNEL_LEVEL_SWITCH, [&] { launch_level_switch(sd, sp.level, sp.n_res_start, st); });
         ++launches;
@@ -1137,6 +1149,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
         chunk.stage_seed = sp.seed;  // resolve_at_random uses the stage seed itself
         for (size_t bk = bi; bk < bj; ++bk) {
           const BatchPlan &bp = sp.batches[bk];
+          lt.items = bp.i1 - bp.i0;
           BatchDev bd{};
           bd.i0 = bp.i0 - c0;
           bd.i1 = bp.i1 - c0;
@@ -1148,7 +1161,6 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
           bd.fb_count = d_fbc.p + fb_index++;
           bd.dist = d_dist.p;
           bd.mean = d_mean.p;
-          bd.minv = d_minv.p;
           bd.res = d_result.p;
           if (k > 0) {
             if (bp.exhaustive) {
@@ -1160,12 +1172,13 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
               launches += 2;
             }
           }
-          if (k > 0) {
+          if (k > 0 && !bp.exhaustive) {  // the exhaustive k-NN over a whole batch computes the mean itself
             lt.run(TS_KERNEL_MEAN, [&] { launch_mean(sd, chunk, bd, st); });
             ++launches;
           }
           if (bp.i1 - bp.i0 <= p.team_max_batch)
-            lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve_team(sd, chunk, bd, st); });
+            lt.run(TS_KERNEL_RESOLVE,
+                   [&] { launch_resolve_team(sd, chunk, bd, bp.i1 - bp.i0 <= p.team_full_max_batch, st); });
           else
             lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve(sd, chunk, bd, st); });
           lt.run(TS_KERNEL_COMMIT, [&] { launch_commit(sd, chunk, bd, st); });
@@ -1231,7 +1244,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     g->stats.stages = plan.size();
     g->stats.kernel_launches = launches;
     g->stats.gpu_ms = ms;
-    lt.collect(g->stats);
+    lt.collect(g->stats, g->launches);
     g->stats.cost_evals = evals;
   } catch (const Failure &f) {
     s->err = f.msg;
@@ -1276,6 +1289,12 @@ int ts_generated_resolved(const ts_generated *g, uint32_t *flat, float *score) {
 }
 void ts_generated_stats(const ts_generated *g, ts_run_stats *out) {
   if (g && out) *out = g->stats;
+}
+uint64_t ts_generated_launch_count(const ts_generated *g) { return g ? g->launches.size() : 0; }
+int ts_generated_launches(const ts_generated *g, ts_launch_record *out) {
+  if (!g || !out) return TS_ERR_NULL;
+  if (!g->launches.empty()) memcpy(out, g->launches.data(), g->launches.size() * sizeof(ts_launch_record));
+  return TS_OK;
 }
 void ts_generated_free(ts_generated *g) { delete g; }
 
