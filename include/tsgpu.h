@@ -144,6 +144,15 @@ typedef struct ts_run_stats {
 const char *ts_status_str(int status);
 void ts_get_limits(ts_limits *out);
 
+/* ImagePyramid::new(img, Some(levels)) (img_pyramid.rs:7-37) on the device:
+ * max(levels, 1) RGBA8 images of width x height, coarsest first, each level
+ * a Gaussian downscale by 2^i resized back up; the last is the image itself.
+ * rgba and out_rgba are host buffers (out: max(levels,1)*width*height*4
+ * bytes).  The session builds the same pyramids for its examples and
+ * guides. */
+int ts_image_pyramid(const uint8_t *rgba, uint32_t width, uint32_t height, uint32_t levels, uint8_t *out_rgba,
+                     int32_t device);
+
 /* ---- SessionBuilder (session.rs:69-448) ---------------------------------- */
 
 /* Session::builder(): a builder with the reference defaults (lib.rs:342-359):

@@ -205,3 +205,30 @@ def test_seeds(ts, oracle, wl, seed):
     spec["params"]["seed"] = seed
     got, ref = run_both(ts, oracle, spec)
     assert_same(got, ref, "seed %d" % seed)
+
+
+def _golden_cases():
+    import glob
+    import os
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    return sorted(glob.glob(os.path.join(here, "golden", "*.npz")))
+
+
+@pytest.mark.parametrize("path", _golden_cases(), ids=lambda p: p.rsplit("/", 1)[-1])
+def test_gpu_matches_golden_fixture(ts, path):
+    """The GPU path reproduces the committed oracle fixtures (made on another
+    machine) bit for bit."""
+    import importlib.util
+    import os
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    sp = importlib.util.spec_from_file_location("make_golden", os.path.join(here, "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(sp)
+    sp.loader.exec_module(mg)
+    d = np.load(path)
+    spec, divisor = mg.unpack(d)
+    got = ts.run_spec(spec, batch_divisor=divisor)
+    ref = {k: d["out_" + k] for k in KEYS}
+    ref["evals"] = int(d["out_evals"])
+    assert_same(got, ref, os.path.basename(path))

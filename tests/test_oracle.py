@@ -1,0 +1,213 @@
+"""The CPU oracle on its own: the RNG against an independent Python
+restatement of the published PCG32 / rand 0.8 algorithms, the k-NN tie rule
+against brute force, the resize against a Python restatement, and
+properties of whole runs (determinism, thread-count independence, every
+pixel resolved, colours taken from the final pyramid level at the recorded
+source coordinates, patch/map ids consistent with their candidates)."""
+import numpy as np
+import pytest
+
+M64 = (1 << 64) - 1
+MUL = 6364136223846793005
+SEED_INC = 11634580027462260723
+
+
+def out32(s):
+    xs = (((s >> 18) ^ s) >> 27) & 0xFFFFFFFF
+    rot = s >> 59
+    return ((xs >> rot) | (xs << ((32 - rot) & 31))) & 0xFFFFFFFF
+
+
+class Pcg:
+    """PCG XSH RR 64/32 seeded the way rand_core 0.6 seed_from_u64 and
+    rand_pcg 0.3 Lcg64Xsh32::from_seed do."""
+
+    def __init__(self, seed):
+        words = []
+        x = seed & M64
+        for _ in range(4):
+            x = (x * MUL + SEED_INC) & M64
+            words.append(out32(x))
+        self.inc = (words[2] | (words[3] << 32)) | 1
+        self.state = ((words[0] | (words[1] << 32)) + self.inc) & M64
+        self.state = (self.state * MUL + self.inc) & M64
+
+    def u32(self):
+        s = self.state
+        self.state = (s * MUL + self.inc) & M64
+        return out32(s)
+
+    def u64(self):
+        lo = self.u32()
+        hi = self.u32()
+        return lo | (hi << 32)
+
+    def range32(self, n):
+        zone = ((n << (32 - n.bit_length())) & 0xFFFFFFFF) - 1
+        while True:
+            m = self.u32() * n
+            if (m & 0xFFFFFFFF) <= zone:
+                return m >> 32
+
+    def range64(self, n):
+        zone = ((n << (64 - n.bit_length())) & M64) - 1
+        while True:
+            m = self.u64() * n
+            if (m & M64) <= zone:
+                return m >> 64
+
+
+def test_pcg_stream_matches_restatement(oracle):
+    import ctypes as C
+
+    out = np.zeros(16, np.uint32)
+    for seed in [0, 1, 2, 211, 12345678901234, M64, 1 << 63]:
+        oracle.lib().tso_pcg_stream(seed, 16, out.ctypes.data)
+        g = Pcg(seed)
+        assert [int(v) for v in out] == [g.u32() for _ in range(16)], seed
+        st, inc = C.c_uint64(), C.c_uint64()
+        oracle.lib().tso_pcg_seed(seed, C.byref(st), C.byref(inc))
+        g = Pcg(seed)
+        assert (st.value, inc.value) == (g.state, g.inc)
+
+
+def test_gen_range_matches_restatement(oracle):
+    rng = np.random.default_rng(1)
+    for _ in range(3000):
+        seed = int(rng.integers(0, 1 << 62))
+        n32 = int(rng.integers(1, 1 << 20))
+        n64 = int(rng.integers(1, 1 << 40))
+        assert oracle.lib().tso_gen_range_u32(seed, n32) == Pcg(seed).range32(n32)
+        assert oracle.lib().tso_gen_range_u64(seed, n64) == Pcg(seed).range64(n64)
+    # power-of-two and unit ranges reject half of all draws (zone rule)
+    for seed in range(200):
+        assert oracle.lib().tso_gen_range_u64(seed, 1) == 0
+        assert oracle.lib().tso_gen_range_u32(seed, 128) == Pcg(seed).range32(128)
+
+
+def brute_knn(W, H, tiling, occ, mir, px, py, k):
+    xl, yb = int(np.float32(W) * np.float32(0.05)), int(np.float32(H) * np.float32(0.05))
+    xr, yt = W - xl, H - yb
+    pts = []
+    for y in range(H):
+        for x in range(W):
+            if occ[y, x]:
+                pts.append((x, y))
+                if tiling and mir[y, x]:
+                    if x < xl:
+                        pts.append((x + W, y))
+                    elif x > xr:
+                        pts.append((x - W, y))
+                    if y < yb:
+                        pts.append((x, y + H))
+                    elif y > yt:
+                        pts.append((x, y - H))
+    pts.sort(key=lambda p: ((p[0] - px) ** 2 + (p[1] - py) ** 2, p[1], p[0]))
+    return pts[:k]
+
+
+@pytest.mark.parametrize("tiling", [False, True])
+def test_knn_tie_rule(oracle, tiling):
+    rng = np.random.default_rng(2 + tiling)
+    for t in range(60):
+        W, H = int(rng.integers(6, 48)), int(rng.integers(6, 48))
+        occ = (rng.random((H, W)) < rng.uniform(0.02, 0.7)).astype(np.uint8)
+        mir = (occ & (rng.random((H, W)) < 0.8)).astype(np.uint8)
+        k = int(rng.integers(1, 60))
+        px, py = int(rng.integers(0, W)), int(rng.integers(0, H))
+        got = [tuple(p) for p in oracle.knn(W, H, tiling, occ, mir, px, py, k)]
+        assert got == brute_knn(W, H, tiling, occ, mir, px, py, k), (t, W, H, k)
+
+
+def test_exp_is_close_to_libm(oracle):
+    import math
+
+    for x in np.linspace(-60, 0, 5001):
+        v = oracle.lib().tso_exp_export(float(x))
+        assert abs(v - math.exp(x)) <= 2 * math.ulp(math.exp(x))
+
+
+def test_resize_weights_sum_and_identity(oracle, wl):
+    img = wl.texture(3, 40, 30)
+    assert (oracle.resize(img, 30, 40, "catmullrom") == img).all()
+    assert (oracle.resize(img, 30, 40, "gaussian") != img).any()  # the Gaussian smooths even at 1:1
+    flat = np.full((17, 23, 4), 77, np.uint8)
+    for f in ("triangle", "catmullrom", "gaussian"):
+        assert (oracle.resize(flat, 9, 31, f) == 77).all(), f
+
+
+def test_pyramid_levels(oracle, wl):
+    img = wl.texture(4, 64, 64)
+    p = oracle.pyramid(img, 5)
+    assert p.shape == (5, 64, 64, 4)
+    assert (p[-1] == img).all()
+    # coarser levels are smoother: neighbouring-pixel differences shrink
+    rough = [np.abs(np.diff(p[l].astype(int), axis=1)).mean() for l in range(5)]
+    assert rough[0] < rough[2] < rough[4]
+    # a level whose downscale has a zero side is all zeros (the crate's empty resize)
+    tiny = oracle.pyramid(wl.texture(5, 6, 6), 4)
+    assert (tiny[0] == 0).all()
+
+
+def check_run_properties(spec, r):
+    W, H = spec["out_w"], spec["out_h"]
+    assert sorted(set(r["resolved"].tolist())) == list(range(W * H)) or spec.get("inpaint_mask") is not None
+    levels = max(1, spec["params"]["backtrack_stages"])
+    maps = [e for e in spec["examples"] if e.get("sample", "all") != "ignore"]
+    from oracle import oracle as o
+
+    finals = [o.pyramid(e["image"], spec["params"]["backtrack_stages"])[levels - 1] for e in maps]
+    c = r["coord"].reshape(-1, 3)
+    img = r["image"].reshape(-1, 4)
+    for i in range(W * H):
+        x, y, m = c[i]
+        assert (img[i] == finals[m][y, x]).all(), i
+
+
+def test_run_determinism_and_threads(oracle, wl):
+    spec = wl.config1(out=48, ex=24)
+    a = oracle.run(spec, batch_divisor=8, nthreads=1)
+    b = oracle.run(spec, batch_divisor=8, nthreads=6)
+    for key in ("image", "coord", "id", "resolved"):
+        assert (a[key] == b[key]).all(), key
+    assert (a["scores"].view(np.uint32) == b["scores"].view(np.uint32)).all()
+    assert a["evals"] == b["evals"]
+    check_run_properties(spec, a)
+
+
+def test_sequential_schedule(oracle, wl):
+    spec = wl.config0(out=20, ex=16)
+    r = oracle.run(spec, batch_divisor=0)
+    assert r["batches"] == r["resolves"]  # one item per batch step
+    check_run_properties(spec, r)
+
+
+def test_guided_and_inpaint_properties(oracle, wl):
+    spec = wl.config2(out=40, ex=24)
+    check_run_properties(spec, oracle.run(spec))
+    spec = wl.inpaint_session(9, side=40)
+    r = oracle.run(spec)
+    locked = spec["inpaint_mask"][..., 0] == 255
+    assert (r["image"][locked] == spec["examples"][0]["image"][locked]).all()
+    assert (r["coord"][locked][:, :2] == np.argwhere(locked)[:, ::-1]).all()
+
+
+def test_random_init_counts(oracle, wl):
+    spec = wl.config0(out=24, ex=16)
+    spec["params"]["random_init"] = 30
+    r = oracle.run(spec)
+    # resolved list: 30 random-init pixels first, then every other pixel once
+    assert len(r["resolved"]) == 24 * 24
+    assert (r["scores"][:30] == 0).all()
+
+
+def test_errors(oracle, wl):
+    spec = wl.config0(out=16, ex=8)
+    spec["params"]["random_init"] = 16 * 16 + 1
+    with pytest.raises(RuntimeError):
+        oracle.run(spec)
+    spec = wl.config0(out=16, ex=8)
+    spec["examples"][0]["sample"] = "image"
+    spec["examples"][0]["mask"] = np.zeros((8, 8, 4), np.uint8)
+    with pytest.raises(RuntimeError):
+        oracle.run(spec)

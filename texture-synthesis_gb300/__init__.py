@@ -93,6 +93,7 @@ _PROGRESS_FN = C.CFUNCTYPE(None, C.POINTER(_Progress), C.c_void_p)
 SIGNATURES = {
     "ts_status_str": (C.c_char_p, [C.c_int]),
     "ts_get_limits": (None, [C.POINTER(_Limits)]),
+    "ts_image_pyramid": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_int32]),
     "ts_builder_new": (C.c_void_p, []),
     "ts_builder_free": (None, [C.c_void_p]),
     "ts_builder_last_error": (C.c_char_p, [C.c_void_p]),
@@ -160,6 +161,18 @@ def limits():
     out = _Limits()
     lib().ts_get_limits(C.byref(out))
     return {f: getattr(out, f) for f, _ in out._fields_}
+
+
+def image_pyramid(image, levels, device=0):
+    """ImagePyramid::new(image, Some(levels)) on the device: an array of
+    max(levels, 1) x H x W x 4, coarsest level first."""
+    img = _rgba(image)
+    h, w = img.shape[:2]
+    out = np.empty((max(1, levels), h, w, 4), np.uint8)
+    rc = lib().ts_image_pyramid(img.ctypes.data, w, h, levels, out.ctypes.data, device)
+    if rc:
+        raise Error(rc, "ts_image_pyramid")
+    return out
 
 
 @dataclass(frozen=True)

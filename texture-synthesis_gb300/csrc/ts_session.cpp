@@ -299,6 +299,24 @@ void ts_get_limits(ts_limits *out) {
   out->max_image_side = kMaxSide;
 }
 
+int ts_image_pyramid(const uint8_t *rgba, uint32_t w, uint32_t h, uint32_t levels, uint8_t *out, int32_t device) {
+  if (!rgba || !out) return TS_ERR_NULL;
+  if (w == 0 || h == 0) return TS_ERR_IMAGE;
+  if (w > kMaxSide || h > kMaxSide || levels > 30) return TS_ERR_LIMIT;
+  try {
+    CUDA_TRY(cudaSetDevice(device));
+    const uint32_t nl = levels == 0 ? 1 : levels;
+    Image img = copy_image(rgba, w, h);
+    DevBuf<uint32_t> d;
+    CUDA_TRY(d.alloc((size_t)w * h * nl));
+    device_pyramid(img, levels, d.p, 0);
+    CUDA_TRY(cudaMemcpy(out, d.p, (size_t)w * h * nl * 4, cudaMemcpyDeviceToHost));
+  } catch (const Failure &f) {
+    return f.status;
+  }
+  return TS_OK;
+}
+
 ts_builder *ts_builder_new(void) { return new (std::nothrow) ts_builder(); }
 void ts_builder_free(ts_builder *b) { delete b; }
 const char *ts_builder_last_error(const ts_builder *b) { return b ? b->err.c_str() : "null builder"; }
