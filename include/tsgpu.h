@@ -153,6 +153,38 @@ void ts_get_limits(ts_limits *out);
 int ts_image_pyramid(const uint8_t *rgba, uint32_t width, uint32_t height, uint32_t levels, uint8_t *out_rgba,
                      int32_t device);
 
+/* ts_image_pyramid_noalloc: no counterpart in the reference.  The same
+ * pyramid as ts_image_pyramid, byte for byte, for callers that cannot let a
+ * library allocate device memory: an engine or renderer that hands its whole
+ * device budget to its own allocator, a framework whose caching allocator
+ * holds the device, or a frame loop where cudaMalloc/cudaFree would stall
+ * the device.  This call allocates nothing and frees nothing.
+ *
+ * d_rgba (width*height*4 bytes) and d_out (max(levels,1)*width*height*4
+ * bytes) are device buffers of the current device, owned by the caller;
+ * they must not overlap.  The work is enqueued on `stream` (a cudaStream_t;
+ * NULL is the legacy default stream) and the call returns without waiting
+ * for it, so d_out is ready once the stream reaches that point.  No buffer
+ * needs to start at zero.
+ *
+ * Intermediate images and filter taps live in one fixed device array of
+ * the library (9.4 MiB, held on every device the library runs on until
+ * the process exits).  Hence the limits: width*height <=
+ * TS_NOALLOC_MAX_PIXELS, each side <= TS_NOALLOC_MAX_SIDE, levels <=
+ * TS_NOALLOC_MAX_LEVELS; larger requests return TS_ERR_LIMIT before any
+ * work is enqueued.  Because that array is shared, two calls on the same
+ * device must not overlap on the device: issue them on one stream or order
+ * them with events, or they race on the array and give wrong images.
+ * The first call on a device looks up the array's device address (a
+ * one-time set-up per device); make it before any stream capture.
+ * Returns TS_OK, TS_ERR_NULL, TS_ERR_IMAGE (zero side), TS_ERR_LIMIT or
+ * TS_ERR_CUDA. */
+#define TS_NOALLOC_MAX_PIXELS (1024u * 1024u)
+#define TS_NOALLOC_MAX_SIDE 4096u
+#define TS_NOALLOC_MAX_LEVELS 16u
+int ts_image_pyramid_noalloc(const uint8_t *d_rgba, uint32_t width, uint32_t height, uint32_t levels, uint8_t *d_out,
+                             void *stream);
+
 /* ---- SessionBuilder (session.rs:69-448) ---------------------------------- */
 
 /* Session::builder(): a builder with the reference defaults (lib.rs:342-359):

@@ -94,6 +94,8 @@ SIGNATURES = {
     "ts_status_str": (C.c_char_p, [C.c_int]),
     "ts_get_limits": (None, [C.POINTER(_Limits)]),
     "ts_image_pyramid": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_int32]),
+    "ts_image_pyramid_noalloc": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p,
+                                           C.c_void_p]),
     "ts_builder_new": (C.c_void_p, []),
     "ts_builder_free": (None, [C.c_void_p]),
     "ts_builder_last_error": (C.c_char_p, [C.c_void_p]),

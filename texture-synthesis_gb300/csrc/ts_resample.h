@@ -105,4 +105,46 @@ inline Taps axis_taps(Filter f, uint32_t in_len, uint32_t out_len) {
   return t;
 }
 
+// axis_taps written into caller storage: left/count/offset per output index
+// packed as {left, count, offset, 0} in `taps4` (out_len entries) and the
+// weights in `weights`.  Returns the weight count, or -1 if more than
+// `weight_cap` weights would be needed.  Same values as axis_taps.
+inline long axis_taps_into(Filter f, uint32_t in_len, uint32_t out_len, uint32_t *taps4, float *weights,
+                           size_t weight_cap) {
+  for (uint32_t o = 0; o < out_len; ++o) {
+    taps4[4 * o] = 0;
+    taps4[4 * o + 1] = 0;
+    taps4[4 * o + 2] = 0;
+    taps4[4 * o + 3] = 0;
+  }
+  if (in_len == 0) return 0;
+  const float ratio = (float)in_len / (float)out_len;
+  const float sratio = ratio < 1.0f ? 1.0f : ratio;
+  const float src_support = filter_support(f) * sratio;
+  size_t nw = 0;
+  for (uint32_t o = 0; o < out_len; ++o) {
+    float c = ((float)o + 0.5f) * ratio;
+    int64_t left = (int64_t)floorf(c - src_support);
+    if (left < 0) left = 0;
+    if (left > (int64_t)in_len - 1) left = (int64_t)in_len - 1;
+    int64_t right = (int64_t)ceilf(c + src_support);
+    if (right < left + 1) right = left + 1;
+    if (right > (int64_t)in_len) right = (int64_t)in_len;
+    c = c - 0.5f;
+    if (nw + (size_t)(right - left) > weight_cap) return -1;
+    const size_t base = nw;
+    float sum = 0.0f;
+    for (int64_t i = left; i < right; ++i) {
+      const float w = filter_eval(f, ((float)i - c) / sratio);
+      weights[nw++] = w;
+      sum += w;
+    }
+    for (size_t i = base; i < nw; ++i) weights[i] /= sum;
+    taps4[4 * o] = (uint32_t)left;
+    taps4[4 * o + 1] = (uint32_t)(right - left);
+    taps4[4 * o + 2] = (uint32_t)base;
+  }
+  return (long)nw;
+}
+
 }  // namespace ts
