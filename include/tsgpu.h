@@ -266,6 +266,58 @@ int ts_session_run(ts_session *s, ts_progress_fn progress, void *user, ts_genera
 void ts_session_free(ts_session *s);
 const char *ts_session_last_error(const ts_session *s);
 
+/* ---- Batched form (no counterpart in the reference) ---------------------
+ * Many independent sessions synthesised together.  Each session's result is
+ * byte-identical to ts_session_run on it (the same batch schedule, the same
+ * kernels' arithmetic); what changes is how the work reaches the GPU: every
+ * batch step of every session becomes one segment of a shared launch per
+ * phase (k-NN, mean, resolve, commit, ...), so one launch carries the step
+ * of up to all sessions at once instead of one tiny launch per session. */
+typedef struct ts_batch ts_batch;
+typedef struct ts_batch_stats {
+  uint64_t sessions;
+  uint64_t steps;          /* global batch steps (the longest session's) */
+  uint64_t launches;       /* kernel launches of the run */
+  uint64_t output_pixels;  /* summed output sizes */
+  uint64_t resolves, cost_evals;
+  double gpu_ms;           /* device time of the run: uploads, launches, read-back */
+  double wall_ms;
+  double plan_ms;          /* host time spent planning the sessions' schedules */
+  /* With ts_batch_profile on: launches and summed device time per phase
+   * (level switch, random candidates, k-NN walk, exhaustive k-NN, mean,
+   * resolve warp form, resolve team form, resolve full team form, commit). */
+  uint64_t phase_launches[9];
+  double phase_ms[9];
+} ts_batch_stats;
+ts_batch *ts_batch_new(int32_t device);
+void ts_batch_free(ts_batch *b);
+const char *ts_batch_last_error(const ts_batch *b);
+/* Hands a built session to the batch: the session is consumed (only
+ * ts_session_free and ts_session_last_error remain valid on it) and is run
+ * by the next ts_batch_run.  Its device must be the batch's. */
+int ts_batch_add(ts_batch *b, ts_session *s);
+uint64_t ts_batch_size(const ts_batch *b);
+/* Launch the whole run as one CUDA graph (captured and instantiated by the
+ * call) instead of stream launches; the results are the same. */
+int ts_batch_use_graph(ts_batch *b, int32_t on);
+/* Time every launch with CUDA events (stream launches only; adds a little
+ * host time per launch). */
+int ts_batch_profile(ts_batch *b, int32_t on);
+/* Host threads that plan the sessions' schedules (default: the hardware
+ * concurrency, at most 32; 1 plans on the calling thread). */
+int ts_batch_plan_threads(ts_batch *b, uint32_t n);
+/* Resolve kernel form per batch step from the step's items summed over all
+ * sessions: one CTA per item up to team_max_items (every candidate scored
+ * in full up to full_max_items), one warp per item above.  Defaults 8192
+ * and 1024; the results do not depend on them. */
+int ts_batch_resolve_team(ts_batch *b, uint32_t team_max_items, uint32_t full_max_items);
+/* Runs every added session; out[i] receives the result of the i-th added
+ * session (free each with ts_generated_free).  The batch is then empty and
+ * may take new sessions.  On failure no result is returned and the message
+ * names the session. */
+int ts_batch_run(ts_batch *b, ts_generated **out);
+void ts_batch_stats_get(const ts_batch *b, ts_batch_stats *out);
+
 /* ---- GeneratedImage (lib.rs:378-455) ------------------------------------- */
 
 void ts_generated_dims(const ts_generated *g, uint32_t *width, uint32_t *height);

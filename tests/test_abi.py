@@ -140,3 +140,16 @@ def test_bad_image_arguments(ts):
         assert lib.ts_builder_inpaint_example_channel(h, 7, C.byref(d), 4, 4) == 1
     finally:
         lib.ts_builder_free(h)
+
+
+def test_empty_batch_is_refused(ts):
+    lib = ts.lib()
+    b = lib.ts_batch_new(0)
+    try:
+        out = (C.c_void_p * 1)()
+        assert lib.ts_batch_run(b, out) == 11  # TS_ERR_STATE
+        assert b"empty batch" in lib.ts_batch_last_error(b)
+        assert lib.ts_batch_size(b) == 0
+        assert lib.ts_batch_add(b, None) == 14  # TS_ERR_NULL
+    finally:
+        lib.ts_batch_free(b)

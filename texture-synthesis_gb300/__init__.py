@@ -68,6 +68,8 @@ class _Progress(C.Structure):
                 ("stage_current", C.c_uint64), ("stage_total", C.c_uint64)]
 
 
+BATCH_PHASES = ("level_switch", "random_candidates", "knn_walk", "knn_exhaustive", "mean", "resolve",
+                "resolve_team", "resolve_team_full", "commit")
 KERNEL_KINDS = ("random_candidates", "knn_walk", "knn_exhaustive", "resolve", "commit", "level_switch", "mean")
 
 
@@ -81,6 +83,13 @@ class RunStats(C.Structure):
         d["kernels"] = {name: {"launches": int(self.kernel_count[i]), "ms": float(self.kernel_ms[i])}
                         for i, name in enumerate(KERNEL_KINDS)}
         return d
+
+
+class _BatchStats(C.Structure):
+    _fields_ = [("sessions", C.c_uint64), ("steps", C.c_uint64), ("launches", C.c_uint64),
+                ("output_pixels", C.c_uint64), ("resolves", C.c_uint64), ("cost_evals", C.c_uint64),
+                ("gpu_ms", C.c_double), ("wall_ms", C.c_double), ("plan_ms", C.c_double),
+                ("phase_launches", C.c_uint64 * 9), ("phase_ms", C.c_double * 9)]
 
 
 class _LaunchRecord(C.Structure):
@@ -135,6 +144,17 @@ SIGNATURES = {
     "ts_generated_free": (None, [C.c_void_p]),
     "ts_generated_launch_count": (C.c_uint64, [C.c_void_p]),
     "ts_generated_launches": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ts_batch_new": (C.c_void_p, [C.c_int32]),
+    "ts_batch_free": (None, [C.c_void_p]),
+    "ts_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "ts_batch_add": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ts_batch_size": (C.c_uint64, [C.c_void_p]),
+    "ts_batch_use_graph": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ts_batch_run": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "ts_batch_profile": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ts_batch_plan_threads": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "ts_batch_resolve_team": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
+    "ts_batch_stats_get": (None, [C.c_void_p, C.POINTER(_BatchStats)]),
 }
 
 
@@ -453,6 +473,58 @@ class GeneratedImage:
         lib().ts_generated_launches(self._h, arr)
         return [{"kernel": KERNEL_KINDS[r.kind], "stage": r.stage, "batch_items": r.batch_items, "ms": r.ms}
                 for r in arr[:n]]
+
+
+class Batch:
+    """The batched form: sessions added here run together, one launch per
+    phase of each batch step carrying every session's step.  Each result is
+    identical to Session.run on the same session."""
+
+    def __init__(self, device=0, graph=False, profile=False, plan_threads=0, team=None):
+        self._h = lib().ts_batch_new(device)
+        if not self._h:
+            raise Error(13, "ts_batch_new")
+        if team is not None:
+            lib().ts_batch_resolve_team(self._h, team[0], team[1])
+        if graph:
+            lib().ts_batch_use_graph(self._h, 1)
+        if profile:
+            lib().ts_batch_profile(self._h, 1)
+        if plan_threads:
+            lib().ts_batch_plan_threads(self._h, plan_threads)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.ts_batch_free(self._h)
+            self._h = None
+
+    def __len__(self):
+        return int(lib().ts_batch_size(self._h))
+
+    def _check(self, rc):
+        if rc:
+            msg = lib().ts_batch_last_error(self._h)
+            raise Error(rc, msg.decode() if msg else "")
+
+    def add(self, session):
+        """Hands a built Session to the batch (the session is consumed)."""
+        self._check(lib().ts_batch_add(self._h, session._h))
+        return self
+
+    def run(self):
+        """Runs every added session; a list of GeneratedImage in add order."""
+        n = len(self)
+        out = (C.c_void_p * max(1, n))()
+        self._check(lib().ts_batch_run(self._h, out))
+        return [GeneratedImage(out[i]) for i in range(n)]
+
+    def stats(self):
+        st = _BatchStats()
+        lib().ts_batch_stats_get(self._h, C.byref(st))
+        d = {f: getattr(st, f) for f, _ in st._fields_ if not f.startswith("phase_")}
+        d["phases"] = {name: {"launches": int(st.phase_launches[i]), "ms": float(st.phase_ms[i])}
+                       for i, name in enumerate(BATCH_PHASES)}
+        return d
 
 
 def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0, profile=False, team_max_batch=None,

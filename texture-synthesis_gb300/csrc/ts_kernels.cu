@@ -110,8 +110,8 @@ __device__ __forceinline__ bool coord_valid(const SessionDev &s, const MapDesc &
 // Pcg32::seed_from_u64(stage_seed + item + 1); per candidate a map
 // (usize range), then (x, y) redrawn until valid.
 // ---------------------------------------------------------------------------
-__global__ void k_random_candidates(SessionDev s, StageDev st) {
-  const uint32_t item = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void random_candidates_body(const SessionDev &s, const StageDev &st, uint32_t vb) {
+  const uint32_t item = vb * blockDim.x + threadIdx.x;
   if (item >= st.n_items) return;
   Pcg32 g = pcg_from_u64(st.stage_seed + (uint64_t)item + 1ULL);
   uint2 *out = st.rcand + (size_t)item * s.m;
@@ -160,12 +160,12 @@ __device__ __forceinline__ double neighbour_dist(const SessionDev &s, int px, in
 // offset with d2 <= its radius^2, in (d2, dy, dx) order, so the first k
 // occupied entries are exactly the k nearest points under the tie rule.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kWalkWarps *kWarp, 4) k_knn_walk(SessionDev s, StageDev st, BatchDev b) {
+__device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t vb,
+                                              uint32_t vg) {
   const int lane = threadIdx.x & 31;
   const uint32_t lt = (1u << lane) - 1u;
   const uint32_t nb = b.i1 - b.i0;
-  for (uint32_t local = blockIdx.x * kWalkWarps + (threadIdx.x >> 5); local < nb;
-       local += gridDim.x * kWalkWarps) {
+  for (uint32_t local = vb * kWalkWarps + (threadIdx.x >> 5); local < nb; local += vg * kWalkWarps) {
     const uint32_t pixel = st.items[b.i0 + local];
     const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
     const double x2 = s.xdiv[px + s.xdiv_off], y2 = s.ydiv[py + s.ydiv_off];
@@ -245,12 +245,12 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
 // receives every point's key in one pass over the resolved list; when they
 // fit, a bitonic sort of them gives the answer directly, otherwise a
 // radix select over further passes finds the cut distance first.
-__global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive(SessionDev s, StageDev st, BatchDev b,
-                                                                 int all_items) {
+__device__ __forceinline__ void knn_exhaustive_body(const SessionDev &s, const StageDev &st, const BatchDev &b,
+                                                    int all_items, uint32_t vb, uint32_t vg) {
   __shared__ ExhShared sh;
   extern __shared__ unsigned long long all_keys[];
   const uint32_t n = all_items ? b.i1 - b.i0 : *b.fb_count;
-  for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
+  for (uint32_t e = vb; e < n; e += vg) {
     const uint32_t local = all_items ? e : b.fb_list[e];
     knn_exhaustive_item(s, st, b, local, sh, all_keys, all_items != 0);
     __syncthreads();
@@ -515,9 +515,9 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
 // mean: thread per item (get_distances_to_k_neighs, ms.rs:417-423): the sum
 // of the 4x-duplicated distance list in order, then / (4k).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_mean(SessionDev s, StageDev st, BatchDev b) {
+__device__ __forceinline__ void mean_body(const SessionDev &s, const BatchDev &b, uint32_t vb) {
   const uint32_t nb = b.i1 - b.i0;
-  const uint32_t local = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t local = vb * blockDim.x + threadIdx.x;
   if (local >= nb) return;
   const uint32_t nk = b.ncnt[local];
   if (nk == 0) return;
@@ -840,7 +840,8 @@ __device__ void write_bad_result(const SessionDev &s, const BatchDev &b, uint32_
   b.res[local] = r;
 }
 
-__global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve(SessionDev s, StageDev st, BatchDev b) {
+__device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t vb,
+                                             uint32_t vg) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double tab[64];
   __shared__ float tab_ff[128];
@@ -855,7 +856,7 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve(SessionDev 
   __syncthreads();
   const uint32_t nb = b.i1 - b.i0;
   const int W = (int)s.W, H = (int)s.H;
-  for (uint32_t local = blockIdx.x * kResolveWarps + warp; local < nb; local += gridDim.x * kResolveWarps) {
+  for (uint32_t local = vb * kResolveWarps + warp; local < nb; local += vg * kResolveWarps) {
     const uint32_t item = b.i0 + local;
     const uint32_t pixel = st.items[item];
     const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
@@ -961,7 +962,8 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve(SessionDev 
 // evaluation, which suits batches too small to fill the GPU with warps.
 // ---------------------------------------------------------------------------
 template <int T, bool kFull>
-__global__ void __launch_bounds__(T) k_resolve_team(SessionDev s, StageDev st, BatchDev b) {
+__device__ __forceinline__ void resolve_team_body(const SessionDev &s, const StageDev &st, const BatchDev &b,
+                                                  uint32_t vb, uint32_t vg) {
   constexpr int NW = T / 32;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double tab[64];
@@ -982,7 +984,7 @@ __global__ void __launch_bounds__(T) k_resolve_team(SessionDev s, StageDev st, B
   const uint32_t lt = (1u << lane) - 1u;
   const uint32_t nb = b.i1 - b.i0;
   __syncthreads();
-  for (uint32_t local = blockIdx.x; local < nb; local += gridDim.x) {
+  for (uint32_t local = vb; local < nb; local += vg) {
     const uint32_t item = b.i0 + local;
     const uint32_t pixel = st.items[item];
     const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
@@ -1201,8 +1203,8 @@ __global__ void __launch_bounds__(T) k_resolve_team(SessionDev s, StageDev st, B
 }
 
 // update + flush_resolved for a batch (ms.rs:296-377).
-__global__ void k_commit(SessionDev s, StageDev st, BatchDev b) {
-  const uint32_t local = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void commit_body(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t vb) {
+  const uint32_t local = vb * blockDim.x + threadIdx.x;
   const uint32_t nb = b.i1 - b.i0;
   if (local >= nb) return;
   const Result r = b.res[local];
@@ -1232,8 +1234,8 @@ __global__ void k_commit(SessionDev s, StageDev st, BatchDev b) {
 }
 
 // next_pyramid_level (ms.rs:687-700)
-__global__ void k_level_switch(SessionDev s, uint32_t level, uint32_t n_res) {
-  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void level_switch_body(const SessionDev &s, uint32_t level, uint32_t n_res, uint32_t vb) {
+  const uint32_t e = vb * blockDim.x + threadIdx.x;
   if (e >= n_res) return;
   const uint32_t p = s.resolved[e];
   const uint4 sv = s.state[p];
@@ -1311,6 +1313,134 @@ __global__ void k_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t leve
   }
 }
 
+// ---------------------------------------------------------------------------
+// Kernels.  The plain form takes one session's descriptors as parameters;
+// the multi form runs one phase of one batch step for many sessions, each
+// segment of its grid belonging to one (session, step).
+// ---------------------------------------------------------------------------
+struct SegView {
+  const SessionDev *s;
+  const StepDev *d;
+  uint32_t vb, vg;
+};
+
+// The segment owning this block: segments are sorted by first block, so the
+// ones starting at or before blockIdx.x form a prefix; one ballot per 32.
+__device__ __forceinline__ SegView find_segment(const MultiLaunch &ml) {
+  const uint32_t bx = blockIdx.x;
+  const int lane = threadIdx.x & 31;
+  uint32_t j = 0;
+  for (uint32_t c = 0; c < ml.n_segs; c += kWarp) {
+    const uint32_t i = c + lane;
+    const bool le = i < ml.n_segs && __ldg(&ml.segs[i].block0) <= bx;
+    const uint32_t bal = __ballot_sync(0xffffffffu, le);
+    j = c + __popc(bal) - 1;
+    if (bal != 0xffffffffu) break;
+  }
+  const Segment g = ml.segs[j];
+  SegView v;
+  v.s = ml.sessions + g.session;
+  v.d = ml.steps + g.step;
+  v.vb = bx - g.block0;
+  v.vg = g.nblocks;
+  return v;
+}
+
+__global__ void k_random_candidates(SessionDev s, StageDev st) { random_candidates_body(s, st, blockIdx.x); }
+__global__ void k_random_candidates_multi(MultiLaunch ml) {
+  const SegView v = find_segment(ml);
+  random_candidates_body(*v.s, v.d->rc, v.vb);
+}
+
+__global__ void __launch_bounds__(kWalkWarps *kWarp, 4) k_knn_walk(SessionDev s, StageDev st, BatchDev b) {
+  knn_walk_body(s, st, b, blockIdx.x, gridDim.x);
+}
+__global__ void __launch_bounds__(kWalkWarps *kWarp, 4) k_knn_walk_multi(MultiLaunch ml) {
+  const SegView v = find_segment(ml);
+  knn_walk_body(*v.s, v.d->st, v.d->b, v.vb, v.vg);
+}
+
+__global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive(SessionDev s, StageDev st, BatchDev b,
+                                                                 int all_items) {
+  knn_exhaustive_body(s, st, b, all_items, blockIdx.x, gridDim.x);
+}
+__global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive_multi(MultiLaunch ml) {
+  __shared__ ExhShared sh;
+  extern __shared__ unsigned long long all_keys[];
+  if (blockIdx.x < ml.pool_block0) {  // whole batches of sparse steps
+    const SegView v = find_segment(ml);
+    const StepDev &d = *v.d;
+    const uint32_t n = d.b.i1 - d.b.i0;
+    for (uint32_t e = v.vb; e < n; e += v.vg) {
+      knn_exhaustive_item(*v.s, d.st, d.b, e, sh, all_keys, true);
+      __syncthreads();
+    }
+    return;
+  }
+  // the pool: the fallback lists of all walk steps, concatenated, in turn;
+  // their lengths are read in parallel, kExhThreads at a time
+  __shared__ uint32_t fb_cnt[kExhThreads];
+  const uint32_t vb = blockIdx.x - ml.pool_block0, vg = gridDim.x - ml.pool_block0;
+  uint32_t base = 0;
+  for (uint32_t c0 = 0; c0 < ml.n_fb; c0 += kExhThreads) {
+    const uint32_t nc = min((uint32_t)kExhThreads, ml.n_fb - c0);
+    __syncthreads();
+    if (threadIdx.x < nc) fb_cnt[threadIdx.x] = *ml.steps[ml.fb[c0 + threadIdx.x].step].b.fb_count;
+    __syncthreads();
+    for (uint32_t j = 0; j < nc; ++j) {
+      const uint32_t cnt = fb_cnt[j];
+      uint32_t v = base + (vb + vg - base % vg) % vg;
+      if (v < base + cnt) {
+        const Segment g = ml.fb[c0 + j];
+        const StepDev &d = ml.steps[g.step];
+        for (; v < base + cnt; v += vg) {
+          knn_exhaustive_item(ml.sessions[g.session], d.st, d.b, d.b.fb_list[v - base], sh, all_keys, false);
+          __syncthreads();
+        }
+      }
+      base += cnt;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) k_mean(SessionDev s, StageDev st, BatchDev b) { mean_body(s, b, blockIdx.x); }
+__global__ void __launch_bounds__(128) k_mean_multi(MultiLaunch ml) {
+  const SegView v = find_segment(ml);
+  mean_body(*v.s, v.d->b, v.vb);
+}
+
+__global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve(SessionDev s, StageDev st, BatchDev b) {
+  resolve_body(s, st, b, blockIdx.x, gridDim.x);
+}
+__global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve_multi(MultiLaunch ml) {
+  const SegView v = find_segment(ml);
+  resolve_body(*v.s, v.d->st, v.d->b, v.vb, v.vg);
+}
+
+template <int T, bool kFull>
+__global__ void __launch_bounds__(T) k_resolve_team(SessionDev s, StageDev st, BatchDev b) {
+  resolve_team_body<T, kFull>(s, st, b, blockIdx.x, gridDim.x);
+}
+template <int T, bool kFull>
+__global__ void __launch_bounds__(T) k_resolve_team_multi(MultiLaunch ml) {
+  const SegView v = find_segment(ml);
+  resolve_team_body<T, kFull>(*v.s, v.d->st, v.d->b, v.vb, v.vg);
+}
+
+__global__ void k_commit(SessionDev s, StageDev st, BatchDev b) { commit_body(s, st, b, blockIdx.x); }
+__global__ void k_commit_multi(MultiLaunch ml) {
+  const SegView v = find_segment(ml);
+  commit_body(*v.s, v.d->st, v.d->b, v.vb);
+}
+
+__global__ void k_level_switch(SessionDev s, uint32_t level, uint32_t n_res) {
+  level_switch_body(s, level, n_res, blockIdx.x);
+}
+__global__ void k_level_switch_multi(MultiLaunch ml) {
+  const SegView v = find_segment(ml);
+  level_switch_body(*v.s, v.d->level, v.d->ls_n_res, v.vb);
+}
+
 inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
 }  // namespace
@@ -1343,6 +1473,83 @@ cudaError_t configure_kernels(uint32_t k, uint32_t m) {
     return cudaFuncSetAttribute(k_resolve_team<kTeamThreads, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)fsm);
   return cudaSuccess;
+}
+
+cudaError_t set_multi_smem(int phase, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  const int v = (int)bytes;
+  const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  switch (phase) {
+    case kPhaseExhaustive: return cudaFuncSetAttribute(k_knn_exhaustive_multi, a, v);
+    case kPhaseResolve: return cudaFuncSetAttribute(k_resolve_multi, a, v);
+    case kPhaseTeamPart: return cudaFuncSetAttribute(k_resolve_team_multi<kTeamThreads, false>, a, v);
+    case kPhaseTeamFull: return cudaFuncSetAttribute(k_resolve_team_multi<kTeamThreads, true>, a, v);
+    default: return cudaSuccess;
+  }
+}
+
+bool team_full_fits(uint32_t k, uint32_t m) { return team_full_smem_bytes(k, m) <= kTeamFullMaxSmem; }
+
+uint32_t multi_threads(int phase) {
+  switch (phase) {
+    case kPhaseLevelSwitch: return 256;
+    case kPhaseRandom: return 128;
+    case kPhaseWalk: return kWalkWarps * kWarp;
+    case kPhaseExhaustive: return kExhThreads;
+    case kPhaseMean: return 128;
+    case kPhaseResolve: return kResolveWarps * kWarp;
+    case kPhaseTeamPart:
+    case kPhaseTeamFull: return kTeamThreads;
+    default: return 256;
+  }
+}
+
+uint32_t multi_blocks(int phase, uint32_t n, uint32_t cap) {
+  if (n == 0) return 0;
+  uint32_t b = 0;
+  switch (phase) {
+    case kPhaseLevelSwitch: b = cdiv(n, 256); break;
+    case kPhaseRandom: b = cdiv(n, 128); break;
+    case kPhaseWalk: b = cdiv(n, kWalkWarps); break;
+    case kPhaseExhaustive: b = n; break;
+    case kPhaseMean: b = cdiv(n, 128); break;
+    case kPhaseResolve: b = cdiv(n, kResolveWarps); break;
+    case kPhaseTeamPart:
+    case kPhaseTeamFull: b = n; break;
+    default: b = cdiv(n, 256); break;
+  }
+  // only the grid-stride phases may take fewer blocks than items need
+  const bool strided = phase == kPhaseWalk || phase == kPhaseExhaustive || phase == kPhaseResolve ||
+                       phase == kPhaseTeamPart || phase == kPhaseTeamFull;
+  if (strided && cap && b > cap) b = cap;
+  return b;
+}
+
+size_t multi_smem_bytes(int phase, uint32_t k, uint32_t m) {
+  switch (phase) {
+    case kPhaseExhaustive: return (size_t)kExhAllKeys * 8;
+    case kPhaseResolve: return resolve_smem_bytes(k, m, 0);
+    case kPhaseTeamPart: return team_smem_bytes(k, m);
+    case kPhaseTeamFull: return team_full_smem_bytes(k, m);
+    default: return 0;
+  }
+}
+
+void launch_multi(int phase, const MultiLaunch &ml, uint32_t blocks, size_t smem, cudaStream_t stream) {
+  if (blocks == 0) return;  // a launch may carry only the exhaustive k-NN's fallback pool (no segments)
+  const uint32_t t = multi_threads(phase);
+  switch (phase) {
+    case kPhaseLevelSwitch: k_level_switch_multi<<<blocks, t, 0, stream>>>(ml); break;
+    case kPhaseRandom: k_random_candidates_multi<<<blocks, t, 0, stream>>>(ml); break;
+    case kPhaseWalk: k_knn_walk_multi<<<blocks, t, 0, stream>>>(ml); break;
+    case kPhaseExhaustive: k_knn_exhaustive_multi<<<blocks, t, smem, stream>>>(ml); break;
+    case kPhaseMean: k_mean_multi<<<blocks, t, 0, stream>>>(ml); break;
+    case kPhaseResolve: k_resolve_multi<<<blocks, t, smem, stream>>>(ml); break;
+    case kPhaseTeamPart: k_resolve_team_multi<kTeamThreads, false><<<blocks, t, smem, stream>>>(ml); break;
+    case kPhaseTeamFull: k_resolve_team_multi<kTeamThreads, true><<<blocks, t, smem, stream>>>(ml); break;
+    case kPhaseCommit: k_commit_multi<<<blocks, t, 0, stream>>>(ml); break;
+    default: break;
+  }
 }
 
 void launch_random_candidates(const SessionDev &s, const StageDev &st, cudaStream_t stream) {

@@ -114,6 +114,63 @@ struct BatchDev {
   Result *res;           // [batch]
 };
 
+// One batch step of one session as the multi-session kernels read it.
+struct StepDev {
+  StageDev st;         // stage view of the step's random-candidate chunk
+  StageDev rc;         // the same chunk as random_candidates sees it (its own seed)
+  BatchDev b;
+  uint32_t level;      // level switch: new level and resolved-list length
+  uint32_t ls_n_res;
+  int all_items;       // exhaustive k-NN over every item of the batch
+  int pad;
+};
+
+// A run of `nblocks` blocks, from block0 on, working on one (session, step).
+struct Segment {
+  uint32_t block0, nblocks, session, step;
+};
+
+// Parameters of one multi-session launch: segments sorted by block0.  The
+// exhaustive k-NN also drains the walk's fallback lists of the steps in
+// `fb` with the blocks from pool_block0 on (whose count is known only on
+// the device).
+struct MultiLaunch {
+  const Segment *segs;
+  uint32_t n_segs;
+  const SessionDev *sessions;
+  const StepDev *steps;
+  const Segment *fb;
+  uint32_t n_fb;
+  uint32_t pool_block0;
+};
+
+// Phases of a batch step, in launch order.
+enum : int {
+  kPhaseLevelSwitch = 0,
+  kPhaseRandom,
+  kPhaseWalk,
+  kPhaseExhaustive,
+  kPhaseMean,
+  kPhaseResolve,
+  kPhaseTeamPart,
+  kPhaseTeamFull,
+  kPhaseCommit,
+  kPhases
+};
+
+// Threads per block, blocks for a segment of n units (items, or resolved
+// points for the level switch; `cap` bounds the grid-stride phases, 0 = no
+// bound) and dynamic shared memory of each phase's multi-session kernel.
+uint32_t multi_threads(int phase);
+uint32_t multi_blocks(int phase, uint32_t n, uint32_t cap);
+size_t multi_smem_bytes(int phase, uint32_t k, uint32_t m);
+void launch_multi(int phase, const MultiLaunch &ml, uint32_t blocks, size_t smem, cudaStream_t stream);
+// Lets a phase's multi-session kernel use `bytes` of dynamic shared memory
+// (current device).
+cudaError_t set_multi_smem(int phase, size_t bytes);
+// Whether the full-evaluation team form has room for (k, m).
+bool team_full_fits(uint32_t k, uint32_t m);
+
 // Launchers (stream-ordered, no synchronisation).
 void launch_random_candidates(const SessionDev &s, const StageDev &st, cudaStream_t stream);
 void launch_knn_walk(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);

@@ -17,9 +17,11 @@
 #include <cmath>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -101,6 +103,20 @@ struct DevBuf {
   DevBuf() = default;
   DevBuf(const DevBuf &) = delete;
   DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  DevBuf &operator=(DevBuf &&o) noexcept {
+    if (this != &o) {
+      reset();
+      p = o.p;
+      n = o.n;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
   ~DevBuf() { reset(); }
   void reset() {
     if (p) cudaFree(p);
@@ -827,6 +843,537 @@ struct LaunchTimer {
 
 }  // namespace
 
+namespace {
+
+// One batch step of a session's run, with the launches it needs; the plain
+// path issues them one session at a time, the batched path one phase of many
+// sessions' steps per launch.
+struct Step {
+  int stage = 0;                 // index into the stage plan
+  bool stage_end = false;        // last step of its stage (progress point)
+  bool ls = false;               // level switch before the step
+  uint32_t ls_level = 0, ls_n_res = 0;
+  bool rc = false;               // random candidates of a new chunk
+  StageDev rc_st{};
+  bool batch = false;
+  StageDev st{};
+  BatchDev bd{};
+  bool exhaustive = false;       // exhaustive k-NN over the whole batch
+  int resolve = kPhaseResolve;   // kPhaseResolve, kPhaseTeamPart or kPhaseTeamFull
+  uint32_t n = 0;                // items of the batch
+};
+
+// Everything one run holds between planning and reading back.
+struct RunCtx {
+  ts_session *s = nullptr;
+  uint32_t W = 0, H = 0, k = 0, m = 0;
+  size_t N = 0;
+  size_t locked = 0;
+  std::vector<StagePlan> plan;
+  std::vector<Step> steps;
+  // host data uploaded at the start of the run
+  std::vector<uint32_t> color, resolved, items, occ, mir;
+  std::vector<uint4> state;
+  std::vector<float> luts;
+  std::vector<int32_t> tab;
+  std::vector<double> xdiv, ydiv, dxt, dy2t;
+  size_t n_batches = 0;
+  uint64_t overall_total = 0;
+  // device state
+  DevBuf<uint32_t> d_color, d_occ, d_mir, d_res, d_items, d_ncnt, d_fbl, d_fbc;
+  DevBuf<uint4> d_state;
+  DevBuf<float> d_rscore, d_lut;
+  DevBuf<double> d_xdiv, d_ydiv, d_dist, d_dxt, d_dy2t, d_mean;
+  DevBuf<int32_t> d_tab, d_nbuf;
+  DevBuf<uint2> d_rcand;
+  DevBuf<Result> d_result;
+  DevBuf<int> d_err;
+  DevBuf<unsigned long long> d_evals;
+  SessionDev sd{};
+  // read back
+  std::vector<uint32_t> col;
+  std::vector<uint4> stv;
+  int derr = 0;
+  unsigned long long evals = 0;
+  std::unique_ptr<ts_generated> g;
+  uint64_t launches = 0, batches = 0, resolves = 0;
+};
+
+// Host schedule of Generator::resolve (ms.rs:702-1051) and the device
+// buffers of the run; nothing is enqueued yet.
+void run_plan(ts_session *s, RunCtx &c) {
+  const Params &p = s->prm;
+  c.s = s;
+  const uint32_t W = c.W = s->W, H = c.H = s->H;
+  const size_t N = c.N = (size_t)W * H;
+  const uint32_t k = c.k = p.k, m = c.m = (uint32_t)p.m;
+  const uint32_t stages = p.backtrack_stages;
+  c.g.reset(new (std::nothrow) ts_generated());
+  if (!c.g) throw Failure{TS_ERR_OUT_OF_MEMORY, "out of host memory"};
+  // ---- initial state (Generator::new / new_from_inpaint) ----
+  std::vector<uint32_t> &color = c.color;
+  std::vector<uint4> &state = c.state;
+  std::vector<uint32_t> &resolved = c.resolved;
+  color.assign(N, 0);
+  state.assign(N, make_uint4(0, 0, 0, 0));
+  std::vector<uint32_t> unresolved;
+  size_t locked = 0;
+  if (s->inpaint) {
+    for (size_t i = 0; i < N; ++i) {
+      const uint8_t *cc = &s->inpaint_colors.px[4 * i];
+      color[i] = (uint32_t)cc[0] | ((uint32_t)cc[1] << 8) | ((uint32_t)cc[2] << 16) | ((uint32_t)cc[3] << 24);
+      if (s->inpaint_mask[i]) {
+        unresolved.push_back((uint32_t)i);
+      } else {
+        resolved.push_back((uint32_t)i);
+        state[i] = make_uint4((uint32_t)(i % W) | ((uint32_t)(i / W) << 16), 0, 0, s->inpaint_index);
+      }
+    }
+    locked = resolved.size();
+  } else {
+    unresolved.resize(N);
+    for (size_t i = 0; i < N; ++i) unresolved[i] = (uint32_t)i;
+  }
+  auto pick = [&](uint64_t seed) -> uint32_t {
+    Pcg32 r = pcg_from_u64(seed);
+    const uint64_t idx = gen_range_u64(r, unresolved.size());
+    const uint32_t v = unresolved[idx];
+    unresolved[idx] = unresolved.back();
+    unresolved.pop_back();
+    return v;
+  };
+  // ---- random init (session.rs:42-52, ms.rs:427-475): all examples ----
+  if (p.has_random_init) {
+    if (p.random_init > unresolved.size())
+      throw Failure{TS_ERR_INVALID_RANGE, "random_init exceeds the number of pixels to synthesise"};
+    for (uint64_t i = 0; i < p.random_init; ++i) {
+      const uint32_t px = pick(p.seed + i);
+      const uint64_t sd = p.seed + i + (uint64_t)px;
+      Pcg32 r = pcg_from_u64(sd);
+      const uint32_t map = (uint32_t)gen_range_u64(r, s->n_ex);
+      const Image &im = s->bottoms[map];
+      r = pcg_from_u64(sd);
+      const uint32_t x = gen_range_u32(r, im.w);
+      r = pcg_from_u64(sd);
+      const uint32_t y = gen_range_u32(r, im.h);
+      if (x > 0xffffu || y > 0xffffu) throw Failure{TS_ERR_LIMIT, "example side exceeds limit"};
+      state[px] = make_uint4(x | (y << 16), px, map, map);
+      const uint8_t *cc = &im.px[((size_t)y * im.w + x) * 4];
+      color[px] = (uint32_t)cc[0] | ((uint32_t)cc[1] << 8) | ((uint32_t)cc[2] << 16) | ((uint32_t)cc[3] << 24);
+      resolved.push_back(px);
+    }
+    locked += p.random_init;
+  }
+  c.locked = locked;
+  const size_t total = unresolved.size();
+  // ---- the schedule of Generator::resolve ----
+  const int32_t x_l = (int32_t)((float)W * kTilingBoundary), y_b = (int32_t)((float)H * kTilingBoundary);
+  const float sig2 = p.cauchy * p.cauchy;
+  float cauchy[256], l2[256];
+  for (int d = 0; d < 256; ++d) {
+    const float x = ((float)d - 0.0f) / 255.0f;
+    const float x2 = x * x;
+    cauchy[d] = log1pf(x2 / sig2);
+    l2[d] = x2;
+  }
+  std::vector<StagePlan> &plan = c.plan;
+  std::vector<uint32_t> &items = c.items;
+  std::vector<float> &luts = c.luts;
+  size_t n_res = resolved.size();
+  int32_t pyramid_level = 0;
+  uint32_t max_batch_items = 1, max_stage_items = 1;
+  c.tab = knn_table(kKnnTabRadius);
+  const std::vector<int32_t> &tab = c.tab;
+  for (int32_t ps = (int32_t)stages; ps >= 0; --ps) {
+    StagePlan sp;
+    sp.p_stage = ps;
+    sp.level = (uint32_t)pyramid_level;
+    sp.level_switch = pyramid_level > 0;
+    pyramid_level += 1;
+    if (pyramid_level > (int32_t)stages - 1) pyramid_level = (int32_t)stages - 1;
+    sp.seed = pcg_stage_seed(p.seed + (uint64_t)ps);
+    const float fp = powf(p.backtrack_percent, (float)ps) * (float)total;
+    size_t P = fp >= 0.0f ? (size_t)fp : 0;  // `as usize` saturates NaN and negatives to 0
+    const size_t redo = n_res - locked;
+    float adaptive = 0.0f;
+    if (s->guided && ps > 0) {
+      const float a = p.alpha * (1.0f - ((float)n_res / (float)total));
+      adaptive = (a * a) * a;
+    }
+    // stage LUTs (ms.rs:853-858): content = (1 - a) * cauchy when guided
+    bool slow = false;
+    for (int d = 0; d < 256; ++d) {
+      const float cv = s->guided ? (1.0f - adaptive) * cauchy[d] : cauchy[d];
+      luts.push_back(cv);
+      slow |= !std::isfinite(cv);
+    }
+    for (int d = 0; d < 256; ++d) {
+      const float gv = s->guided ? adaptive * l2[d] : 0.0f;
+      luts.push_back(gv);
+      slow |= !std::isfinite(gv);
+    }
+    sp.slow_lut = slow;
+    const size_t P_eff = std::min(P, redo + unresolved.size());
+    sp.items_off = (uint32_t)items.size();
+    sp.n_items = (uint32_t)P_eff;
+    sp.redo = (uint32_t)redo;
+    sp.n_res_start = (uint32_t)n_res;
+    for (size_t i = 0; i < P_eff; ++i) {
+      if (i < redo)
+        items.push_back(resolved[i + locked]);
+      else
+        items.push_back(pick(sp.seed + (uint64_t)i));
+    }
+    size_t i = 0, R = n_res;
+    while (i < P_eff) {
+      size_t bsz = 1;
+      if (p.batch_divisor) {
+        bsz = R / p.batch_divisor;
+        if (bsz < 1) bsz = 1;
+        if (p.max_batch && bsz > p.max_batch) bsz = p.max_batch;
+      }
+      if (bsz > P_eff - i) bsz = P_eff - i;
+      BatchPlan bp;
+      bp.i0 = (uint32_t)i;
+      bp.i1 = (uint32_t)(i + bsz);
+      bp.n_res = (uint32_t)R;
+      bp.append_from = k == 0 ? bp.i0 : std::max<uint32_t>(bp.i0, (uint32_t)std::min(redo, (size_t)bp.i1));
+      // exhaustive k-NN when the table walk is unlikely to find k points
+      bp.exhaustive = k > 0 && (R <= 4096 && (double)R * tab.size() < 2.0 * k * (double)N);
+      const size_t appended = bp.i1 - bp.append_from;
+      for (size_t t = bp.append_from; t < bp.i1; ++t) resolved.push_back(items[sp.items_off + t]);
+      R += appended;
+      sp.batches.push_back(bp);
+      max_batch_items = std::max<uint32_t>(max_batch_items, (uint32_t)bsz);
+      i += bsz;
+    }
+    n_res = R;
+    max_stage_items = std::max<uint32_t>(max_stage_items, (uint32_t)P_eff);
+    plan.push_back(std::move(sp));
+  }
+  // ---- device state ----
+  const uint32_t wpr = (W + 31) / 32;
+  for (auto &sp : plan) c.n_batches += sp.batches.size();
+  CUDA_TRY(c.d_color.alloc(N));
+  CUDA_TRY(c.d_state.alloc(N));
+  CUDA_TRY(c.d_occ.alloc((size_t)wpr * H));
+  CUDA_TRY(c.d_mir.alloc((size_t)wpr * H));
+  CUDA_TRY(c.d_res.alloc(resolved.size()));
+  CUDA_TRY(c.d_rscore.alloc(resolved.size()));
+  CUDA_TRY(c.d_items.alloc(items.size()));
+  CUDA_TRY(c.d_lut.alloc(luts.size()));
+  CUDA_TRY(c.d_tab.alloc(tab.size()));
+  CUDA_TRY(c.d_nbuf.alloc((size_t)max_batch_items * std::max<uint32_t>(k, 1)));
+  CUDA_TRY(c.d_ncnt.alloc(max_batch_items));
+  CUDA_TRY(c.d_dist.alloc((size_t)max_batch_items * std::max<uint32_t>(k, 1)));
+  CUDA_TRY(c.d_mean.alloc(max_batch_items));
+  CUDA_TRY(c.d_fbl.alloc(max_batch_items));
+  CUDA_TRY(c.d_fbc.alloc(c.n_batches));
+  CUDA_TRY(c.d_result.alloc(max_batch_items));
+  CUDA_TRY(c.d_err.alloc(1));
+  CUDA_TRY(c.d_evals.alloc(1));
+  const uint64_t rc_items = std::max<uint64_t>(1, std::min<uint64_t>(max_stage_items, kRcandBudget / std::max(m, 1u)));
+  CUDA_TRY(c.d_rcand.alloc((size_t)std::max<uint64_t>(rc_items, max_batch_items) * m));
+  const int32_t xo = x_l + 2, yo = y_b + 2;
+  c.xdiv.resize(W + 2 * (size_t)xo + 1);
+  c.ydiv.resize(H + 2 * (size_t)yo + 1);
+  for (size_t i = 0; i < c.xdiv.size(); ++i) c.xdiv[i] = (double)((int64_t)i - xo) / (double)W;
+  for (size_t i = 0; i < c.ydiv.size(); ++i) c.ydiv[i] = (double)((int64_t)i - yo) / (double)H;
+  CUDA_TRY(c.d_xdiv.alloc(c.xdiv.size()));
+  CUDA_TRY(c.d_ydiv.alloc(c.ydiv.size()));
+  // per-pixel tables of the normalised offsets the weights use: dx and
+  // dy * dy for |offset| <= kDistTabRadius, the same IEEE operations as
+  // get_distances_to_k_neighs (ms.rs:410-415)
+  const int32_t R = kDistTabRadius;
+  c.dxt.resize((size_t)W * (2 * R + 1));
+  c.dy2t.resize((size_t)H * (2 * R + 1));
+  for (uint32_t x = 0; x < W; ++x)
+    for (int32_t o = -R; o <= R; ++o)
+      c.dxt[(size_t)x * (2 * R + 1) + o + R] = (double)((int64_t)x + o) / (double)W - (double)x / (double)W;
+  for (uint32_t y = 0; y < H; ++y)
+    for (int32_t o = -R; o <= R; ++o) {
+      const double dy = (double)((int64_t)y + o) / (double)H - (double)y / (double)H;
+      c.dy2t[(size_t)y * (2 * R + 1) + o + R] = dy * dy;
+    }
+  CUDA_TRY(c.d_dxt.alloc(c.dxt.size()));
+  CUDA_TRY(c.d_dy2t.alloc(c.dy2t.size()));
+  // the tree is rebuilt from the resolved list, mirrors included (ms.rs:747-779)
+  c.occ.assign((size_t)wpr * H, 0);
+  c.mir.assign((size_t)wpr * H, 0);
+  for (size_t i = 0; i < locked; ++i) {
+    const uint32_t q = resolved[i];
+    c.occ[(size_t)(q / W) * wpr + (q % W) / 32] |= 1u << ((q % W) & 31);
+    if (p.tiling) c.mir[(size_t)(q / W) * wpr + (q % W) / 32] |= 1u << ((q % W) & 31);
+  }
+
+  SessionDev &sd = c.sd;
+  sd = SessionDev{};
+  sd.levels = s->levels.p;
+  sd.plevels = s->plevels.p;
+  sd.pguides = s->pguides.p;
+  sd.guide_dims_differ = s->guide_dims_differ ? 1 : 0;
+  sd.masks = s->masks.p;
+  sd.maps = s->d_maps.p;
+  sd.n_maps = s->n_maps;
+  sd.n_levels = s->n_levels;
+  sd.guides = s->guides.p;
+  sd.gdesc = s->d_gdesc.p;
+  sd.n_guides = s->guided ? s->n_ex : 0;
+  sd.guided = s->guided ? 1 : 0;
+  sd.tguide = s->tguide.p;
+  sd.xdiv = c.d_xdiv.p;
+  sd.ydiv = c.d_ydiv.p;
+  sd.xdiv_off = xo;
+  sd.ydiv_off = yo;
+  sd.dxt = c.d_dxt.p;
+  sd.dy2t = c.d_dy2t.p;
+  sd.dtab_r = R;
+  sd.color = c.d_color.p;
+  sd.state = c.d_state.p;
+  sd.occ = c.d_occ.p;
+  sd.mir = c.d_mir.p;
+  sd.resolved = c.d_res.p;
+  sd.rscore = c.d_rscore.p;
+  sd.knn_tab = c.d_tab.p;
+  sd.knn_tab_n = (uint32_t)tab.size();
+  sd.err = c.d_err.p;
+  sd.evals = c.d_evals.p;
+  sd.W = W;
+  sd.H = H;
+  sd.wpr = wpr;
+  sd.tiling = p.tiling ? 1 : 0;
+  sd.x_l = x_l;
+  sd.x_r = (int32_t)W - x_l;
+  sd.y_b = y_b;
+  sd.y_t = (int32_t)H - y_b;
+  sd.k = k;
+  sd.m = m;
+
+  // ---- the steps ----
+  size_t fb_index = 0;
+  for (size_t si = 0; si < plan.size(); ++si) {
+    const StagePlan &sp = plan[si];
+    c.overall_total += sp.n_items;
+    const size_t first = c.steps.size();
+    Step pending;
+    pending.stage = (int)si;
+    if (sp.level_switch) {
+      pending.ls = true;
+      pending.ls_level = sp.level;
+      pending.ls_n_res = sp.n_res_start;
+    }
+    StageDev sdv{};
+    sdv.level = sp.level;
+    sdv.slow_lut = sp.slow_lut ? 1 : 0;
+    sdv.lut = c.d_lut.p + si * 512;
+    sdv.stage_seed = sp.seed;
+    sdv.items = c.d_items.p + sp.items_off;
+    sdv.redo = sp.redo;
+    // random candidates in chunks of whole batches that fit the buffer
+    size_t bi = 0;
+    while (bi < sp.batches.size()) {
+      size_t bj = bi;
+      const uint32_t c0 = sp.batches[bi].i0;
+      while (bj < sp.batches.size() && (bj == bi || sp.batches[bj].i1 - c0 <= rc_items)) ++bj;
+      const uint32_t c1 = sp.batches[bj - 1].i1;
+      StageDev chunk = sdv;
+      chunk.items = sdv.items + c0;
+      chunk.n_items = c1 - c0;
+      chunk.stage_seed = sp.seed + c0;  // item i's stream is seeded with stage_seed + i + 1
+      chunk.rcand = c.d_rcand.p;
+      chunk.redo = sp.redo > c0 ? sp.redo - c0 : 0;
+      pending.rc = true;
+      pending.rc_st = chunk;
+      chunk.stage_seed = sp.seed;  // resolve_at_random uses the stage seed itself
+      for (size_t bk = bi; bk < bj; ++bk) {
+        const BatchPlan &bp = sp.batches[bk];
+        Step stp = pending;
+        pending = Step{};
+        pending.stage = (int)si;
+        stp.batch = true;
+        stp.st = chunk;
+        BatchDev &bd = stp.bd;
+        bd.i0 = bp.i0 - c0;
+        bd.i1 = bp.i1 - c0;
+        bd.n_res = bp.n_res;
+        bd.append_from = bp.append_from - c0;
+        bd.nbuf = c.d_nbuf.p;
+        bd.ncnt = c.d_ncnt.p;
+        bd.fb_list = c.d_fbl.p;
+        bd.fb_count = c.d_fbc.p + fb_index++;
+        bd.dist = c.d_dist.p;
+        bd.mean = c.d_mean.p;
+        bd.res = c.d_result.p;
+        stp.n = bp.i1 - bp.i0;
+        stp.exhaustive = bp.exhaustive;
+        if (stp.n <= p.team_max_batch)
+          stp.resolve = (stp.n <= p.team_full_max_batch && team_full_fits(k, m)) ? kPhaseTeamFull : kPhaseTeamPart;
+        else
+          stp.resolve = kPhaseResolve;
+        c.steps.push_back(stp);
+      }
+      bi = bj;
+    }
+    if (c.steps.size() == first) c.steps.push_back(pending);  // a stage without batches
+    c.steps.back().stage_end = true;
+  }
+}
+
+// Uploads of the initial state, enqueued on st.
+void run_upload(RunCtx &c, cudaStream_t st) {
+  CUDA_TRY(cudaMemcpyAsync(c.d_color.p, c.color.data(), c.N * 4, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(c.d_state.p, c.state.data(), c.N * sizeof(uint4), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(c.d_occ.p, c.occ.data(), c.occ.size() * 4, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(c.d_mir.p, c.mir.data(), c.mir.size() * 4, cudaMemcpyHostToDevice, st));
+  if (c.locked) CUDA_TRY(cudaMemcpyAsync(c.d_res.p, c.resolved.data(), c.locked * 4, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemsetAsync(c.d_rscore.p, 0, c.resolved.size() * 4, st));
+  if (!c.items.empty())
+    CUDA_TRY(cudaMemcpyAsync(c.d_items.p, c.items.data(), c.items.size() * 4, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(c.d_lut.p, c.luts.data(), c.luts.size() * 4, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(c.d_tab.p, c.tab.data(), c.tab.size() * 4, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(c.d_xdiv.p, c.xdiv.data(), c.xdiv.size() * 8, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(c.d_ydiv.p, c.ydiv.data(), c.ydiv.size() * 8, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(c.d_dxt.p, c.dxt.data(), c.dxt.size() * 8, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(c.d_dy2t.p, c.dy2t.data(), c.dy2t.size() * 8, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemsetAsync(c.d_fbc.p, 0, c.n_batches * 4, st));
+  CUDA_TRY(cudaMemsetAsync(c.d_err.p, 0, sizeof(int), st));
+  CUDA_TRY(cudaMemsetAsync(c.d_evals.p, 0, sizeof(unsigned long long), st));
+}
+
+// The plain path: one session's launches, step by step.
+void run_enqueue_plain(RunCtx &c, cudaStream_t st, LaunchTimer &lt, ts_progress_fn progress, void *user) {
+  const SessionDev &sd = c.sd;
+  const uint32_t k = c.k;
+  uint64_t overall_current = 0;
+  std::vector<uint8_t> prog_img;
+  for (const Step &stp : c.steps) {
+    const StagePlan &sp = c.plan[stp.stage];
+    lt.stage = sp.p_stage;
+    lt.items = sp.n_items;
+    if (stp.ls) {
+      lt.run(TS_KERNEL_LEVEL_SWITCH, [&] { launch_level_switch(sd, stp.ls_level, stp.ls_n_res, st); });
+      ++c.launches;
+    }
+    if (stp.rc) {
+      lt.run(TS_KERNEL_RANDOM_CANDIDATES, [&] { launch_random_candidates(sd, stp.rc_st, st); });
+      ++c.launches;
+    }
+    if (stp.batch) {
+      lt.items = stp.n;
+      if (k > 0) {
+        if (stp.exhaustive) {
+          lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, stp.st, stp.bd, true, st); });
+          ++c.launches;
+        } else {
+          lt.run(TS_KERNEL_KNN_WALK, [&] { launch_knn_walk(sd, stp.st, stp.bd, st); });
+          lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, stp.st, stp.bd, false, st); });
+          c.launches += 2;
+        }
+      }
+      if (k > 0 && !stp.exhaustive) {  // the exhaustive k-NN over a whole batch computes the mean itself
+        lt.run(TS_KERNEL_MEAN, [&] { launch_mean(sd, stp.st, stp.bd, st); });
+        ++c.launches;
+      }
+      if (stp.resolve == kPhaseResolve)
+        lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve(sd, stp.st, stp.bd, st); });
+      else
+        lt.run(TS_KERNEL_RESOLVE,
+               [&] { launch_resolve_team(sd, stp.st, stp.bd, stp.resolve == kPhaseTeamFull, st); });
+      lt.run(TS_KERNEL_COMMIT, [&] { launch_commit(sd, stp.st, stp.bd, st); });
+      c.launches += 2;
+      ++c.batches;
+      c.resolves += stp.n;
+    }
+    if (stp.stage_end) {
+      CUDA_TRY(cudaGetLastError());
+      overall_current += sp.n_items;
+      if (progress) {
+        prog_img.resize(c.N * 4);
+        CUDA_TRY(cudaMemcpyAsync(prog_img.data(), c.d_color.p, c.N * 4, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        ts_progress up;
+        up.image = prog_img.data();
+        up.width = c.W;
+        up.height = c.H;
+        up.total_current = overall_current;
+        up.total_total = c.overall_total;
+        up.stage_current = sp.n_items;
+        up.stage_total = sp.n_items;
+        progress(&up, user);
+      }
+    }
+  }
+}
+
+// Device-to-host copies of the results, enqueued on st.
+void run_readback(RunCtx &c, cudaStream_t st) {
+  ts_generated *g = c.g.get();
+  c.col.resize(c.N);
+  c.stv.resize(c.N);
+  g->resolved.resize(c.resolved.size());
+  g->scores.resize(c.resolved.size());
+  CUDA_TRY(cudaMemcpyAsync(&c.evals, c.d_evals.p, sizeof(c.evals), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(c.col.data(), c.d_color.p, c.N * 4, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(c.stv.data(), c.d_state.p, c.N * sizeof(uint4), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(g->resolved.data(), c.d_res.p, c.resolved.size() * 4, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(g->scores.data(), c.d_rscore.p, c.resolved.size() * 4, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(&c.derr, c.d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+}
+
+// After the stream has drained: device errors and the host-side result.
+void run_finish(RunCtx &c) {
+  if (c.derr == kDevErrIndex) throw Failure{TS_ERR_INDEX, "a map id points past the non-ignored examples"};
+  if (c.derr == kDevErrNoSample) throw Failure{TS_ERR_NO_VALID_SAMPLE, "no valid sample location found"};
+  if (c.derr == kDevErrLimit) throw Failure{TS_ERR_LIMIT, "too many equidistant neighbours for the k-NN buffer"};
+  if (c.derr) throw Failure{TS_ERR_CUDA, "device reported error " + std::to_string(c.derr)};
+  ts_generated *g = c.g.get();
+  const size_t N = c.N;
+  g->W = c.W;
+  g->H = c.H;
+  g->image.resize(N * 4);
+  memcpy(g->image.data(), c.col.data(), N * 4);
+  g->coord.resize(N * 3);
+  g->ids.resize(N * 2);
+  for (size_t i = 0; i < N; ++i) {
+    g->coord[3 * i] = c.stv[i].x & 0xffffu;
+    g->coord[3 * i + 1] = c.stv[i].x >> 16;
+    g->coord[3 * i + 2] = c.stv[i].w;
+    g->ids[2 * i] = c.stv[i].y;
+    g->ids[2 * i + 1] = c.stv[i].z;
+  }
+  g->stats.resolves = c.resolves;
+  g->stats.batches = c.batches;
+  g->stats.stages = c.plan.size();
+  g->stats.kernel_launches = c.launches;
+  g->stats.cost_evals = c.evals;
+}
+
+struct StreamGuard {
+  cudaStream_t s = nullptr;
+  ~StreamGuard() {
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  ~EventPair() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+  void create() {
+    CUDA_TRY(cudaEventCreate(&a));
+    CUDA_TRY(cudaEventCreate(&b));
+  }
+  float ms() const {
+    float v = 0.0f;
+    CUDA_TRY(cudaEventElapsedTime(&v, a, b));
+    return v;
+  }
+};
+
+}  // namespace
+
 extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user, ts_generated **out) {
   if (!s || !out) return TS_ERR_NULL;
   *out = nullptr;
@@ -836,440 +1383,33 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
   }
   s->consumed = true;
   const auto t_wall0 = std::chrono::steady_clock::now();
-  const Params &p = s->prm;
-  const uint32_t W = s->W, H = s->H;
-  const size_t N = (size_t)W * H;
-  const uint32_t k = p.k, m = (uint32_t)p.m;
-  const uint32_t stages = p.backtrack_stages;
-  std::unique_ptr<ts_generated> g(new (std::nothrow) ts_generated());
-  if (!g) return TS_ERR_OUT_OF_MEMORY;
+  RunCtx c;
   try {
-    CUDA_TRY(cudaSetDevice(p.device));
-    cudaStream_t st;
-    CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    struct StreamGuard {
-      cudaStream_t s;
-      ~StreamGuard() { cudaStreamDestroy(s); }
-    } sg{st};
-    // ---- initial state (Generator::new / new_from_inpaint) ----
-    std::vector<uint32_t> color(N, 0);
-    std::vector<uint4> state(N, make_uint4(0, 0, 0, 0));
-    std::vector<uint32_t> resolved;
-    std::vector<float> rscore;
-    std::vector<uint32_t> unresolved;
-    std::vector<uint8_t> mirf;  // per resolved entry: insert with mirrors
-    size_t locked = 0;
-    if (s->inpaint) {
-      for (size_t i = 0; i < N; ++i) {
-        const uint8_t *c = &s->inpaint_colors.px[4 * i];
-        color[i] = (uint32_t)c[0] | ((uint32_t)c[1] << 8) | ((uint32_t)c[2] << 16) | ((uint32_t)c[3] << 24);
-        if (s->inpaint_mask[i]) {
-          unresolved.push_back((uint32_t)i);
-        } else {
-          resolved.push_back((uint32_t)i);
-          rscore.push_back(0.0f);
-          state[i] = make_uint4((uint32_t)(i % W) | ((uint32_t)(i / W) << 16), 0, 0, s->inpaint_index);
-        }
-      }
-      locked = resolved.size();
-    } else {
-      unresolved.resize(N);
-      for (size_t i = 0; i < N; ++i) unresolved[i] = (uint32_t)i;
-    }
-    auto pick = [&](uint64_t seed) -> uint32_t {
-      Pcg32 r = pcg_from_u64(seed);
-      const uint64_t idx = gen_range_u64(r, unresolved.size());
-      const uint32_t v = unresolved[idx];
-      unresolved[idx] = unresolved.back();
-      unresolved.pop_back();
-      return v;
-    };
-    // ---- random init (session.rs:42-52, ms.rs:427-475): all examples ----
-    if (p.has_random_init) {
-      if (p.random_init > unresolved.size())
-        throw Failure{TS_ERR_INVALID_RANGE, "random_init exceeds the number of pixels to synthesise"};
-      for (uint64_t i = 0; i < p.random_init; ++i) {
-        const uint32_t px = pick(p.seed + i);
-        const uint64_t sd = p.seed + i + (uint64_t)px;
-        Pcg32 r = pcg_from_u64(sd);
-        const uint32_t map = (uint32_t)gen_range_u64(r, s->n_ex);
-        const Image &im = s->bottoms[map];
-        r = pcg_from_u64(sd);
-        const uint32_t x = gen_range_u32(r, im.w);
-        r = pcg_from_u64(sd);
-        const uint32_t y = gen_range_u32(r, im.h);
-        if (x > 0xffffu || y > 0xffffu) throw Failure{TS_ERR_LIMIT, "example side exceeds limit"};
-        state[px] = make_uint4(x | (y << 16), px, map, map);
-        const uint8_t *c = &im.px[((size_t)y * im.w + x) * 4];
-        color[px] = (uint32_t)c[0] | ((uint32_t)c[1] << 8) | ((uint32_t)c[2] << 16) | ((uint32_t)c[3] << 24);
-        resolved.push_back(px);
-        rscore.push_back(0.0f);
-      }
-      locked += p.random_init;
-    }
-    const size_t total = unresolved.size();
-    // ---- the schedule of Generator::resolve ----
-    const int32_t x_l = (int32_t)((float)W * kTilingBoundary), y_b = (int32_t)((float)H * kTilingBoundary);
-    const float sig2 = p.cauchy * p.cauchy;
-    float cauchy[256], l2[256];
-    for (int d = 0; d < 256; ++d) {
-      const float x = ((float)d - 0.0f) / 255.0f;
-      const float x2 = x * x;
-      cauchy[d] = log1pf(x2 / sig2);
-      l2[d] = x2;
-    }
-    std::vector<StagePlan> plan;
-    std::vector<uint32_t> items;
-    std::vector<float> luts;
-    size_t n_res = resolved.size();
-    int32_t pyramid_level = 0;
-    uint32_t max_batch_items = 1, max_stage_items = 1;
-    const std::vector<int32_t> tab = knn_table(kKnnTabRadius);
-    for (int32_t ps = (int32_t)stages; ps >= 0; --ps) {
-      StagePlan sp;
-      sp.p_stage = ps;
-      sp.level = (uint32_t)pyramid_level;
-      sp.level_switch = pyramid_level > 0;
-      pyramid_level += 1;
-      if (pyramid_level > (int32_t)stages - 1) pyramid_level = (int32_t)stages - 1;
-      sp.seed = pcg_stage_seed(p.seed + (uint64_t)ps);
-      const float fp = powf(p.backtrack_percent, (float)ps) * (float)total;
-      size_t P = fp >= 0.0f ? (size_t)fp : 0;  // `as usize` saturates NaN and negatives to 0
-      const size_t redo = n_res - locked;
-      float adaptive = 0.0f;
-      if (s->guided && ps > 0) {
-        const float a = p.alpha * (1.0f - ((float)n_res / (float)total));
-        adaptive = (a * a) * a;
-      }
-      // stage LUTs (ms.rs:853-858): content = (1 - a) * cauchy when guided
-      bool slow = false;
-      for (int d = 0; d < 256; ++d) {
-        const float c = s->guided ? (1.0f - adaptive) * cauchy[d] : cauchy[d];
-        luts.push_back(c);
-        slow |= !std::isfinite(c);
-      }
-      for (int d = 0; d < 256; ++d) {
-        const float gv = s->guided ? adaptive * l2[d] : 0.0f;
-        luts.push_back(gv);
-        slow |= !std::isfinite(gv);
-      }
-      sp.slow_lut = slow;
-      const size_t P_eff = std::min(P, redo + unresolved.size());
-      sp.items_off = (uint32_t)items.size();
-      sp.n_items = (uint32_t)P_eff;
-      sp.redo = (uint32_t)redo;
-      sp.n_res_start = (uint32_t)n_res;
-      for (size_t i = 0; i < P_eff; ++i) {
-        if (i < redo)
-          items.push_back(resolved[i + locked]);
-        else
-          items.push_back(pick(sp.seed + (uint64_t)i));
-      }
-      size_t i = 0, R = n_res;
-      while (i < P_eff) {
-        size_t bsz = 1;
-        if (p.batch_divisor) {
-          bsz = R / p.batch_divisor;
-          if (bsz < 1) bsz = 1;
-          if (p.max_batch && bsz > p.max_batch) bsz = p.max_batch;
-        }
-        if (bsz > P_eff - i) bsz = P_eff - i;
-        BatchPlan bp;
-        bp.i0 = (uint32_t)i;
-        bp.i1 = (uint32_t)(i + bsz);
-        bp.n_res = (uint32_t)R;
-        bp.append_from = k == 0 ? bp.i0 : std::max<uint32_t>(bp.i0, (uint32_t)std::min(redo, (size_t)bp.i1));
-        // exhaustive k-NN when the table walk is unlikely to find k points
-        bp.exhaustive = k > 0 && (R <= 4096 && (double)R * tab.size() < 2.0 * k * (double)N);
-        const size_t appended = bp.i1 - bp.append_from;
-        for (size_t t = bp.append_from; t < bp.i1; ++t) {
-          resolved.push_back(items[sp.items_off + t]);
-          rscore.push_back(0.0f);
-        }
-        R += appended;
-        sp.batches.push_back(bp);
-        max_batch_items = std::max<uint32_t>(max_batch_items, (uint32_t)bsz);
-        i += bsz;
-      }
-      n_res = R;
-      max_stage_items = std::max<uint32_t>(max_stage_items, (uint32_t)P_eff);
-      plan.push_back(std::move(sp));
-    }
-    // ---- device state and schedule ----
-    DevBuf<uint32_t> d_color, d_occ, d_mir, d_res, d_items, d_ncnt, d_fbl, d_fbc;
-    DevBuf<uint4> d_state;
-    DevBuf<float> d_rscore, d_lut;
-    DevBuf<double> d_xdiv, d_ydiv, d_dist, d_dxt, d_dy2t, d_mean;
-    DevBuf<int32_t> d_tab, d_nbuf;
-    DevBuf<uint2> d_rcand;
-    DevBuf<Result> d_result;
-    DevBuf<int> d_err;
-    DevBuf<unsigned long long> d_evals;
-    const uint32_t wpr = (W + 31) / 32;
-    size_t n_batches = 0;
-    for (auto &sp : plan) n_batches += sp.batches.size();
-    CUDA_TRY(d_color.alloc(N));
-    CUDA_TRY(d_state.alloc(N));
-    CUDA_TRY(d_occ.alloc((size_t)wpr * H));
-    CUDA_TRY(d_mir.alloc((size_t)wpr * H));
-    CUDA_TRY(d_res.alloc(resolved.size()));
-    CUDA_TRY(d_rscore.alloc(resolved.size()));
-    CUDA_TRY(d_items.alloc(items.size()));
-    CUDA_TRY(d_lut.alloc(luts.size()));
-    CUDA_TRY(d_tab.alloc(tab.size()));
-    CUDA_TRY(d_nbuf.alloc((size_t)max_batch_items * std::max<uint32_t>(k, 1)));
-    CUDA_TRY(d_ncnt.alloc(max_batch_items));
-    CUDA_TRY(d_dist.alloc((size_t)max_batch_items * std::max<uint32_t>(k, 1)));
-    CUDA_TRY(d_mean.alloc(max_batch_items));
-    CUDA_TRY(d_fbl.alloc(max_batch_items));
-    CUDA_TRY(d_fbc.alloc(n_batches));
-    CUDA_TRY(d_result.alloc(max_batch_items));
-    CUDA_TRY(d_err.alloc(1));
-    CUDA_TRY(d_evals.alloc(1));
-    const uint64_t rc_items = std::max<uint64_t>(1, std::min<uint64_t>(max_stage_items, kRcandBudget / std::max(m, 1u)));
-    CUDA_TRY(d_rcand.alloc((size_t)std::max<uint64_t>(rc_items, max_batch_items) * m));
-    const int32_t xo = x_l + 2, yo = y_b + 2;
-    std::vector<double> xdiv(W + 2 * (size_t)xo + 1), ydiv(H + 2 * (size_t)yo + 1);
-    for (size_t i = 0; i < xdiv.size(); ++i) xdiv[i] = (double)((int64_t)i - xo) / (double)W;
-    for (size_t i = 0; i < ydiv.size(); ++i) ydiv[i] = (double)((int64_t)i - yo) / (double)H;
-    CUDA_TRY(d_xdiv.alloc(xdiv.size()));
-    CUDA_TRY(d_ydiv.alloc(ydiv.size()));
-    // per-pixel tables of the normalised offsets the weights use: dx and
-    // dy * dy for |offset| <= kDistTabRadius, the same IEEE operations as
-    // get_distances_to_k_neighs (ms.rs:410-415)
-    const int32_t R = kDistTabRadius;
-    std::vector<double> dxt((size_t)W * (2 * R + 1)), dy2t((size_t)H * (2 * R + 1));
-    for (uint32_t x = 0; x < W; ++x)
-      for (int32_t o = -R; o <= R; ++o)
-        dxt[(size_t)x * (2 * R + 1) + o + R] = (double)((int64_t)x + o) / (double)W - (double)x / (double)W;
-    for (uint32_t y = 0; y < H; ++y)
-      for (int32_t o = -R; o <= R; ++o) {
-        const double dy = (double)((int64_t)y + o) / (double)H - (double)y / (double)H;
-        dy2t[(size_t)y * (2 * R + 1) + o + R] = dy * dy;
-      }
-    CUDA_TRY(d_dxt.alloc(dxt.size()));
-    CUDA_TRY(d_dy2t.alloc(dy2t.size()));
-    // the tree is rebuilt from the resolved list, mirrors included (ms.rs:747-779)
-    std::vector<uint32_t> occ((size_t)wpr * H, 0), mir((size_t)wpr * H, 0);
-    for (size_t i = 0; i < locked; ++i) {
-      const uint32_t q = resolved[i];
-      occ[(size_t)(q / W) * wpr + (q % W) / 32] |= 1u << ((q % W) & 31);
-      if (p.tiling) mir[(size_t)(q / W) * wpr + (q % W) / 32] |= 1u << ((q % W) & 31);
-    }
-    cudaEvent_t ev0, ev1;
-    CUDA_TRY(cudaEventCreate(&ev0));
-    CUDA_TRY(cudaEventCreate(&ev1));
-    struct EvGuard {
-      cudaEvent_t a, b;
-      ~EvGuard() {
-        cudaEventDestroy(a);
-        cudaEventDestroy(b);
-      }
-    } eg{ev0, ev1};
-    CUDA_TRY(cudaEventRecord(ev0, st));
-    CUDA_TRY(cudaMemcpyAsync(d_color.p, color.data(), N * 4, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_state.p, state.data(), N * sizeof(uint4), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_occ.p, occ.data(), occ.size() * 4, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_mir.p, mir.data(), mir.size() * 4, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_res.p, resolved.data(), locked * 4, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemsetAsync(d_rscore.p, 0, resolved.size() * 4, st));
-    if (!items.empty())
-      CUDA_TRY(cudaMemcpyAsync(d_items.p, items.data(), items.size() * 4, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_lut.p, luts.data(), luts.size() * 4, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_tab.p, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_xdiv.p, xdiv.data(), xdiv.size() * 8, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_ydiv.p, ydiv.data(), ydiv.size() * 8, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_dxt.p, dxt.data(), dxt.size() * 8, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_dy2t.p, dy2t.data(), dy2t.size() * 8, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemsetAsync(d_fbc.p, 0, n_batches * 4, st));
-    CUDA_TRY(cudaMemsetAsync(d_err.p, 0, sizeof(int), st));
-    CUDA_TRY(cudaMemsetAsync(d_evals.p, 0, sizeof(unsigned long long), st));
-
-    SessionDev sd{};
-    sd.levels = s->levels.p;
-    sd.plevels = s->plevels.p;
-    sd.pguides = s->pguides.p;
-    sd.guide_dims_differ = s->guide_dims_differ ? 1 : 0;
-    sd.masks = s->masks.p;
-    sd.maps = s->d_maps.p;
-    sd.n_maps = s->n_maps;
-    sd.n_levels = s->n_levels;
-    sd.guides = s->guides.p;
-    sd.gdesc = s->d_gdesc.p;
-    sd.n_guides = s->guided ? s->n_ex : 0;
-    sd.guided = s->guided ? 1 : 0;
-    sd.tguide = s->tguide.p;
-    sd.xdiv = d_xdiv.p;
-    sd.ydiv = d_ydiv.p;
-    sd.xdiv_off = xo;
-    sd.ydiv_off = yo;
-    sd.dxt = d_dxt.p;
-    sd.dy2t = d_dy2t.p;
-    sd.dtab_r = R;
-    sd.color = d_color.p;
-    sd.state = d_state.p;
-    sd.occ = d_occ.p;
-    sd.mir = d_mir.p;
-    sd.resolved = d_res.p;
-    sd.rscore = d_rscore.p;
-    sd.knn_tab = d_tab.p;
-    sd.knn_tab_n = (uint32_t)tab.size();
-    sd.err = d_err.p;
-    sd.evals = d_evals.p;
-    sd.W = W;
-    sd.H = H;
-    sd.wpr = wpr;
-    sd.tiling = p.tiling ? 1 : 0;
-    sd.x_l = x_l;
-    sd.x_r = (int32_t)W - x_l;
-    sd.y_b = y_b;
-    sd.y_t = (int32_t)H - y_b;
-    sd.k = k;
-    sd.m = m;
-    uint64_t launches = 0, batches = 0, resolves = 0;
+    CUDA_TRY(cudaSetDevice(s->prm.device));
+    StreamGuard sg;
+    CUDA_TRY(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
+    const cudaStream_t st = sg.s;
+    run_plan(s, c);
+    EventPair ev;
+    ev.create();
+    CUDA_TRY(cudaEventRecord(ev.a, st));
+    run_upload(c, st);
     LaunchTimer lt;
-    lt.on = p.profile;
+    lt.on = s->prm.profile;
     lt.st = st;
-    size_t fb_index = 0;
-    uint64_t overall_total = 0, overall_current = 0;
-    for (auto &sp : plan) overall_total += sp.n_items;
-    std::vector<uint8_t> prog_img;
-    for (size_t si = 0; si < plan.size(); ++si) {
-      const StagePlan &sp = plan[si];
-      lt.stage = sp.p_stage;
-      lt.items = sp.n_items;
-      if (sp.level_switch) {
-        lt.run(TS_KERNEL_LEVEL_SWITCH, [&] { launch_level_switch(sd, sp.level, sp.n_res_start, st); });
-        ++launches;
-      }
-      StageDev sdv{};
-      sdv.level = sp.level;
-      sdv.slow_lut = sp.slow_lut ? 1 : 0;
-      sdv.lut = d_lut.p + si * 512;
-      sdv.stage_seed = sp.seed;
-      sdv.items = d_items.p + sp.items_off;
-      sdv.redo = sp.redo;
-      // random candidates in chunks of whole batches that fit the buffer
-      size_t bi = 0;
-      while (bi < sp.batches.size()) {
-        size_t bj = bi;
-        const uint32_t c0 = sp.batches[bi].i0;
-        while (bj < sp.batches.size() && (bj == bi || sp.batches[bj].i1 - c0 <= rc_items)) ++bj;
-        const uint32_t c1 = sp.batches[bj - 1].i1;
-        StageDev chunk = sdv;
-        chunk.items = sdv.items + c0;
-        chunk.n_items = c1 - c0;
-        chunk.stage_seed = sp.seed + c0;  // item i's stream is seeded with stage_seed + i + 1
-        chunk.rcand = d_rcand.p;
-        chunk.redo = sp.redo > c0 ? sp.redo - c0 : 0;
-        lt.run(TS_KERNEL_RANDOM_CANDIDATES, [&] { launch_random_candidates(sd, chunk, st); });
-        ++launches;
-        chunk.stage_seed = sp.seed;  // resolve_at_random uses the stage seed itself
-        for (size_t bk = bi; bk < bj; ++bk) {
-          const BatchPlan &bp = sp.batches[bk];
-          lt.items = bp.i1 - bp.i0;
-          BatchDev bd{};
-          bd.i0 = bp.i0 - c0;
-          bd.i1 = bp.i1 - c0;
-          bd.n_res = bp.n_res;
-          bd.append_from = bp.append_from - c0;
-          bd.nbuf = d_nbuf.p;
-          bd.ncnt = d_ncnt.p;
-          bd.fb_list = d_fbl.p;
-          bd.fb_count = d_fbc.p + fb_index++;
-          bd.dist = d_dist.p;
-          bd.mean = d_mean.p;
-          bd.res = d_result.p;
-          if (k > 0) {
-            if (bp.exhaustive) {
-              lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, chunk, bd, true, st); });
-              ++launches;
-            } else {
-              lt.run(TS_KERNEL_KNN_WALK, [&] { launch_knn_walk(sd, chunk, bd, st); });
-              lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, chunk, bd, false, st); });
-              launches += 2;
-            }
-          }
-          if (k > 0 && !bp.exhaustive) {  // the exhaustive k-NN over a whole batch computes the mean itself
-            lt.run(TS_KERNEL_MEAN, [&] { launch_mean(sd, chunk, bd, st); });
-            ++launches;
-          }
-          if (bp.i1 - bp.i0 <= p.team_max_batch)
-            lt.run(TS_KERNEL_RESOLVE,
-                   [&] { launch_resolve_team(sd, chunk, bd, bp.i1 - bp.i0 <= p.team_full_max_batch, st); });
-          else
-            lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve(sd, chunk, bd, st); });
-          lt.run(TS_KERNEL_COMMIT, [&] { launch_commit(sd, chunk, bd, st); });
-          launches += 2;
-          ++batches;
-          resolves += bp.i1 - bp.i0;
-        }
-        bi = bj;
-      }
-      CUDA_TRY(cudaGetLastError());
-      overall_current += sp.n_items;
-      if (progress) {
-        prog_img.resize(N * 4);
-        CUDA_TRY(cudaMemcpyAsync(prog_img.data(), d_color.p, N * 4, cudaMemcpyDeviceToHost, st));
-        CUDA_TRY(cudaStreamSynchronize(st));
-        ts_progress up;
-        up.image = prog_img.data();
-        up.width = W;
-        up.height = H;
-        up.total_current = overall_current;
-        up.total_total = overall_total;
-        up.stage_current = sp.n_items;
-        up.stage_total = sp.n_items;
-        progress(&up, user);
-      }
-    }
-    // ---- results ----
-    g->W = W;
-    g->H = H;
-    std::vector<uint32_t> col(N);
-    std::vector<uint4> stv(N);
-    g->resolved.resize(resolved.size());
-    g->scores.resize(resolved.size());
-    int derr = 0;
-    unsigned long long evals = 0;
-    CUDA_TRY(cudaMemcpyAsync(&evals, d_evals.p, sizeof(evals), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(col.data(), d_color.p, N * 4, cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(stv.data(), d_state.p, N * sizeof(uint4), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(g->resolved.data(), d_res.p, resolved.size() * 4, cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(g->scores.data(), d_rscore.p, resolved.size() * 4, cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(&derr, d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaEventRecord(ev1, st));
+    run_enqueue_plain(c, st, lt, progress, user);
+    run_readback(c, st);
+    CUDA_TRY(cudaEventRecord(ev.b, st));
     CUDA_TRY(cudaStreamSynchronize(st));
-    if (derr == kDevErrIndex) throw Failure{TS_ERR_INDEX, "a map id points past the non-ignored examples"};
-    if (derr == kDevErrNoSample) throw Failure{TS_ERR_NO_VALID_SAMPLE, "no valid sample location found"};
-    if (derr == kDevErrLimit) throw Failure{TS_ERR_LIMIT, "too many equidistant neighbours for the k-NN buffer"};
-    if (derr) throw Failure{TS_ERR_CUDA, "device reported error " + std::to_string(derr)};
-    float ms = 0.0f;
-    CUDA_TRY(cudaEventElapsedTime(&ms, ev0, ev1));
-    g->image.resize(N * 4);
-    memcpy(g->image.data(), col.data(), N * 4);
-    g->coord.resize(N * 3);
-    g->ids.resize(N * 2);
-    for (size_t i = 0; i < N; ++i) {
-      g->coord[3 * i] = stv[i].x & 0xffffu;
-      g->coord[3 * i + 1] = stv[i].x >> 16;
-      g->coord[3 * i + 2] = stv[i].w;
-      g->ids[2 * i] = stv[i].y;
-      g->ids[2 * i + 1] = stv[i].z;
-    }
-    g->stats.resolves = resolves;
-    g->stats.batches = batches;
-    g->stats.stages = plan.size();
-    g->stats.kernel_launches = launches;
-    g->stats.gpu_ms = ms;
-    lt.collect(g->stats, g->launches);
-    g->stats.cost_evals = evals;
+    run_finish(c);
+    c.g->stats.gpu_ms = ev.ms();
+    lt.collect(c.g->stats, c.g->launches);
   } catch (const Failure &f) {
     s->err = f.msg;
     return f.status;
   }
-  g->stats.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
-  *out = g.release();
+  c.g->stats.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
+  *out = c.g.release();
   return TS_OK;
 }
 
@@ -1315,5 +1455,363 @@ int ts_generated_launches(const ts_generated *g, ts_launch_record *out) {
   return TS_OK;
 }
 void ts_generated_free(ts_generated *g) { delete g; }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched form: every session's steps advance together, one launch per phase
+// of a global step carrying one segment per session that has work in it.
+// ---------------------------------------------------------------------------
+struct ts_batch {
+  int device = 0;
+  std::vector<ts_session *> sessions;
+  bool graph = false;
+  bool profile = false;
+  uint32_t plan_threads = 0;
+  uint32_t team_max_items = 8192, team_full_max_items = 1024;
+  ts_batch_stats stats{};
+  std::string err;
+};
+
+namespace {
+
+// Units a session's step hands to a phase (0 = no segment).
+uint32_t phase_units(const Step &stp, const RunCtx &c, int phase) {
+  const bool knn = stp.batch && c.k > 0;
+  switch (phase) {
+    case kPhaseLevelSwitch: return stp.ls ? stp.ls_n_res : 0;
+    case kPhaseRandom: return (stp.rc && c.m > 0) ? stp.rc_st.n_items : 0;
+    case kPhaseWalk: return (knn && !stp.exhaustive) ? stp.n : 0;
+    case kPhaseExhaustive: return (knn && stp.exhaustive) ? stp.n : 0;
+    case kPhaseMean: return (knn && !stp.exhaustive) ? stp.n : 0;
+    case kPhaseResolve:
+    case kPhaseTeamPart:
+    case kPhaseTeamFull: return (stp.batch && stp.resolve == phase) ? stp.n : 0;
+    case kPhaseCommit: return stp.batch ? stp.n : 0;
+    default: return 0;
+  }
+}
+
+// Grid bound per segment of the grid-stride phases: the exhaustive k-NN's
+// fallback segments usually hold few items (the walk finds k points for
+// most), so they get few blocks.
+uint32_t phase_cap(const Step &stp, int phase) {
+  switch (phase) {
+    case kPhaseExhaustive: return 608u;
+    case kPhaseTeamPart:
+    case kPhaseTeamFull: return 152u * 16u;
+    default: return 0;
+  }
+}
+
+struct PlannedLaunch {
+  int phase;
+  uint32_t seg0, n_segs, blocks;
+  size_t smem;
+  uint32_t fb0 = 0, n_fb = 0, pool_block0 = 0;  // exhaustive k-NN: fallback lists drained by a block pool
+};
+
+// Blocks of the exhaustive k-NN's fallback pool (three 64 KB CTAs per SM).
+constexpr uint32_t kFallbackPool = 152u * 3u;
+
+}  // namespace
+
+extern "C" {
+
+ts_batch *ts_batch_new(int32_t device) {
+  ts_batch *b = new (std::nothrow) ts_batch();
+  if (b) b->device = device;
+  return b;
+}
+void ts_batch_free(ts_batch *b) {
+  if (!b) return;
+  for (ts_session *s : b->sessions) delete s;
+  delete b;
+}
+const char *ts_batch_last_error(const ts_batch *b) { return b ? b->err.c_str() : "null batch"; }
+uint64_t ts_batch_size(const ts_batch *b) { return b ? b->sessions.size() : 0; }
+int ts_batch_use_graph(ts_batch *b, int32_t on) {
+  if (!b) return TS_ERR_NULL;
+  b->graph = on != 0;
+  return TS_OK;
+}
+int ts_batch_profile(ts_batch *b, int32_t on) {
+  if (!b) return TS_ERR_NULL;
+  b->profile = on != 0;
+  return TS_OK;
+}
+int ts_batch_resolve_team(ts_batch *b, uint32_t team_max_items, uint32_t full_max_items) {
+  if (!b) return TS_ERR_NULL;
+  b->team_max_items = team_max_items;
+  b->team_full_max_items = full_max_items;
+  return TS_OK;
+}
+int ts_batch_plan_threads(ts_batch *b, uint32_t n) {
+  if (!b) return TS_ERR_NULL;
+  b->plan_threads = n;
+  return TS_OK;
+}
+void ts_batch_stats_get(const ts_batch *b, ts_batch_stats *out) {
+  if (b && out) *out = b->stats;
+}
+
+int ts_batch_add(ts_batch *b, ts_session *s) {
+  if (!b || !s) return TS_ERR_NULL;
+  if (s->consumed) {
+    b->err = "session already consumed";
+    return TS_ERR_STATE;
+  }
+  if (s->prm.device != b->device) {
+    b->err = "session device " + std::to_string(s->prm.device) + " differs from the batch's " +
+             std::to_string(b->device);
+    return TS_ERR_STATE;
+  }
+  // the batch owns the session's device data from here on; the caller's
+  // handle stays valid but consumed
+  ts_session *own = new (std::nothrow) ts_session();
+  if (!own) return TS_ERR_OUT_OF_MEMORY;
+  *own = std::move(*s);
+  s->consumed = true;
+  s->err = "session handed to a batch";
+  b->sessions.push_back(own);
+  return TS_OK;
+}
+
+int ts_batch_run(ts_batch *b, ts_generated **out) {
+  if (!b || !out) return TS_ERR_NULL;
+  const size_t n = b->sessions.size();
+  if (n == 0) {
+    b->err = "empty batch";
+    return TS_ERR_STATE;
+  }
+  for (size_t i = 0; i < n; ++i) out[i] = nullptr;
+  const auto t_wall0 = std::chrono::steady_clock::now();
+  std::vector<ts_session *> sessions;
+  sessions.swap(b->sessions);
+  struct Owned {
+    std::vector<ts_session *> &v;
+    ~Owned() {
+      for (ts_session *s : v) delete s;
+    }
+  } owned{sessions};
+  std::vector<std::unique_ptr<RunCtx>> ctx(n);
+  size_t current = 0;
+  try {
+    CUDA_TRY(cudaSetDevice(b->device));
+    StreamGuard sg;
+    CUDA_TRY(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
+    const cudaStream_t st = sg.s;
+    size_t max_steps = 0;
+    const auto t_plan0 = std::chrono::steady_clock::now();
+    {
+      // sessions plan independently: host threads take them in turn
+      unsigned nt = b->plan_threads ? b->plan_threads : std::min(32u, std::max(1u, std::thread::hardware_concurrency()));
+      nt = (unsigned)std::min<size_t>(nt, n);
+      std::atomic<size_t> next{0};
+      std::vector<Failure> fails(n, Failure{TS_OK, ""});
+      auto work = [&] {
+        if (cudaSetDevice(b->device) != cudaSuccess) return;
+        for (size_t j = next++; j < n; j = next++) {
+          try {
+            ctx[j].reset(new RunCtx());
+            run_plan(sessions[j], *ctx[j]);
+          } catch (const Failure &f) {
+            fails[j] = f;
+          } catch (const std::bad_alloc &) {
+            fails[j] = Failure{TS_ERR_OUT_OF_MEMORY, "out of host memory"};
+          }
+        }
+      };
+      std::vector<std::thread> pool;
+      for (unsigned i = 1; i < nt; ++i) pool.emplace_back(work);
+      work();
+      for (auto &t : pool) t.join();
+      for (current = 0; current < n; ++current) {
+        if (fails[current].status != TS_OK) throw fails[current];
+        if (!ctx[current]) throw Failure{TS_ERR_CUDA, "cannot select the device"};
+        max_steps = std::max(max_steps, ctx[current]->steps.size());
+      }
+    }
+    const double plan_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_plan0).count();
+    // ---- the launch plan: per global step and phase, one segment per session ----
+    std::vector<SessionDev> h_sess(n);
+    std::vector<size_t> step_base(n);
+    size_t n_steps = 0;
+    for (size_t j = 0; j < n; ++j) {
+      h_sess[j] = ctx[j]->sd;
+      step_base[j] = n_steps;
+      n_steps += ctx[j]->steps.size();
+    }
+    std::vector<StepDev> h_steps(n_steps);
+    for (size_t j = 0; j < n; ++j)
+      for (size_t t = 0; t < ctx[j]->steps.size(); ++t) {
+        const Step &stp = ctx[j]->steps[t];
+        StepDev &d = h_steps[step_base[j] + t];
+        d = StepDev{};
+        d.st = stp.st;
+        d.rc = stp.rc_st;
+        d.b = stp.bd;
+        d.level = stp.ls_level;
+        d.ls_n_res = stp.ls_n_res;
+        d.all_items = stp.exhaustive ? 1 : 0;
+      }
+    std::vector<Segment> h_segs, h_fb;
+    std::vector<PlannedLaunch> launches;
+    size_t phase_smem[kPhases] = {};
+    for (size_t t = 0; t < max_steps; ++t) {
+      // the resolve form follows the step's items over all sessions: the
+      // team forms only pay while the whole launch is too small to fill
+      // the GPU with warps
+      uint64_t step_items = 0;
+      bool all_team_full = true;
+      for (size_t j = 0; j < n; ++j)
+        if (t < ctx[j]->steps.size() && ctx[j]->steps[t].batch) {
+          step_items += ctx[j]->steps[t].n;
+          all_team_full &= team_full_fits(ctx[j]->k, ctx[j]->m);
+        }
+      const int form = step_items > b->team_max_items ? kPhaseResolve
+                       : (step_items <= b->team_full_max_items && all_team_full) ? kPhaseTeamFull
+                                                                                 : kPhaseTeamPart;
+      for (size_t j = 0; j < n; ++j)
+        if (t < ctx[j]->steps.size()) ctx[j]->steps[t].resolve = form;
+      for (int ph = 0; ph < kPhases; ++ph) {
+        PlannedLaunch pl;
+        pl.phase = ph;
+        pl.seg0 = (uint32_t)h_segs.size();
+        pl.n_segs = pl.blocks = 0;
+        pl.smem = 0;
+        pl.fb0 = (uint32_t)h_fb.size();
+        for (size_t j = 0; j < n; ++j) {
+          const RunCtx &c = *ctx[j];
+          if (t >= c.steps.size()) continue;
+          const Step &stp = c.steps[t];
+          if (ph == kPhaseExhaustive && stp.batch && c.k > 0 && !stp.exhaustive) {
+            h_fb.push_back(Segment{0, 0, (uint32_t)j, (uint32_t)(step_base[j] + t)});
+            pl.n_fb += 1;
+            pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
+          }
+          const uint32_t units = phase_units(stp, c, ph);
+          const uint32_t nb = multi_blocks(ph, units, phase_cap(stp, ph));
+          if (nb == 0) continue;
+          h_segs.push_back(Segment{pl.blocks, nb, (uint32_t)j, (uint32_t)(step_base[j] + t)});
+          pl.blocks += nb;
+          pl.n_segs += 1;
+          pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
+        }
+        pl.pool_block0 = pl.blocks;
+        if (pl.n_fb) pl.blocks += kFallbackPool;
+        if (pl.n_segs || pl.n_fb) {
+          phase_smem[ph] = std::max(phase_smem[ph], pl.smem);
+          launches.push_back(pl);
+        }
+      }
+    }
+    for (int ph = 0; ph < kPhases; ++ph) CUDA_TRY(set_multi_smem(ph, phase_smem[ph]));
+    DevBuf<SessionDev> d_sess;
+    DevBuf<StepDev> d_steps;
+    DevBuf<Segment> d_segs, d_fb;
+    CUDA_TRY(d_sess.alloc(n));
+    CUDA_TRY(d_steps.alloc(n_steps));
+    CUDA_TRY(d_segs.alloc(h_segs.size()));
+    CUDA_TRY(d_fb.alloc(h_fb.size()));
+    EventPair ev;
+    ev.create();
+    CUDA_TRY(cudaEventRecord(ev.a, st));
+    for (current = 0; current < n; ++current) run_upload(*ctx[current], st);
+    CUDA_TRY(cudaMemcpyAsync(d_sess.p, h_sess.data(), n * sizeof(SessionDev), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_steps.p, h_steps.data(), n_steps * sizeof(StepDev), cudaMemcpyHostToDevice, st));
+    if (!h_segs.empty())
+      CUDA_TRY(cudaMemcpyAsync(d_segs.p, h_segs.data(), h_segs.size() * sizeof(Segment), cudaMemcpyHostToDevice,
+                               st));
+    if (!h_fb.empty())
+      CUDA_TRY(cudaMemcpyAsync(d_fb.p, h_fb.data(), h_fb.size() * sizeof(Segment), cudaMemcpyHostToDevice, st));
+    std::vector<EventPair> pev(b->profile && !b->graph ? launches.size() : 0);
+    for (auto &e : pev) e.create();
+    auto enqueue = [&](cudaStream_t s) {
+      for (size_t li = 0; li < launches.size(); ++li) {
+        const PlannedLaunch &pl = launches[li];
+        MultiLaunch ml;
+        ml.segs = d_segs.p + pl.seg0;
+        ml.n_segs = pl.n_segs;
+        ml.sessions = d_sess.p;
+        ml.steps = d_steps.p;
+        ml.fb = d_fb.p + pl.fb0;
+        ml.n_fb = pl.n_fb;
+        ml.pool_block0 = pl.n_fb ? pl.pool_block0 : pl.blocks;
+        if (!pev.empty()) CUDA_TRY(cudaEventRecord(pev[li].a, s));
+        launch_multi(pl.phase, ml, pl.blocks, pl.smem, s);
+        if (!pev.empty()) CUDA_TRY(cudaEventRecord(pev[li].b, s));
+      }
+      CUDA_TRY(cudaGetLastError());
+    };
+    if (b->graph) {
+      cudaGraph_t graph = nullptr;
+      cudaGraphExec_t exec = nullptr;
+      CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      try {
+        enqueue(st);
+      } catch (...) {
+        cudaStreamEndCapture(st, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        throw;
+      }
+      CUDA_TRY(cudaStreamEndCapture(st, &graph));
+      struct GraphGuard {
+        cudaGraph_t g;
+        cudaGraphExec_t &e;
+        ~GraphGuard() {
+          if (e) cudaGraphExecDestroy(e);
+          if (g) cudaGraphDestroy(g);
+        }
+      } gg{graph, exec};
+      CUDA_TRY(cudaGraphInstantiate(&exec, graph, 0));
+      CUDA_TRY(cudaGraphLaunch(exec, st));
+      for (current = 0; current < n; ++current) run_readback(*ctx[current], st);
+      CUDA_TRY(cudaEventRecord(ev.b, st));
+      CUDA_TRY(cudaStreamSynchronize(st));
+    } else {
+      enqueue(st);
+      for (current = 0; current < n; ++current) run_readback(*ctx[current], st);
+      CUDA_TRY(cudaEventRecord(ev.b, st));
+      CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    const double gpu_ms = ev.ms();
+    ts_batch_stats bs{};
+    bs.sessions = n;
+    bs.steps = max_steps;
+    bs.launches = launches.size();
+    bs.plan_ms = plan_ms;
+    for (size_t li = 0; li < pev.size(); ++li) {
+      bs.phase_launches[launches[li].phase] += 1;
+      bs.phase_ms[launches[li].phase] += pev[li].ms();
+    }
+    for (current = 0; current < n; ++current) {
+      RunCtx &c = *ctx[current];
+      for (const Step &stp : c.steps)
+        if (stp.batch) {
+          ++c.batches;
+          c.resolves += stp.n;
+        }
+      run_finish(c);
+      c.g->stats.gpu_ms = gpu_ms;
+      c.g->stats.kernel_launches = launches.size();
+      bs.output_pixels += c.N;
+      bs.resolves += c.resolves;
+      bs.cost_evals += c.evals;
+    }
+    bs.gpu_ms = gpu_ms;
+    bs.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
+    b->stats = bs;
+  } catch (const Failure &f) {
+    b->err = "session " + std::to_string(current < n ? current : 0) + ": " + f.msg;
+    return f.status;
+  }
+  for (size_t i = 0; i < n; ++i) {
+    ctx[i]->g->stats.wall_ms = b->stats.wall_ms;
+    out[i] = ctx[i]->g.release();
+  }
+  return TS_OK;
+}
 
 }  // extern "C"
