@@ -42,7 +42,12 @@ def run_both(ts, oracle, spec, divisor=8, max_batch=0, team=None, full=1024):
 def test_resolve_forms(ts, oracle, wl, team, full):
     """Resolve kernel forms on every batch: warp per item; CTA per item with
     early exit; CTA per item scoring every candidate."""
-    for spec in (wl.config0(out=64, ex=32), wl.config1(out=64, ex=32), wl.config2(out=64, ex=32)):
+    specs = [wl.config0(out=64, ex=32), wl.config1(out=64, ex=32), wl.config2(out=64, ex=32)]
+    mixed = wl.config1(out=48, ex=20)  # examples of different sizes: one padded pitch for all
+    mixed["examples"][1]["image"] = wl.texture(77, 13, 29)
+    mixed["examples"][2]["image"] = wl.texture(78, 31, 9)
+    specs.append(mixed)
+    for spec in specs:
         got, ref = run_both(ts, oracle, spec, team=team, full=full)
         assert_same(got, ref, "%s team=%d full=%d" % (spec["name"], team, full))
 

@@ -34,6 +34,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <utility>
 
 #include "ts_common.h"
 #include "ts_kernels.cuh"
@@ -544,6 +545,8 @@ __device__ __forceinline__ void mean_body(const SessionDev &s, const BatchDev &b
 struct WarpSmem {
   uint4 *nbr;
   uint32_t *cxy, *caux;
+  float *term;   // candidate 0's neighbour terms
+  int32_t *lin;  // neighbour offsets as texel offsets on the padded planes (dy * ppitch + dx)
 };
 
 __device__ __forceinline__ size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
@@ -552,6 +555,8 @@ __host__ __device__ __forceinline__ size_t warp_smem_bytes(uint32_t k, uint32_t 
   const size_t kk = k ? k : 1;
   size_t b = kk * 16;                            // nbr
   b += (((kk + m) * 4 + 15) & ~(size_t)15) * 2;  // cxy, caux
+  b += (kk * 4 + 15) & ~(size_t)15;              // term
+  b += (kk * 4 + 15) & ~(size_t)15;              // lin
   return b;
 }
 
@@ -564,6 +569,10 @@ __device__ __forceinline__ WarpSmem carve(unsigned char *base, uint32_t k, uint3
   w.cxy = (uint32_t *)p;
   p += align16((kk + m) * 4);
   w.caux = (uint32_t *)p;
+  p += align16((kk + m) * 4);
+  w.term = (float *)p;
+  p += align16(kk * 4);
+  w.lin = (int32_t *)p;
   return w;
 }
 
@@ -575,18 +584,23 @@ __device__ __forceinline__ uint32_t texel(const uint32_t *lv, const MapDesc &md,
 }
 
 // Sum of the four channel LUT terms in channel order, starting from acc.
+// The byte offsets of the four entries come straight from the packed
+// differences (d >> (8c - 2)) & 0x3fc.
 __device__ __forceinline__ float lut4(const float *lut, uint32_t d, float acc) {
-  acc = __fadd_rn(acc, lut[d & 255u]);
-  acc = __fadd_rn(acc, lut[(d >> 8) & 255u]);
-  acc = __fadd_rn(acc, lut[(d >> 16) & 255u]);
-  acc = __fadd_rn(acc, lut[d >> 24]);
+  const char *lb = (const char *)lut;
+  acc = __fadd_rn(acc, *(const float *)(lb + ((d << 2) & 0x3fcu)));
+  acc = __fadd_rn(acc, *(const float *)(lb + ((d >> 6) & 0x3fcu)));
+  acc = __fadd_rn(acc, *(const float *)(lb + ((d >> 14) & 0x3fcu)));
+  acc = __fadd_rn(acc, *(const float *)(lb + ((d >> 22) & 0x3fcu)));
   return acc;
 }
 
-// Cost of candidate c (better_match, ms.rs:1225-1288), abandoning as soon as
-// the partial sum reaches `bound`; bounds-checked gathers (out-of-bounds
-// texels read Rgba(0,0,0,255)), issued four neighbours ahead.  Returns false
-// when abandoned.
+// Cost of candidate c (better_match, ms.rs:1225-1288), abandoning once the
+// partial sum reaches `bound`; bounds-checked gathers (out-of-bounds texels
+// read Rgba(0,0,0,255)), issued four neighbours ahead.  Returns false when
+// abandoned.  The terms are never negative, so partial sums never decrease
+// and testing every fourth one, and the total, decides as the reference's
+// test after every term does.
 __device__ __forceinline__ bool candidate_cost(const SessionDev &s, const StageDev &st, const WarpSmem &w,
                                                const float *lc, const float *lg, uint32_t nk, uint32_t cxy,
                                                uint32_t aux, float bound, float &out) {
@@ -622,8 +636,8 @@ __device__ __forceinline__ bool candidate_cost(const SessionDev &s, const StageD
       float nps = lut4(lc, __vabsdiffu4(nr[u].y, t[u]), 0.0f);
       if (s.guided) nps = lut4(lg, __vabsdiffu4(nr[u].z, gt[u]), nps);
       score = __fadd_rn(score, __fmul_rn(nps, __uint_as_float(nr[u].w)));
-      if (score >= bound) return false;
     }
+    if (score >= bound) return false;
   }
   out = score;
   return true;
@@ -639,14 +653,9 @@ __device__ __forceinline__ bool candidate_cost_padded(const SessionDev &s, const
   const int sg = (aux & kAuxNeg) ? -1 : 1;
   const MapDesc md = s.maps[map];
   const int cx = (int)(cxy & 0xffffu), cy = (int)(cxy >> 16);
-  const int pw = (int)md.pw;
-  const uint32_t *base = s.plevels + md.poff + (size_t)st.level * md.pw * md.ph +
-                         (size_t)(cy + kPad) * md.pw + (cx + kPad);
-  const uint32_t *gbase = nullptr;
-  if (kGuided) {
-    const GuideDesc gd = s.gdesc[map];
-    gbase = s.pguides + gd.poff + (size_t)st.level * gd.pw * gd.ph + (size_t)(cy + kPad) * gd.pw + (cx + kPad);
-  }
+  const size_t poff = md.poff + (size_t)st.level * md.pw * md.ph + (size_t)(cy + kPad) * md.pw + (cx + kPad);
+  const uint32_t *base = s.plevels + poff;
+  const uint32_t *gbase = kGuided ? s.pguides + poff : nullptr;
   float score = 0.0f;
   uint32_t j = 0;
   for (; j + 4 <= nk; j += 4) {
@@ -655,7 +664,7 @@ __device__ __forceinline__ bool candidate_cost_padded(const SessionDev &s, const
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       nr[u] = w.nbr[j + u];
-      const int lin = sg * (off_dy((int32_t)nr[u].x) * pw + off_dx((int32_t)nr[u].x));
+      const int lin = sg * w.lin[j + u];
       t[u] = __ldg(base + lin);
       if (kGuided) gt[u] = __ldg(gbase + lin);
     }
@@ -664,17 +673,17 @@ __device__ __forceinline__ bool candidate_cost_padded(const SessionDev &s, const
       float nps = lut4(lc, __vabsdiffu4(nr[u].y, t[u]), 0.0f);
       if (kGuided) nps = lut4(lg, __vabsdiffu4(nr[u].z, gt[u]), nps);
       score = __fadd_rn(score, __fmul_rn(nps, __uint_as_float(nr[u].w)));
-      if (score >= bound) return false;
     }
+    if (score >= bound) return false;
   }
   for (; j < nk; ++j) {
     const uint4 nr = w.nbr[j];
-    const int lin = sg * (off_dy((int32_t)nr.x) * pw + off_dx((int32_t)nr.x));
+    const int lin = sg * w.lin[j];
     float nps = lut4(lc, __vabsdiffu4(nr.y, __ldg(base + lin)), 0.0f);
     if (kGuided) nps = lut4(lg, __vabsdiffu4(nr.z, __ldg(gbase + lin)), nps);
     score = __fadd_rn(score, __fmul_rn(nps, __uint_as_float(nr.w)));
-    if (score >= bound) return false;
   }
+  if (score >= bound) return false;
   out = score;
   return true;
 }
@@ -707,6 +716,7 @@ __device__ __forceinline__ bool neighbour_setup(const SessionDev &s, const Stage
   uint32_t gpat = 0;
   if (s.guided) gpat = inb ? __ldg(&s.tguide[(size_t)st.level * s.W * s.H + (size_t)qy * s.W + qx]) : kOutside;
   w.nbr[j] = make_uint4((uint32_t)off, pat, gpat, __float_as_uint(wv));
+  w.lin[j] = off_dy(off) * (int)s.ppitch + off_dx(off);
   const int wx = modi(nx, W), wy = modi(ny, H);
   const uint4 sv = s.state[(size_t)wy * s.W + wx];
   const uint32_t map = sv.z;
@@ -720,6 +730,45 @@ __device__ __forceinline__ bool neighbour_setup(const SessionDev &s, const Stage
   cxy = (uint32_t)ccx | ((uint32_t)ccy << 16);
   aux = map | (j << 16);
   return true;
+}
+
+// Candidate 0's exact score (better_match, ms.rs:1225-1288, with no bound):
+// lane j of a group of G lanes (a warp, or a CTA's warp) computes the terms
+// nps_j * w_j of neighbours j, j + G, ..., lane 0 sums them in order; every
+// lane returns the sum.
+template <int G>
+__device__ __forceinline__ float candidate0_score(const SessionDev &s, const StageDev &st, const WarpSmem &w,
+                                                  const float *lc, const float *lg, uint32_t nk, int gl,
+                                                  uint32_t gmask) {
+  const uint32_t cxy0 = w.cxy[0], aux0 = w.caux[0];
+  const uint32_t map = aux0 & 0x7fffu;
+  const bool neg = (aux0 & kAuxNeg) != 0;
+  const MapDesc md = s.maps[map];
+  const uint32_t *lv = s.levels + md.off + (size_t)st.level * md.w * md.h;
+  const int cx = (int)(cxy0 & 0xffffu), cy = (int)(cxy0 >> 16);
+  for (uint32_t j = gl; j < nk; j += G) {
+    const uint4 nr = w.nbr[j];
+    int dx = off_dx((int32_t)nr.x), dy = off_dy((int32_t)nr.x);
+    if (neg) {
+      dx = -dx;
+      dy = -dy;
+    }
+    const int qx = cx + dx, qy = cy + dy;
+    float nps = lut4(lc, __vabsdiffu4(nr.y, texel(lv, md, qx, qy)), 0.0f);
+    if (s.guided) {
+      const GuideDesc gd = s.gdesc[map];
+      const uint32_t *gv = s.guides + gd.off + (size_t)st.level * gd.w * gd.h;
+      uint32_t gt = kOutside;
+      if ((unsigned)qx < gd.w && (unsigned)qy < gd.h) gt = __ldg(&gv[(size_t)qy * gd.w + qx]);
+      nps = lut4(lg, __vabsdiffu4(nr.z, gt), nps);
+    }
+    w.term[j] = __fmul_rn(nps, __uint_as_float(nr.w));
+  }
+  __syncwarp(gmask);
+  float sc = 0.0f;
+  if (gl == 0)
+    for (uint32_t j = 0; j < nk; ++j) sc = __fadd_rn(sc, w.term[j]);
+  return __shfl_sync(gmask, sc, 0, G);
 }
 
 // The reference's sequential find_best_match (ms.rs:1184-1221), for stages or
@@ -915,7 +964,14 @@ __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev
     float best_s = FLT_MAX;
     uint32_t best_i = 0;
     if (!slow) {
-      for (uint32_t base = 0; base < nc; base += kWarp) {
+      // candidate 0 first: its terms on all lanes, their in-order sum on
+      // lane 0; it wins ties with every later candidate, so the rest run
+      // against min(S_0, f32::MAX) from the start
+      {
+        const float s0 = candidate0_score<kWarp>(s, st, w, lc, lg, nk, lane, 0xffffffffu);
+        if (s0 < best_s) best_s = s0;
+      }
+      for (uint32_t base = 1; base < nc; base += kWarp) {
         const uint32_t c = base + lane;
         float sc = 0.0f;
         bool alive = false;
@@ -949,6 +1005,7 @@ __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev
     if (lane == 0) write_result(s, w, b, local, pixel, px, py, is_new, nc, best_s, best_i);
   }
 }
+
 
 // ---------------------------------------------------------------------------
 // resolve, team form: one CTA of T threads per item, one candidate per
@@ -1302,8 +1359,8 @@ __global__ void k_resize_h(const float *tmp, uint32_t w, uint32_t nh, uint8_t *d
 }
 
 // Padded copy: dst[l][y + kPad][x + kPad] = src[l][y][x], border = kOutside.
-__global__ void k_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, uint32_t *dst) {
-  const uint32_t pw = w + 2 * kPad, ph = h + 2 * kPad;
+__global__ void k_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, uint32_t pw, uint32_t *dst) {
+  const uint32_t ph = h + 2 * kPad;
   const size_t n = (size_t)pw * ph * levels;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const size_t l = i / ((size_t)pw * ph);
@@ -1311,6 +1368,16 @@ __global__ void k_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t leve
     const int y = (int)(r / pw) - kPad, x = (int)(r % pw) - kPad;
     dst[i] = ((unsigned)x < w && (unsigned)y < h) ? src[l * w * h + (size_t)y * w + x] : kOutside;
   }
+}
+
+// Programmatic dependent launch: every hot-loop kernel first waits for the
+// kernel before it in the stream to complete (its memory is then visible),
+// then lets the next one launch, whose blocks start and wait in turn while
+// this one's last wave runs.  Kernels launched without the attribute pass
+// both instructions at once.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -1340,31 +1407,38 @@ __device__ __forceinline__ SegView find_segment(const MultiLaunch &ml) {
   const Segment g = ml.segs[j];
   SegView v;
   v.s = ml.sessions + g.session;
-  v.d = ml.steps + g.step;
+  v.d = ml.step_tabs[g.session] + g.step;
   v.vb = bx - g.block0;
   v.vg = g.nblocks;
   return v;
 }
 
-__global__ void k_random_candidates(SessionDev s, StageDev st) { random_candidates_body(s, st, blockIdx.x); }
+__global__ void k_random_candidates(SessionDev s, StageDev st) {
+  pdl_enter(); random_candidates_body(s, st, blockIdx.x); }
 __global__ void k_random_candidates_multi(MultiLaunch ml) {
+  pdl_enter();
   const SegView v = find_segment(ml);
   random_candidates_body(*v.s, v.d->rc, v.vb);
 }
 
 __global__ void __launch_bounds__(kWalkWarps *kWarp, 4) k_knn_walk(SessionDev s, StageDev st, BatchDev b) {
+  pdl_enter();
   knn_walk_body(s, st, b, blockIdx.x, gridDim.x);
 }
 __global__ void __launch_bounds__(kWalkWarps *kWarp, 4) k_knn_walk_multi(MultiLaunch ml) {
+  pdl_enter();
   const SegView v = find_segment(ml);
   knn_walk_body(*v.s, v.d->st, v.d->b, v.vb, v.vg);
 }
 
 __global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive(SessionDev s, StageDev st, BatchDev b,
                                                                  int all_items) {
+  pdl_enter();
+  pdl_enter();
   knn_exhaustive_body(s, st, b, all_items, blockIdx.x, gridDim.x);
 }
 __global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive_multi(MultiLaunch ml) {
+  pdl_enter();
   __shared__ ExhShared sh;
   extern __shared__ unsigned long long all_keys[];
   if (blockIdx.x < ml.pool_block0) {  // whole batches of sparse steps
@@ -1385,14 +1459,17 @@ __global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive_multi(MultiLaunc
   for (uint32_t c0 = 0; c0 < ml.n_fb; c0 += kExhThreads) {
     const uint32_t nc = min((uint32_t)kExhThreads, ml.n_fb - c0);
     __syncthreads();
-    if (threadIdx.x < nc) fb_cnt[threadIdx.x] = *ml.steps[ml.fb[c0 + threadIdx.x].step].b.fb_count;
+    if (threadIdx.x < nc) {
+      const Segment g = ml.fb[c0 + threadIdx.x];
+      fb_cnt[threadIdx.x] = *ml.step_tabs[g.session][g.step].b.fb_count;
+    }
     __syncthreads();
     for (uint32_t j = 0; j < nc; ++j) {
       const uint32_t cnt = fb_cnt[j];
       uint32_t v = base + (vb + vg - base % vg) % vg;
       if (v < base + cnt) {
         const Segment g = ml.fb[c0 + j];
-        const StepDev &d = ml.steps[g.step];
+        const StepDev &d = ml.step_tabs[g.session][g.step];
         for (; v < base + cnt; v += vg) {
           knn_exhaustive_item(ml.sessions[g.session], d.st, d.b, d.b.fb_list[v - base], sh, all_keys, false);
           __syncthreads();
@@ -1403,45 +1480,71 @@ __global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive_multi(MultiLaunc
   }
 }
 
-__global__ void __launch_bounds__(128) k_mean(SessionDev s, StageDev st, BatchDev b) { mean_body(s, b, blockIdx.x); }
+__global__ void __launch_bounds__(128) k_mean(SessionDev s, StageDev st, BatchDev b) {
+  pdl_enter(); mean_body(s, b, blockIdx.x); }
 __global__ void __launch_bounds__(128) k_mean_multi(MultiLaunch ml) {
+  pdl_enter();
   const SegView v = find_segment(ml);
   mean_body(*v.s, v.d->b, v.vb);
 }
 
 __global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve(SessionDev s, StageDev st, BatchDev b) {
+  pdl_enter();
   resolve_body(s, st, b, blockIdx.x, gridDim.x);
 }
 __global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve_multi(MultiLaunch ml) {
+  pdl_enter();
   const SegView v = find_segment(ml);
   resolve_body(*v.s, v.d->st, v.d->b, v.vb, v.vg);
 }
 
 template <int T, bool kFull>
 __global__ void __launch_bounds__(T) k_resolve_team(SessionDev s, StageDev st, BatchDev b) {
+  pdl_enter();
   resolve_team_body<T, kFull>(s, st, b, blockIdx.x, gridDim.x);
 }
 template <int T, bool kFull>
 __global__ void __launch_bounds__(T) k_resolve_team_multi(MultiLaunch ml) {
+  pdl_enter();
   const SegView v = find_segment(ml);
   resolve_team_body<T, kFull>(*v.s, v.d->st, v.d->b, v.vb, v.vg);
 }
 
-__global__ void k_commit(SessionDev s, StageDev st, BatchDev b) { commit_body(s, st, b, blockIdx.x); }
+__global__ void k_commit(SessionDev s, StageDev st, BatchDev b) {
+  pdl_enter(); commit_body(s, st, b, blockIdx.x); }
 __global__ void k_commit_multi(MultiLaunch ml) {
+  pdl_enter();
   const SegView v = find_segment(ml);
   commit_body(*v.s, v.d->st, v.d->b, v.vb);
 }
 
 __global__ void k_level_switch(SessionDev s, uint32_t level, uint32_t n_res) {
+  pdl_enter();
   level_switch_body(s, level, n_res, blockIdx.x);
 }
 __global__ void k_level_switch_multi(MultiLaunch ml) {
+  pdl_enter();
   const SegView v = find_segment(ml);
   level_switch_body(*v.s, v.d->level, v.d->ls_n_res, v.vb);
 }
 
 inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 }  // namespace
 
@@ -1489,6 +1592,7 @@ cudaError_t set_multi_smem(int phase, size_t bytes) {
 }
 
 bool team_full_fits(uint32_t k, uint32_t m) { return team_full_smem_bytes(k, m) <= kTeamFullMaxSmem; }
+
 
 uint32_t multi_threads(int phase) {
   switch (phase) {
@@ -1539,28 +1643,28 @@ void launch_multi(int phase, const MultiLaunch &ml, uint32_t blocks, size_t smem
   if (blocks == 0) return;  // a launch may carry only the exhaustive k-NN's fallback pool (no segments)
   const uint32_t t = multi_threads(phase);
   switch (phase) {
-    case kPhaseLevelSwitch: k_level_switch_multi<<<blocks, t, 0, stream>>>(ml); break;
-    case kPhaseRandom: k_random_candidates_multi<<<blocks, t, 0, stream>>>(ml); break;
-    case kPhaseWalk: k_knn_walk_multi<<<blocks, t, 0, stream>>>(ml); break;
-    case kPhaseExhaustive: k_knn_exhaustive_multi<<<blocks, t, smem, stream>>>(ml); break;
-    case kPhaseMean: k_mean_multi<<<blocks, t, 0, stream>>>(ml); break;
-    case kPhaseResolve: k_resolve_multi<<<blocks, t, smem, stream>>>(ml); break;
-    case kPhaseTeamPart: k_resolve_team_multi<kTeamThreads, false><<<blocks, t, smem, stream>>>(ml); break;
-    case kPhaseTeamFull: k_resolve_team_multi<kTeamThreads, true><<<blocks, t, smem, stream>>>(ml); break;
-    case kPhaseCommit: k_commit_multi<<<blocks, t, 0, stream>>>(ml); break;
+    case kPhaseLevelSwitch: launch_pdl(k_level_switch_multi, blocks, t, 0, stream, ml); break;
+    case kPhaseRandom: launch_pdl(k_random_candidates_multi, blocks, t, 0, stream, ml); break;
+    case kPhaseWalk: launch_pdl(k_knn_walk_multi, blocks, t, 0, stream, ml); break;
+    case kPhaseExhaustive: launch_pdl(k_knn_exhaustive_multi, blocks, t, smem, stream, ml); break;
+    case kPhaseMean: launch_pdl(k_mean_multi, blocks, t, 0, stream, ml); break;
+    case kPhaseResolve: launch_pdl(k_resolve_multi, blocks, t, smem, stream, ml); break;
+    case kPhaseTeamPart: launch_pdl(k_resolve_team_multi<kTeamThreads, false>, blocks, t, smem, stream, ml); break;
+    case kPhaseTeamFull: launch_pdl(k_resolve_team_multi<kTeamThreads, true>, blocks, t, smem, stream, ml); break;
+    case kPhaseCommit: launch_pdl(k_commit_multi, blocks, t, 0, stream, ml); break;
     default: break;
   }
 }
 
 void launch_random_candidates(const SessionDev &s, const StageDev &st, cudaStream_t stream) {
   if (st.n_items == 0 || s.m == 0) return;
-  k_random_candidates<<<cdiv(st.n_items, 128), 128, 0, stream>>>(s, st);
+  launch_pdl(k_random_candidates, cdiv(st.n_items, 128), 128, 0, stream, s, st);
 }
 
 void launch_knn_walk(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
   const uint32_t n = b.i1 - b.i0;
   if (n == 0) return;
-  k_knn_walk<<<cdiv(n, kWalkWarps), kWalkWarps * kWarp, 0, stream>>>(s, st, b);
+  launch_pdl(k_knn_walk, cdiv(n, kWalkWarps), kWalkWarps * kWarp, 0, stream, s, st, b);
 }
 
 void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchDev &b, bool all_items,
@@ -1568,20 +1672,20 @@ void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchD
   const uint32_t n = b.i1 - b.i0;
   if (n == 0) return;
   const uint32_t grid = n < 608u ? n : 608u;  // 152 SMs x 4 CTAs, grid-stride beyond
-  k_knn_exhaustive<<<grid, kExhThreads, (size_t)kExhAllKeys * 8, stream>>>(s, st, b, all_items ? 1 : 0);
+  launch_pdl(k_knn_exhaustive, grid, kExhThreads, (size_t)kExhAllKeys * 8, stream, s, st, b, all_items ? 1 : 0);
 }
 
 void launch_mean(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
   const uint32_t n = b.i1 - b.i0;
   if (n == 0 || s.k == 0) return;
-  k_mean<<<cdiv(n, 128), 128, 0, stream>>>(s, st, b);
+  launch_pdl(k_mean, cdiv(n, 128), 128, 0, stream, s, st, b);
 }
 
 void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
   const uint32_t n = b.i1 - b.i0;
   if (n == 0) return;
   const size_t smem = resolve_smem_bytes(s.k, s.m, s.guided);
-  k_resolve<<<cdiv(n, kResolveWarps), kResolveWarps * kWarp, smem, stream>>>(s, st, b);
+  launch_pdl(k_resolve, cdiv(n, kResolveWarps), kResolveWarps * kWarp, smem, stream, s, st, b);
 }
 
 void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev &b, bool full,
@@ -1590,26 +1694,27 @@ void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev
   if (n == 0) return;
   const uint32_t grid = n < 152u * 16u ? n : 152u * 16u;
   if (full && team_full_smem_bytes(s.k, s.m) <= kTeamFullMaxSmem)
-    k_resolve_team<kTeamThreads, true><<<grid, kTeamThreads, team_full_smem_bytes(s.k, s.m), stream>>>(s, st, b);
+    launch_pdl(k_resolve_team<kTeamThreads, true>, grid, kTeamThreads, team_full_smem_bytes(s.k, s.m), stream, s, st, b);
   else
-    k_resolve_team<kTeamThreads, false><<<grid, kTeamThreads, team_smem_bytes(s.k, s.m), stream>>>(s, st, b);
+    launch_pdl(k_resolve_team<kTeamThreads, false>, grid, kTeamThreads, team_smem_bytes(s.k, s.m), stream, s, st, b);
 }
 
 void launch_commit(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
   const uint32_t n = b.i1 - b.i0;
   if (n == 0) return;
-  k_commit<<<cdiv(n, 256), 256, 0, stream>>>(s, st, b);
+  launch_pdl(k_commit, cdiv(n, 256), 256, 0, stream, s, st, b);
 }
 
 void launch_level_switch(const SessionDev &s, uint32_t level, uint32_t n_res, cudaStream_t stream) {
   if (n_res == 0) return;
-  k_level_switch<<<cdiv(n_res, 256), 256, 0, stream>>>(s, level, n_res);
+  launch_pdl(k_level_switch, cdiv(n_res, 256), 256, 0, stream, s, level, n_res);
 }
 
-void launch_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, uint32_t *dst, cudaStream_t stream) {
-  const size_t n = (size_t)(w + 2 * kPad) * (h + 2 * kPad) * levels;
+void launch_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, uint32_t pitch, uint32_t *dst,
+                cudaStream_t stream) {
+  const size_t n = (size_t)pitch * (h + 2 * kPad) * levels;
   if (n == 0) return;
-  k_pad<<<(uint32_t)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, stream>>>(src, w, h, levels, dst);
+  k_pad<<<(uint32_t)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, stream>>>(src, w, h, levels, pitch, dst);
 }
 
 void launch_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uint32_t nh, const uint4 *taps,

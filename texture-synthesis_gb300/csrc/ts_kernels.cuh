@@ -30,14 +30,12 @@ struct MapDesc {
   uint64_t off;      // texel offset of level 0
   int64_t mask_off;  // byte offset in the mask buffer, -1 = every texel valid
   uint64_t poff;     // texel offset of level 0's padded image (its (-kPad, -kPad) corner)
-  uint32_t pw, ph;   // padded pitch and height
+  uint32_t pw, ph;   // padded pitch (the session's common one) and height
 };
 
 struct GuideDesc {
   uint32_t w, h;
   uint64_t off;
-  uint64_t poff;
-  uint32_t pw, ph;
 };
 
 enum : uint32_t { kResAppend = 1u, kResMirrors = 2u };
@@ -54,8 +52,9 @@ enum : int { kDevOk = 0, kDevErrIndex = 1, kDevErrNoSample = 2, kDevErrLimit = 3
 
 struct SessionDev {
   const uint32_t *levels;
-  const uint32_t *plevels;  // padded copies of levels
-  const uint32_t *pguides;  // padded copies of guides
+  const uint32_t *plevels;  // padded copies of levels, row pitch ppitch
+  const uint32_t *pguides;  // padded guide of map f at maps[f].poff (when sizes agree)
+  uint32_t ppitch;
   const uint8_t *masks;
   const MapDesc *maps;
   uint32_t n_maps;
@@ -125,12 +124,14 @@ struct StepDev {
   int pad;
 };
 
-// A run of `nblocks` blocks, from block0 on, working on one (session, step).
+// A run of `nblocks` blocks, from block0 on, working on step `step` of
+// session slot `session`.
 struct Segment {
   uint32_t block0, nblocks, session, step;
 };
 
-// Parameters of one multi-session launch: segments sorted by block0.  The
+// Parameters of one multi-session launch: segments sorted by block0;
+// sessions[slot] and step_tabs[slot][step] describe a segment's work.  The
 // exhaustive k-NN also drains the walk's fallback lists of the steps in
 // `fb` with the blocks from pool_block0 on (whose count is known only on
 // the device).
@@ -138,7 +139,7 @@ struct MultiLaunch {
   const Segment *segs;
   uint32_t n_segs;
   const SessionDev *sessions;
-  const StepDev *steps;
+  const StepDev *const *step_tabs;
   const Segment *fb;
   uint32_t n_fb;
   uint32_t pool_block0;
@@ -194,8 +195,10 @@ void launch_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uin
 void launch_resize_h(const float *tmp, uint32_t w, uint32_t nh, uint8_t *dst, uint32_t nw, const uint4 *taps,
                      const float *wts, cudaStream_t stream);
 
-// Padded copy of `levels` images of w x h texels (see kPad).
-void launch_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, uint32_t *dst, cudaStream_t stream);
+// Padded copy of `levels` images of w x h texels (see kPad) with row pitch
+// `pitch` >= w + 2 kPad.
+void launch_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, uint32_t pitch, uint32_t *dst,
+                cudaStream_t stream);
 
 // Bytes of dynamic shared memory the resolve kernel needs per CTA.
 size_t resolve_smem_bytes(uint32_t k, uint32_t m, int guided);

@@ -96,14 +96,20 @@ std::string fmt_float(float v) {
   return buf;
 }
 
+// A device array.  alloc() uses cudaMalloc (freed with cudaFree, which
+// waits for the device); alloc_on(stream) takes stream-ordered pool memory,
+// freed with cudaFreeAsync on the stream set by free_on (at first the
+// allocating one), so that freeing never stalls the device.
 template <typename T>
 struct DevBuf {
   T *p = nullptr;
   size_t n = 0;
+  bool pooled = false;
+  cudaStream_t fs = nullptr;
   DevBuf() = default;
   DevBuf(const DevBuf &) = delete;
   DevBuf &operator=(const DevBuf &) = delete;
-  DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) {
+  DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n), pooled(o.pooled), fs(o.fs) {
     o.p = nullptr;
     o.n = 0;
   }
@@ -112,6 +118,8 @@ struct DevBuf {
       reset();
       p = o.p;
       n = o.n;
+      pooled = o.pooled;
+      fs = o.fs;
       o.p = nullptr;
       o.n = 0;
     }
@@ -119,16 +127,47 @@ struct DevBuf {
   }
   ~DevBuf() { reset(); }
   void reset() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (pooled)
+        cudaFreeAsync(p, fs);
+      else
+        cudaFree(p);
+    }
     p = nullptr;
     n = 0;
+    pooled = false;
   }
   cudaError_t alloc(size_t count) {
     reset();
     if (count == 0) count = 1;
     cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
-    if (e == cudaSuccess) n = count;
+    if (e == cudaSuccess)
+      n = count;
+    else
+      p = nullptr;
     return e;
+  }
+  cudaError_t alloc_on(size_t count, cudaStream_t st) {
+    reset();
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMallocAsync((void **)&p, count * sizeof(T), st);
+    if (e == cudaSuccess) {
+      n = count;
+      pooled = true;
+      fs = st;
+    } else {
+      p = nullptr;
+    }
+    return e;
+  }
+  void free_on(cudaStream_t st) { fs = st; }
+  size_t bytes() const { return p ? n * sizeof(T) : 0; }
+};
+
+struct StreamGuard {
+  cudaStream_t s = nullptr;
+  ~StreamGuard() {
+    if (s) cudaStreamDestroy(s);
   }
 };
 
@@ -162,15 +201,15 @@ struct DevTaps {
 void upload_taps(const Taps &t, DevTaps &d, cudaStream_t st) {
   std::vector<uint4> v(t.left.size());
   for (size_t i = 0; i < v.size(); ++i) v[i] = make_uint4(t.left[i], t.count[i], t.offset[i], 0);
-  CUDA_TRY(d.taps.alloc(v.size()));
-  CUDA_TRY(d.wts.alloc(t.weights.size()));
+  CUDA_TRY(d.taps.alloc_on(v.size(), st));
+  CUDA_TRY(d.wts.alloc_on(t.weights.size(), st));
   if (!v.empty()) CUDA_TRY(cudaMemcpyAsync(d.taps.p, v.data(), v.size() * sizeof(uint4), cudaMemcpyHostToDevice, st));
   if (!t.weights.empty())
     CUDA_TRY(cudaMemcpyAsync(d.wts.p, t.weights.data(), t.weights.size() * 4, cudaMemcpyHostToDevice, st));
 }
 
 // imageops::resize on the device: src (device u8, w x h) -> dst (device u8,
-// nw x nh).  Synchronises the stream before returning (the taps are freed).
+// nw x nh), enqueued on st (its temporaries are freed in stream order).
 void device_resize(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uint32_t nw, uint32_t nh, Filter f,
                    cudaStream_t st) {
   if (nw == 0 || nh == 0) return;
@@ -178,7 +217,7 @@ void device_resize(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uin
   upload_taps(axis_taps(f, h, nh), tv, st);
   upload_taps(axis_taps(f, w, nw), th, st);
   DevBuf<float> tmp;
-  CUDA_TRY(tmp.alloc((size_t)w * nh * 4));
+  CUDA_TRY(tmp.alloc_on((size_t)w * nh * 4, st));
   CUDA_TRY(cudaMemsetAsync(tmp.p, 0, (size_t)w * nh * 4 * sizeof(float), st));
   if (h > 0) launch_resize_v(src, w, h, tmp.p, nh, tv.taps.p, tv.wts.p, st);
   if (w > 0) {
@@ -187,7 +226,6 @@ void device_resize(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uin
     CUDA_TRY(cudaMemsetAsync(dst, 0, (size_t)nw * nh * 4, st));
   }
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(st));
 }
 
 // load_image (utils.rs:55-80): resize with CatmullRom when a size is given
@@ -195,15 +233,16 @@ void device_resize(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uin
 Image load_image(const Image &in, bool has_size, uint32_t w, uint32_t h, cudaStream_t st) {
   if (!has_size || (in.w == w && in.h == h)) return in;
   DevBuf<uint8_t> a, b;
-  CUDA_TRY(a.alloc(in.px.size()));
-  CUDA_TRY(b.alloc((size_t)w * h * 4));
+  CUDA_TRY(a.alloc_on(in.px.size(), st));
+  CUDA_TRY(b.alloc_on((size_t)w * h * 4, st));
   CUDA_TRY(cudaMemcpyAsync(a.p, in.px.data(), in.px.size(), cudaMemcpyHostToDevice, st));
   device_resize(a.p, in.w, in.h, b.p, w, h, kCatmullRom, st);
   Image out;
   out.w = w;
   out.h = h;
   out.px.resize((size_t)w * h * 4);
-  CUDA_TRY(cudaMemcpy(out.px.data(), b.p, out.px.size(), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpyAsync(out.px.data(), b.p, out.px.size(), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
   return out;
 }
 
@@ -220,7 +259,7 @@ void device_pyramid(const Image &img, uint32_t levels, uint32_t *dst, cudaStream
     const uint32_t p = 1u << i;
     const uint32_t sw = img.w / p, sh = img.h / p;
     DevBuf<uint8_t> small;
-    CUDA_TRY(small.alloc((size_t)sw * sh * 4));
+    CUDA_TRY(small.alloc_on((size_t)sw * sh * 4, st));
     if (sw == 0 || sh == 0) {
       // a zero-sized intermediate makes the crate return a zero image
       CUDA_TRY(cudaMemsetAsync(base + (size_t)l * sz * 4, 0, sz * 4, st));
@@ -256,6 +295,8 @@ struct ts_session {
   Params prm;
   uint32_t W = 0, H = 0;
   uint32_t n_ex = 0, n_maps = 0, n_levels = 1;
+  uint32_t ppitch = 0;  // row pitch of the padded levels
+  uint64_t dev_bytes = 0;  // device memory the session holds
   bool guided = false;
   std::vector<uint32_t> filtered;            // filtered map -> unfiltered example index
   std::vector<MapDesc> maps;
@@ -628,7 +669,9 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
   s->guided = b->has_target;
   try {
     CUDA_TRY(cudaSetDevice(p.device));
-    cudaStream_t st = 0;
+    StreamGuard sg;
+    CUDA_TRY(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
+    const cudaStream_t st = sg.s;
     CUDA_TRY(configure_kernels(p.k, (uint32_t)p.m));
     // inputs at their final sizes (Example::resolve, lib.rs:564-603)
     std::vector<Image> imgs(s->n_ex), guides(s->n_ex), masks(s->n_ex);
@@ -677,11 +720,7 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
       md.h = imgs[e].h;
       md.off = texels;
       md.mask_off = -1;
-      md.pw = md.w + 2 * kPad;
-      md.ph = md.h + 2 * kPad;
-      md.poff = ptexels;
       texels += (uint64_t)md.w * md.h * s->n_levels;
-      ptexels += (uint64_t)md.pw * md.ph * s->n_levels;
       if (b->examples[e].method == TS_SAMPLE_IMAGE) {
         bool any = false;
         for (size_t i = 0; i < (size_t)md.w * md.h && !any; ++i) any = masks[e].px[4 * i] != 0;
@@ -693,6 +732,17 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
       s->filtered.push_back(e);
     }
     s->n_maps = (uint32_t)s->maps.size();
+    // padded copies share one row pitch, the widest map's, so that a
+    // neighbour offset is one texel offset on every map
+    uint32_t pitch = 0;
+    for (const MapDesc &md : s->maps) pitch = std::max(pitch, md.w + 2 * kPad);
+    s->ppitch = pitch;
+    for (MapDesc &md : s->maps) {
+      md.pw = pitch;
+      md.ph = md.h + 2 * kPad;
+      md.poff = ptexels;
+      ptexels += (uint64_t)md.pw * md.ph * s->n_levels;
+    }
     CUDA_TRY(s->levels.alloc(texels));
     CUDA_TRY(s->masks.alloc(mask_bytes));
     for (uint32_t f = 0; f < s->n_maps; ++f) {
@@ -706,7 +756,7 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
     }
     CUDA_TRY(s->plevels.alloc(ptexels));
     for (uint32_t f = 0; f < s->n_maps; ++f)
-      launch_pad(s->levels.p + s->maps[f].off, s->maps[f].w, s->maps[f].h, s->n_levels,
+      launch_pad(s->levels.p + s->maps[f].off, s->maps[f].w, s->maps[f].h, s->n_levels, pitch,
                  s->plevels.p + s->maps[f].poff, st);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(s->d_maps.alloc(s->n_maps));
@@ -714,26 +764,27 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
     // guides: every example (unfiltered order) plus the target guide
     std::vector<GuideDesc> gd(std::max<uint32_t>(s->n_ex, 1));
     if (s->guided) {
-      uint64_t gtex = 0, pgtex = 0;
+      uint64_t gtex = 0;
       for (uint32_t e = 0; e < s->n_ex; ++e) {
         gd[e].w = guides[e].w;
         gd[e].h = guides[e].h;
         gd[e].off = gtex;
-        gd[e].pw = gd[e].w + 2 * kPad;
-        gd[e].ph = gd[e].h + 2 * kPad;
-        gd[e].poff = pgtex;
         gtex += (uint64_t)guides[e].w * guides[e].h * s->n_levels;
-        pgtex += (uint64_t)gd[e].pw * gd[e].ph * s->n_levels;
       }
       // the guide of map f is example f's guide (unfiltered index); the
       // padded fast path needs its size to equal the map's
       for (uint32_t f = 0; f < s->n_maps; ++f)
         if (f >= s->n_ex || gd[f].w != s->maps[f].w || gd[f].h != s->maps[f].h) s->guide_dims_differ = true;
       CUDA_TRY(s->guides.alloc(gtex));
-      CUDA_TRY(s->pguides.alloc(pgtex));
-      for (uint32_t e = 0; e < s->n_ex; ++e) {
+      for (uint32_t e = 0; e < s->n_ex; ++e)
         device_pyramid(guides[e], p.backtrack_stages, s->guides.p + gd[e].off, st);
-        launch_pad(s->guides.p + gd[e].off, gd[e].w, gd[e].h, s->n_levels, s->pguides.p + gd[e].poff, st);
+      // padded guides per map, at the map's own padded offsets (same size:
+      // only then are they read)
+      if (!s->guide_dims_differ) {
+        CUDA_TRY(s->pguides.alloc(ptexels));
+        for (uint32_t f = 0; f < s->n_maps; ++f)
+          launch_pad(s->guides.p + gd[f].off, gd[f].w, gd[f].h, s->n_levels, pitch, s->pguides.p + s->maps[f].poff,
+                     st);
       }
       CUDA_TRY(cudaGetLastError());
       Image tg = load_image(b->target, true, W, H, st);
@@ -742,7 +793,9 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
     }
     CUDA_TRY(s->d_gdesc.alloc(gd.size()));
     CUDA_TRY(cudaMemcpy(s->d_gdesc.p, gd.data(), gd.size() * sizeof(GuideDesc), cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaDeviceSynchronize());
+    CUDA_TRY(cudaStreamSynchronize(st));
+    s->dev_bytes = s->levels.bytes() + s->plevels.bytes() + s->guides.bytes() + s->pguides.bytes() +
+                   s->tguide.bytes() + s->masks.bytes() + s->d_maps.bytes() + s->d_gdesc.bytes();
     s->bottoms = std::move(imgs);
   } catch (const Failure &f) {
     b->err = f.msg;
@@ -879,6 +932,10 @@ struct RunCtx {
   std::vector<double> xdiv, ydiv, dxt, dy2t;
   size_t n_batches = 0;
   uint64_t overall_total = 0;
+  uint32_t max_batch_items = 1;
+  uint64_t rc_items = 1;
+  int32_t x_l = 0, y_b = 0;
+  uint64_t dev_bytes = 0;  // device memory run_alloc takes
   // device state
   DevBuf<uint32_t> d_color, d_occ, d_mir, d_res, d_items, d_ncnt, d_fbl, d_fbc;
   DevBuf<uint4> d_state;
@@ -1051,36 +1108,18 @@ void run_plan(ts_session *s, RunCtx &c) {
     max_stage_items = std::max<uint32_t>(max_stage_items, (uint32_t)P_eff);
     plan.push_back(std::move(sp));
   }
-  // ---- device state ----
+  // ---- host tables ----
   const uint32_t wpr = (W + 31) / 32;
   for (auto &sp : plan) c.n_batches += sp.batches.size();
-  CUDA_TRY(c.d_color.alloc(N));
-  CUDA_TRY(c.d_state.alloc(N));
-  CUDA_TRY(c.d_occ.alloc((size_t)wpr * H));
-  CUDA_TRY(c.d_mir.alloc((size_t)wpr * H));
-  CUDA_TRY(c.d_res.alloc(resolved.size()));
-  CUDA_TRY(c.d_rscore.alloc(resolved.size()));
-  CUDA_TRY(c.d_items.alloc(items.size()));
-  CUDA_TRY(c.d_lut.alloc(luts.size()));
-  CUDA_TRY(c.d_tab.alloc(tab.size()));
-  CUDA_TRY(c.d_nbuf.alloc((size_t)max_batch_items * std::max<uint32_t>(k, 1)));
-  CUDA_TRY(c.d_ncnt.alloc(max_batch_items));
-  CUDA_TRY(c.d_dist.alloc((size_t)max_batch_items * std::max<uint32_t>(k, 1)));
-  CUDA_TRY(c.d_mean.alloc(max_batch_items));
-  CUDA_TRY(c.d_fbl.alloc(max_batch_items));
-  CUDA_TRY(c.d_fbc.alloc(c.n_batches));
-  CUDA_TRY(c.d_result.alloc(max_batch_items));
-  CUDA_TRY(c.d_err.alloc(1));
-  CUDA_TRY(c.d_evals.alloc(1));
-  const uint64_t rc_items = std::max<uint64_t>(1, std::min<uint64_t>(max_stage_items, kRcandBudget / std::max(m, 1u)));
-  CUDA_TRY(c.d_rcand.alloc((size_t)std::max<uint64_t>(rc_items, max_batch_items) * m));
+  c.max_batch_items = max_batch_items;
+  c.rc_items = std::max<uint64_t>(1, std::min<uint64_t>(max_stage_items, kRcandBudget / std::max(m, 1u)));
+  c.x_l = x_l;
+  c.y_b = y_b;
   const int32_t xo = x_l + 2, yo = y_b + 2;
   c.xdiv.resize(W + 2 * (size_t)xo + 1);
   c.ydiv.resize(H + 2 * (size_t)yo + 1);
   for (size_t i = 0; i < c.xdiv.size(); ++i) c.xdiv[i] = (double)((int64_t)i - xo) / (double)W;
   for (size_t i = 0; i < c.ydiv.size(); ++i) c.ydiv[i] = (double)((int64_t)i - yo) / (double)H;
-  CUDA_TRY(c.d_xdiv.alloc(c.xdiv.size()));
-  CUDA_TRY(c.d_ydiv.alloc(c.ydiv.size()));
   // per-pixel tables of the normalised offsets the weights use: dx and
   // dy * dy for |offset| <= kDistTabRadius, the same IEEE operations as
   // get_distances_to_k_neighs (ms.rs:410-415)
@@ -1095,8 +1134,6 @@ void run_plan(ts_session *s, RunCtx &c) {
       const double dy = (double)((int64_t)y + o) / (double)H - (double)y / (double)H;
       c.dy2t[(size_t)y * (2 * R + 1) + o + R] = dy * dy;
     }
-  CUDA_TRY(c.d_dxt.alloc(c.dxt.size()));
-  CUDA_TRY(c.d_dy2t.alloc(c.dy2t.size()));
   // the tree is rebuilt from the resolved list, mirrors included (ms.rs:747-779)
   c.occ.assign((size_t)wpr * H, 0);
   c.mir.assign((size_t)wpr * H, 0);
@@ -1105,12 +1142,64 @@ void run_plan(ts_session *s, RunCtx &c) {
     c.occ[(size_t)(q / W) * wpr + (q % W) / 32] |= 1u << ((q % W) & 31);
     if (p.tiling) c.mir[(size_t)(q / W) * wpr + (q % W) / 32] |= 1u << ((q % W) & 31);
   }
+  // device memory the run will hold (run_alloc), for admission control
+  const size_t kk = std::max<uint32_t>(k, 1), mb = max_batch_items;
+  uint64_t steps_est = 0;
+  for (auto &sp : plan) steps_est += sp.batches.size() + 1;
+  c.dev_bytes = N * 4 + N * sizeof(uint4) + 2 * (uint64_t)wpr * H * 4 + resolved.size() * 8 + items.size() * 4 +
+                c.luts.size() * 4 + c.tab.size() * 4 + mb * kk * 12 + mb * (4 + 8 + 4 + sizeof(Result)) +
+                c.n_batches * 4 + std::max<uint64_t>(c.rc_items, mb) * m * 8 +
+                (c.xdiv.size() + c.ydiv.size() + c.dxt.size() + c.dy2t.size()) * 8 + steps_est * sizeof(StepDev);
+}
+
+// Device buffers of a run and the step descriptors that point into them.
+// With a pool stream, the buffers are stream-ordered pool memory (freed
+// without waiting for the device); otherwise plain cudaMalloc.
+void run_alloc(RunCtx &c, cudaStream_t pool) {
+  ts_session *s = c.s;
+  const Params &p = s->prm;
+  const uint32_t W = c.W, H = c.H;
+  const size_t N = c.N;
+  const uint32_t k = c.k, m = c.m;
+  const std::vector<StagePlan> &plan = c.plan;
+  const uint32_t max_batch_items = c.max_batch_items;
+  const uint64_t rc_items = c.rc_items;
+  const int32_t x_l = c.x_l, y_b = c.y_b;
+  const int32_t xo = x_l + 2, yo = y_b + 2;
+  const int32_t R = kDistTabRadius;
+  const uint32_t wpr = (W + 31) / 32;
+  auto A = [&](auto &buf, size_t n) { return pool ? buf.alloc_on(n, pool) : buf.alloc(n); };
+  CUDA_TRY(A(c.d_color, N));
+  CUDA_TRY(A(c.d_state, N));
+  CUDA_TRY(A(c.d_occ, (size_t)wpr * H));
+  CUDA_TRY(A(c.d_mir, (size_t)wpr * H));
+  CUDA_TRY(A(c.d_res, c.resolved.size()));
+  CUDA_TRY(A(c.d_rscore, c.resolved.size()));
+  CUDA_TRY(A(c.d_items, c.items.size()));
+  CUDA_TRY(A(c.d_lut, c.luts.size()));
+  CUDA_TRY(A(c.d_tab, c.tab.size()));
+  CUDA_TRY(A(c.d_nbuf, (size_t)max_batch_items * std::max<uint32_t>(k, 1)));
+  CUDA_TRY(A(c.d_ncnt, max_batch_items));
+  CUDA_TRY(A(c.d_dist, (size_t)max_batch_items * std::max<uint32_t>(k, 1)));
+  CUDA_TRY(A(c.d_mean, max_batch_items));
+  CUDA_TRY(A(c.d_fbl, max_batch_items));
+  CUDA_TRY(A(c.d_fbc, c.n_batches));
+  CUDA_TRY(A(c.d_result, max_batch_items));
+  CUDA_TRY(A(c.d_err, 1));
+  CUDA_TRY(A(c.d_evals, 1));
+  CUDA_TRY(A(c.d_rcand, (size_t)std::max<uint64_t>(rc_items, max_batch_items) * m));
+  CUDA_TRY(A(c.d_xdiv, c.xdiv.size()));
+  CUDA_TRY(A(c.d_ydiv, c.ydiv.size()));
+  CUDA_TRY(A(c.d_dxt, c.dxt.size()));
+  CUDA_TRY(A(c.d_dy2t, c.dy2t.size()));
+  const std::vector<int32_t> &tab = c.tab;
 
   SessionDev &sd = c.sd;
   sd = SessionDev{};
   sd.levels = s->levels.p;
   sd.plevels = s->plevels.p;
   sd.pguides = s->pguides.p;
+  sd.ppitch = s->ppitch;
   sd.guide_dims_differ = s->guide_dims_differ ? 1 : 0;
   sd.masks = s->masks.p;
   sd.maps = s->d_maps.p;
@@ -1348,13 +1437,6 @@ void run_finish(RunCtx &c) {
   g->stats.cost_evals = c.evals;
 }
 
-struct StreamGuard {
-  cudaStream_t s = nullptr;
-  ~StreamGuard() {
-    if (s) cudaStreamDestroy(s);
-  }
-};
-
 struct EventPair {
   cudaEvent_t a = nullptr, b = nullptr;
   ~EventPair() {
@@ -1390,6 +1472,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     CUDA_TRY(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
     const cudaStream_t st = sg.s;
     run_plan(s, c);
+    run_alloc(c, nullptr);
     EventPair ev;
     ev.create();
     CUDA_TRY(cudaEventRecord(ev.a, st));
@@ -1615,6 +1698,7 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
           try {
             ctx[j].reset(new RunCtx());
             run_plan(sessions[j], *ctx[j]);
+            run_alloc(*ctx[j], nullptr);
           } catch (const Failure &f) {
             fails[j] = f;
           } catch (const std::bad_alloc &) {
@@ -1687,14 +1771,14 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
           if (t >= c.steps.size()) continue;
           const Step &stp = c.steps[t];
           if (ph == kPhaseExhaustive && stp.batch && c.k > 0 && !stp.exhaustive) {
-            h_fb.push_back(Segment{0, 0, (uint32_t)j, (uint32_t)(step_base[j] + t)});
+            h_fb.push_back(Segment{0, 0, (uint32_t)j, (uint32_t)t});
             pl.n_fb += 1;
             pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
           }
           const uint32_t units = phase_units(stp, c, ph);
           const uint32_t nb = multi_blocks(ph, units, phase_cap(stp, ph));
           if (nb == 0) continue;
-          h_segs.push_back(Segment{pl.blocks, nb, (uint32_t)j, (uint32_t)(step_base[j] + t)});
+          h_segs.push_back(Segment{pl.blocks, nb, (uint32_t)j, (uint32_t)t});
           pl.blocks += nb;
           pl.n_segs += 1;
           pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
@@ -1711,6 +1795,8 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
     DevBuf<SessionDev> d_sess;
     DevBuf<StepDev> d_steps;
     DevBuf<Segment> d_segs, d_fb;
+    DevBuf<const StepDev *> d_tabs;
+    CUDA_TRY(d_tabs.alloc(n));
     CUDA_TRY(d_sess.alloc(n));
     CUDA_TRY(d_steps.alloc(n_steps));
     CUDA_TRY(d_segs.alloc(h_segs.size()));
@@ -1721,6 +1807,9 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
     for (current = 0; current < n; ++current) run_upload(*ctx[current], st);
     CUDA_TRY(cudaMemcpyAsync(d_sess.p, h_sess.data(), n * sizeof(SessionDev), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_steps.p, h_steps.data(), n_steps * sizeof(StepDev), cudaMemcpyHostToDevice, st));
+    std::vector<const StepDev *> h_tabs(n);
+    for (size_t j = 0; j < n; ++j) h_tabs[j] = d_steps.p + step_base[j];
+    CUDA_TRY(cudaMemcpyAsync(d_tabs.p, h_tabs.data(), n * sizeof(const StepDev *), cudaMemcpyHostToDevice, st));
     if (!h_segs.empty())
       CUDA_TRY(cudaMemcpyAsync(d_segs.p, h_segs.data(), h_segs.size() * sizeof(Segment), cudaMemcpyHostToDevice,
                                st));
@@ -1735,7 +1824,7 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
         ml.segs = d_segs.p + pl.seg0;
         ml.n_segs = pl.n_segs;
         ml.sessions = d_sess.p;
-        ml.steps = d_steps.p;
+        ml.step_tabs = d_tabs.p;
         ml.fb = d_fb.p + pl.fb0;
         ml.n_fb = pl.n_fb;
         ml.pool_block0 = pl.n_fb ? pl.pool_block0 : pl.blocks;
