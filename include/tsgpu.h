@@ -318,6 +318,49 @@ int ts_batch_resolve_team(ts_batch *b, uint32_t team_max_items, uint32_t full_ma
 int ts_batch_run(ts_batch *b, ts_generated **out);
 void ts_batch_stats_get(const ts_batch *b, ts_batch_stats *out);
 
+/* ---- Served form (no counterpart in the reference) ----------------------
+ * Continuous batching of requests.  A request is a built session, handed to
+ * ts_server_submit (which plans its schedule on the calling thread).  A
+ * driver thread admits queued requests into session slots while their
+ * device memory fits the budget (a request that does not fit waits; one
+ * that does not fit an empty server runs alone), then runs ticks: each tick
+ * issues one batch step of every admitted request as shared launches, so a
+ * request admitted while others run overlaps with them on the device from
+ * its first step.  Results are byte-identical to ts_session_run on the same
+ * session, alone or in any mix.  Device memory of finished requests is
+ * returned in stream order, without waiting for the device. */
+typedef struct ts_server ts_server;
+typedef struct ts_request_times {
+  double submit_ms, admit_ms, done_ms;  /* host clock, from the server's creation */
+} ts_request_times;
+typedef struct ts_server_stats {
+  uint64_t submitted, admitted, completed, failed;
+  uint64_t ticks, launches;
+  uint64_t peak_active;   /* most requests on the device at once */
+  uint64_t peak_bytes;    /* most budget charged at once */
+  uint64_t budget_bytes;
+  uint64_t output_pixels, cost_evals;
+} ts_server_stats;
+/* hbm_budget_bytes 0: half the device's free memory; max_active 0: 64
+ * session slots.  NULL if the device cannot be used. */
+ts_server *ts_server_new(int32_t device, uint64_t hbm_budget_bytes, uint32_t max_active);
+/* Waits for every submitted request, then stops; results not collected
+ * with ts_server_wait are freed. */
+void ts_server_free(ts_server *s);
+const char *ts_server_last_error(const ts_server *s);
+/* As ts_batch_resolve_team, over the items of a tick. */
+int ts_server_resolve_team(ts_server *s, uint32_t team_max_items, uint32_t full_max_items);
+/* Consumes the session (only ts_session_free and ts_session_last_error
+ * remain valid on it) and queues it; *ticket names the request. */
+int ts_server_submit(ts_server *s, ts_session *session, uint64_t *ticket);
+/* Blocks until the request is done; *out receives its result (free with
+ * ts_generated_free), times its host timestamps (may be NULL).  A ticket
+ * can be waited for once. */
+int ts_server_wait(ts_server *s, uint64_t ticket, ts_generated **out, ts_request_times *times);
+/* 1 when done, 0 while queued or running, -1 for an unknown ticket. */
+int ts_server_done(ts_server *s, uint64_t ticket);
+void ts_server_stats_get(ts_server *s, ts_server_stats *out);
+
 /* ---- GeneratedImage (lib.rs:378-455) ------------------------------------- */
 
 void ts_generated_dims(const ts_generated *g, uint32_t *width, uint32_t *height);

@@ -153,3 +153,14 @@ def test_empty_batch_is_refused(ts):
         assert lib.ts_batch_add(b, None) == 14  # TS_ERR_NULL
     finally:
         lib.ts_batch_free(b)
+
+
+def test_server_handles(ts):
+    lib = ts.lib()
+    lib.ts_server_free(None)
+    h = lib.ts_server_new(0, 0, 4)  # NULL without a usable device
+    if h:
+        assert lib.ts_server_done(h, 12345) == -1
+        lib.ts_server_free(h)
+    out = C.c_void_p()
+    assert lib.ts_server_wait(None, 1, C.byref(out), None) == 14  # TS_ERR_NULL

@@ -92,6 +92,16 @@ class _BatchStats(C.Structure):
                 ("phase_launches", C.c_uint64 * 9), ("phase_ms", C.c_double * 9)]
 
 
+class _RequestTimes(C.Structure):
+    _fields_ = [("submit_ms", C.c_double), ("admit_ms", C.c_double), ("done_ms", C.c_double)]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [(f, C.c_uint64) for f in ("submitted", "admitted", "completed", "failed", "ticks", "launches",
+                                          "peak_active", "peak_bytes", "budget_bytes", "output_pixels",
+                                          "cost_evals")]
+
+
 class _LaunchRecord(C.Structure):
     _fields_ = [("kind", C.c_int32), ("stage", C.c_int32), ("batch_items", C.c_uint32), ("ms", C.c_float)]
 
@@ -155,6 +165,14 @@ SIGNATURES = {
     "ts_batch_plan_threads": (C.c_int, [C.c_void_p, C.c_uint32]),
     "ts_batch_resolve_team": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
     "ts_batch_stats_get": (None, [C.c_void_p, C.POINTER(_BatchStats)]),
+    "ts_server_new": (C.c_void_p, [C.c_int32, C.c_uint64, C.c_uint32]),
+    "ts_server_free": (None, [C.c_void_p]),
+    "ts_server_last_error": (C.c_char_p, [C.c_void_p]),
+    "ts_server_resolve_team": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
+    "ts_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
+    "ts_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p), C.POINTER(_RequestTimes)]),
+    "ts_server_done": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "ts_server_stats_get": (None, [C.c_void_p, C.POINTER(_ServerStats)]),
 }
 
 
@@ -525,6 +543,61 @@ class Batch:
         d["phases"] = {name: {"launches": int(st.phase_launches[i]), "ms": float(st.phase_ms[i])}
                        for i, name in enumerate(BATCH_PHASES)}
         return d
+
+
+class Server:
+    """The served form: continuous batching of requests (built sessions).
+    submit() queues a session and returns a ticket; wait(ticket) returns
+    (GeneratedImage, times) with host timestamps in ms (submit, admit,
+    done).  Results equal Session.run on the same session."""
+
+    def __init__(self, device=0, hbm_budget=0, max_active=64, team=None):
+        self._h = lib().ts_server_new(device, int(hbm_budget), int(max_active))
+        if not self._h:
+            raise Error(10, "ts_server_new: the device cannot be used")
+        if team is not None:
+            lib().ts_server_resolve_team(self._h, team[0], team[1])
+
+    def close(self):
+        """Waits for every submitted request, then stops the server."""
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.ts_server_free(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _err(self, rc):
+        msg = lib().ts_server_last_error(self._h)
+        return Error(rc, msg.decode() if msg else "")
+
+    def submit(self, session):
+        ticket = C.c_uint64()
+        rc = lib().ts_server_submit(self._h, session._h, C.byref(ticket))
+        if rc:
+            raise self._err(rc)
+        return ticket.value
+
+    def done(self, ticket):
+        return lib().ts_server_done(self._h, ticket) == 1
+
+    def wait(self, ticket):
+        out = C.c_void_p()
+        t = _RequestTimes()
+        rc = lib().ts_server_wait(self._h, ticket, C.byref(out), C.byref(t))
+        if rc:
+            raise self._err(rc)
+        return GeneratedImage(out.value), {"submit_ms": t.submit_ms, "admit_ms": t.admit_ms, "done_ms": t.done_ms}
+
+    def stats(self):
+        st = _ServerStats()
+        lib().ts_server_stats_get(self._h, C.byref(st))
+        return {f: getattr(st, f) for f, _ in st._fields_}
 
 
 def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0, profile=False, team_max_batch=None,

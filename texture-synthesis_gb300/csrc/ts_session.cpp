@@ -19,6 +19,10 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <unordered_map>
 #include <memory>
 #include <string>
 #include <thread>
@@ -1901,6 +1905,495 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
     out[i] = ctx[i]->g.release();
   }
   return TS_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Served form: continuous batching.  Requests (built sessions) are planned
+// on the submitting thread and queued; a driver thread admits them into
+// session slots while the device-memory budget allows and then runs ticks:
+// one tick is one batch step of every admitted session, issued as the
+// multi-session launches of the batched form, so a request that arrives
+// while others run joins them at the next tick.  A completion thread reads
+// finished sessions back and releases their memory and slot.
+// ---------------------------------------------------------------------------
+namespace {
+
+double host_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct ServerReq {
+  uint64_t ticket = 0;
+  ts_session *s = nullptr;  // owned
+  std::unique_ptr<RunCtx> c;
+  DevBuf<StepDev> d_steps;
+  uint32_t slot = 0;
+  bool slotted = false;  // holds a slot and its budget charge
+  size_t cursor = 0;
+  uint64_t bytes = 0;  // admission charge: the run's buffers plus the session's pyramids
+  double t_submit = 0, t_admit = 0, t_done = 0;
+  int status = TS_OK;
+  std::string err;
+  ts_generated *result = nullptr;
+  bool done = false;
+  cudaEvent_t up_ev = nullptr, ev = nullptr;  // uploads done; last kernels done
+  ~ServerReq() {
+    if (up_ev) cudaEventDestroy(up_ev);
+    if (ev) cudaEventDestroy(ev);
+    delete result;
+    delete s;
+  }
+};
+
+constexpr uint32_t kServerRing = 4;  // ticks in flight
+
+}  // namespace
+
+struct ts_server {
+  int device = 0;
+  uint64_t budget = 0;
+  uint32_t max_active = 0;
+  uint32_t team_max_items = 8192, team_full_max_items = 1024;
+  double t0 = 0;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done, cv_complete;
+  std::deque<ServerReq *> pending;
+  std::unordered_map<uint64_t, ServerReq *> reqs;  // submitted, not yet collected
+  std::deque<ServerReq *> completing;              // steps done, waiting for read-back
+  std::vector<uint32_t> free_slots;
+  uint64_t used = 0;
+  uint64_t next_ticket = 1;
+  bool stop = false, stop_completer = false;
+  int fatal = TS_OK;
+  std::string err;
+  std::vector<ServerReq *> active;  // driver thread only
+  std::thread driver, completer;
+  cudaStream_t st = nullptr, ust = nullptr, cst = nullptr;  // compute, upload, completion
+  DevBuf<SessionDev> d_sess;
+  DevBuf<const StepDev *> d_tabs;
+  struct Ring {
+    Segment *h = nullptr;
+    DevBuf<Segment> d;
+    cudaEvent_t ev = nullptr;
+    bool used = false;
+  };
+  Ring ring[kServerRing];
+  uint32_t seg_cap = 0;
+  ts_server_stats stats{};
+};
+
+namespace {
+
+void server_fail(ts_server *S, ServerReq *r, const Failure &f) {
+  r->status = f.status;
+  r->err = f.msg;
+}
+
+// Device buffers, uploads and slot entries of an admitted request, on the
+// upload stream; the compute stream waits for them before its next tick.
+void server_admit(ts_server *S, ServerReq *r) {
+  RunCtx &c = *r->c;
+  run_alloc(c, S->ust);
+  run_upload(c, S->ust);
+  std::vector<StepDev> h(c.steps.size());
+  for (size_t t = 0; t < c.steps.size(); ++t) {
+    const Step &stp = c.steps[t];
+    StepDev &d = h[t];
+    d = StepDev{};
+    d.st = stp.st;
+    d.rc = stp.rc_st;
+    d.b = stp.bd;
+    d.level = stp.ls_level;
+    d.ls_n_res = stp.ls_n_res;
+    d.all_items = stp.exhaustive ? 1 : 0;
+  }
+  CUDA_TRY(r->d_steps.alloc_on(h.size(), S->ust));
+  CUDA_TRY(cudaMemcpyAsync(r->d_steps.p, h.data(), h.size() * sizeof(StepDev), cudaMemcpyHostToDevice, S->ust));
+  const StepDev *tab = r->d_steps.p;
+  CUDA_TRY(cudaMemcpyAsync(S->d_sess.p + r->slot, &c.sd, sizeof(SessionDev), cudaMemcpyHostToDevice, S->ust));
+  CUDA_TRY(cudaMemcpyAsync(S->d_tabs.p + r->slot, &tab, sizeof(tab), cudaMemcpyHostToDevice, S->ust));
+  CUDA_TRY(cudaEventCreateWithFlags(&r->up_ev, cudaEventDisableTiming));
+  CUDA_TRY(cudaEventCreateWithFlags(&r->ev, cudaEventDisableTiming));
+  CUDA_TRY(cudaEventRecord(r->up_ev, S->ust));
+  CUDA_TRY(cudaStreamWaitEvent(S->st, r->up_ev, 0));
+}
+
+void server_driver(ts_server *S) {
+  if (cudaSetDevice(S->device) != cudaSuccess) return;
+  std::vector<Segment> segs, fb;
+  std::vector<PlannedLaunch> launches;
+  size_t phase_smem[kPhases] = {};
+  uint32_t ri = 0;
+  for (;;) {
+    // ---- admission ----
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      if (S->active.empty()) {
+        S->cv_work.wait(lk, [&] { return S->stop || !S->pending.empty(); });
+        if (S->pending.empty()) break;  // stopping, nothing left
+      }
+      while (!S->pending.empty() && !S->free_slots.empty()) {
+        ServerReq *r = S->pending.front();
+        // within the budget, or alone on the device
+        if (!S->active.empty() && S->used + r->bytes > S->budget) break;
+        S->pending.pop_front();
+        r->slot = S->free_slots.back();
+        S->free_slots.pop_back();
+        r->slotted = true;
+        S->used += r->bytes;
+        S->stats.peak_bytes = std::max(S->stats.peak_bytes, S->used);
+        lk.unlock();
+        r->t_admit = host_ms() - S->t0;
+        bool ok = true;
+        try {
+          server_admit(S, r);
+        } catch (const Failure &f) {
+          server_fail(S, r, f);
+          ok = false;
+        }
+        lk.lock();
+        if (ok) {
+          S->active.push_back(r);
+          S->stats.admitted += 1;
+        } else {
+          S->completing.push_back(r);
+          S->cv_complete.notify_one();
+        }
+      }
+      S->stats.peak_active = std::max<uint64_t>(S->stats.peak_active, S->active.size());
+    }
+    if (S->active.empty()) continue;
+    // ---- one tick: the next step of every active session ----
+    try {
+      ts_server::Ring &R = S->ring[ri];
+      if (R.used) CUDA_TRY(cudaEventSynchronize(R.ev));  // the slot's previous tick is done
+      uint64_t step_items = 0;
+      bool all_team_full = true;
+      for (ServerReq *r : S->active) {
+        const Step &stp = r->c->steps[r->cursor];
+        if (stp.batch) {
+          step_items += stp.n;
+          all_team_full &= team_full_fits(r->c->k, r->c->m);
+        }
+      }
+      const int form = step_items > S->team_max_items                              ? kPhaseResolve
+                       : (step_items <= S->team_full_max_items && all_team_full) ? kPhaseTeamFull
+                                                                                 : kPhaseTeamPart;
+      segs.clear();
+      fb.clear();
+      launches.clear();
+      for (ServerReq *r : S->active) r->c->steps[r->cursor].resolve = form;
+      for (int ph = 0; ph < kPhases; ++ph) {
+        PlannedLaunch pl;
+        pl.phase = ph;
+        pl.seg0 = (uint32_t)segs.size();
+        pl.n_segs = pl.blocks = 0;
+        pl.smem = 0;
+        pl.fb0 = (uint32_t)fb.size();
+        for (ServerReq *r : S->active) {
+          const RunCtx &c = *r->c;
+          const Step &stp = c.steps[r->cursor];
+          if (ph == kPhaseExhaustive && stp.batch && c.k > 0 && !stp.exhaustive) {
+            fb.push_back(Segment{0, 0, r->slot, (uint32_t)r->cursor});
+            pl.n_fb += 1;
+            pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
+          }
+          const uint32_t nb = multi_blocks(ph, phase_units(stp, c, ph), phase_cap(stp, ph));
+          if (nb == 0) continue;
+          segs.push_back(Segment{pl.blocks, nb, r->slot, (uint32_t)r->cursor});
+          pl.blocks += nb;
+          pl.n_segs += 1;
+          pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
+        }
+        pl.pool_block0 = pl.blocks;
+        if (pl.n_fb) pl.blocks += kFallbackPool;
+        if (pl.n_segs || pl.n_fb) {
+          if (pl.smem > phase_smem[ph]) {
+            CUDA_TRY(set_multi_smem(ph, pl.smem));
+            phase_smem[ph] = pl.smem;
+          }
+          launches.push_back(pl);
+        }
+      }
+      const size_t nseg = segs.size() + fb.size();
+      if (nseg > S->seg_cap) throw Failure{TS_ERR_LIMIT, "segment table overflow"};
+      std::copy(segs.begin(), segs.end(), R.h);
+      std::copy(fb.begin(), fb.end(), R.h + segs.size());
+      if (nseg)
+        CUDA_TRY(cudaMemcpyAsync(R.d.p, R.h, nseg * sizeof(Segment), cudaMemcpyHostToDevice, S->st));
+      for (const PlannedLaunch &pl : launches) {
+        MultiLaunch ml;
+        ml.segs = R.d.p + pl.seg0;
+        ml.n_segs = pl.n_segs;
+        ml.sessions = S->d_sess.p;
+        ml.step_tabs = S->d_tabs.p;
+        ml.fb = R.d.p + segs.size() + pl.fb0;
+        ml.n_fb = pl.n_fb;
+        ml.pool_block0 = pl.n_fb ? pl.pool_block0 : pl.blocks;
+        launch_multi(pl.phase, ml, pl.blocks, pl.smem, S->st);
+      }
+      CUDA_TRY(cudaGetLastError());
+      CUDA_TRY(cudaEventRecord(R.ev, S->st));
+      R.used = true;
+      ri = (ri + 1) % kServerRing;
+      // advance; finished sessions go to the completion thread
+      std::vector<ServerReq *> still;
+      std::vector<ServerReq *> finished;
+      for (ServerReq *r : S->active) {
+        RunCtx &c = *r->c;
+        const Step &stp = c.steps[r->cursor];
+        if (stp.batch) {
+          ++c.batches;
+          c.resolves += stp.n;
+        }
+        if (++r->cursor == c.steps.size()) {
+          CUDA_TRY(cudaEventRecord(r->ev, S->st));
+          finished.push_back(r);
+        } else {
+          still.push_back(r);
+        }
+      }
+      S->active.swap(still);
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->stats.ticks += 1;
+        S->stats.launches += launches.size();
+        for (ServerReq *r : finished) S->completing.push_back(r);
+        if (!finished.empty()) S->cv_complete.notify_one();
+      }
+    } catch (const Failure &f) {
+      // the device is unusable for this server: fail everything in flight
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->fatal = f.status;
+      S->err = f.msg;
+      for (ServerReq *r : S->active) {
+        server_fail(S, r, f);
+        S->completing.push_back(r);
+      }
+      S->active.clear();
+      for (ServerReq *r : S->pending) {
+        server_fail(S, r, f);
+        S->completing.push_back(r);
+      }
+      S->pending.clear();
+      S->cv_complete.notify_one();
+    }
+  }
+}
+
+void server_completer(ts_server *S) {
+  if (cudaSetDevice(S->device) != cudaSuccess) return;
+  for (;;) {
+    ServerReq *r = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_complete.wait(lk, [&] { return S->stop_completer || !S->completing.empty(); });
+      if (S->completing.empty()) break;
+      r = S->completing.front();
+      S->completing.pop_front();
+    }
+    if (r->status == TS_OK) {
+      try {
+        CUDA_TRY(cudaEventSynchronize(r->ev));
+        run_readback(*r->c, S->cst);
+        CUDA_TRY(cudaStreamSynchronize(S->cst));
+        run_finish(*r->c);
+        r->result = r->c->g.release();
+      } catch (const Failure &f) {
+        server_fail(S, r, f);
+      }
+    }
+    const bool admitted = r->slotted;
+    if (r->ev) cudaEventSynchronize(r->ev);  // no kernel of the request is left
+    // the run's buffers are pool memory (freed in stream order, no device
+    // wait); the session's pyramids are freed with it
+    r->c.reset();
+    r->d_steps.reset();
+    delete r->s;
+    r->s = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      r->t_done = host_ms() - S->t0;
+      if (admitted) {
+        S->used -= r->bytes;
+        S->free_slots.push_back(r->slot);
+      }
+      if (r->result) {
+        S->stats.completed += 1;
+        S->stats.output_pixels += (uint64_t)r->result->W * r->result->H;
+        S->stats.cost_evals += r->result->stats.cost_evals;
+        r->result->stats.wall_ms = r->t_done - r->t_submit;
+        r->result->stats.kernel_launches = 0;
+      } else {
+        S->stats.failed += 1;
+      }
+      r->done = true;
+      S->cv_done.notify_all();
+      S->cv_work.notify_one();
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+ts_server *ts_server_new(int32_t device, uint64_t hbm_budget_bytes, uint32_t max_active) {
+  std::unique_ptr<ts_server> S(new (std::nothrow) ts_server());
+  if (!S) return nullptr;
+  S->device = device;
+  S->max_active = max_active ? max_active : 64;
+  try {
+    CUDA_TRY(cudaSetDevice(device));
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    S->budget = hbm_budget_bytes ? hbm_budget_bytes : (uint64_t)(free_b / 2);
+    CUDA_TRY(cudaStreamCreateWithFlags(&S->st, cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&S->ust, cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&S->cst, cudaStreamNonBlocking));
+    CUDA_TRY(S->d_sess.alloc(S->max_active));
+    CUDA_TRY(S->d_tabs.alloc(S->max_active));
+    S->seg_cap = S->max_active * (kPhases + 1);
+    for (auto &R : S->ring) {
+      CUDA_TRY(cudaMallocHost((void **)&R.h, S->seg_cap * sizeof(Segment)));
+      CUDA_TRY(R.d.alloc(S->seg_cap));
+      CUDA_TRY(cudaEventCreateWithFlags(&R.ev, cudaEventDisableTiming));
+    }
+  } catch (const Failure &) {
+    ts_server_free(S.release());
+    return nullptr;
+  }
+  for (uint32_t i = 0; i < S->max_active; ++i) S->free_slots.push_back(S->max_active - 1 - i);
+  S->t0 = host_ms();
+  S->driver = std::thread(server_driver, S.get());
+  S->completer = std::thread(server_completer, S.get());
+  return S.release();
+}
+
+void ts_server_free(ts_server *S) {
+  if (!S) return;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+    S->cv_work.notify_all();
+  }
+  if (S->driver.joinable()) S->driver.join();  // drains every submitted request first
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop_completer = true;
+    S->cv_complete.notify_all();
+  }
+  if (S->completer.joinable()) S->completer.join();
+  for (auto &kv : S->reqs) delete kv.second;
+  if (S->st) cudaStreamSynchronize(S->st);
+  for (auto &R : S->ring) {
+    if (R.h) cudaFreeHost(R.h);
+    if (R.ev) cudaEventDestroy(R.ev);
+    R.d.reset();
+  }
+  S->d_sess.reset();
+  S->d_tabs.reset();
+  if (S->st) cudaStreamDestroy(S->st);
+  if (S->ust) cudaStreamDestroy(S->ust);
+  if (S->cst) cudaStreamDestroy(S->cst);
+  delete S;
+}
+
+const char *ts_server_last_error(const ts_server *S) { return S ? S->err.c_str() : "null server"; }
+
+int ts_server_resolve_team(ts_server *S, uint32_t team_max_items, uint32_t full_max_items) {
+  if (!S) return TS_ERR_NULL;
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->team_max_items = team_max_items;
+  S->team_full_max_items = full_max_items;
+  return TS_OK;
+}
+
+int ts_server_submit(ts_server *S, ts_session *s, uint64_t *ticket) {
+  if (!S || !s || !ticket) return TS_ERR_NULL;
+  if (s->consumed) {
+    S->err = "session already consumed";
+    return TS_ERR_STATE;
+  }
+  if (s->prm.device != S->device) {
+    S->err = "session device differs from the server's";
+    return TS_ERR_STATE;
+  }
+  std::unique_ptr<ServerReq> r(new (std::nothrow) ServerReq());
+  if (!r) return TS_ERR_OUT_OF_MEMORY;
+  r->s = new (std::nothrow) ts_session();
+  if (!r->s) return TS_ERR_OUT_OF_MEMORY;
+  *r->s = std::move(*s);
+  s->consumed = true;
+  s->err = "session handed to a server";
+  r->t_submit = host_ms() - S->t0;
+  r->c.reset(new RunCtx());
+  try {
+    run_plan(r->s, *r->c);  // host schedule, on the caller's thread
+  } catch (const Failure &f) {
+    S->err = f.msg;
+    return f.status;
+  }
+  r->bytes = r->c->dev_bytes + r->s->dev_bytes;
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (S->fatal) {
+    S->err = "server stopped after a device error";
+    return S->fatal;
+  }
+  r->ticket = S->next_ticket++;
+  *ticket = r->ticket;
+  S->reqs[r->ticket] = r.get();
+  S->pending.push_back(r.release());
+  S->stats.submitted += 1;
+  S->cv_work.notify_one();
+  return TS_OK;
+}
+
+int ts_server_wait(ts_server *S, uint64_t ticket, ts_generated **out, ts_request_times *times) {
+  if (!S || !out) return TS_ERR_NULL;
+  *out = nullptr;
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto it = S->reqs.find(ticket);
+  if (it == S->reqs.end()) {
+    S->err = "unknown ticket";
+    return TS_ERR_STATE;
+  }
+  ServerReq *r = it->second;
+  S->cv_done.wait(lk, [&] { return r->done; });
+  S->reqs.erase(it);
+  lk.unlock();
+  if (times) {
+    times->submit_ms = r->t_submit;
+    times->admit_ms = r->t_admit;
+    times->done_ms = r->t_done;
+  }
+  const int status = r->status;
+  if (status == TS_OK) {
+    *out = r->result;
+    r->result = nullptr;
+  } else {
+    std::lock_guard<std::mutex> lk2(S->mu);
+    S->err = r->err;
+  }
+  delete r;
+  return status;
+}
+
+int ts_server_done(ts_server *S, uint64_t ticket) {
+  if (!S) return -1;
+  std::lock_guard<std::mutex> lk(S->mu);
+  auto it = S->reqs.find(ticket);
+  if (it == S->reqs.end()) return -1;
+  return it->second->done ? 1 : 0;
+}
+
+void ts_server_stats_get(ts_server *S, ts_server_stats *out) {
+  if (!S || !out) return;
+  std::lock_guard<std::mutex> lk(S->mu);
+  *out = S->stats;
+  out->budget_bytes = S->budget;
 }
 
 }  // extern "C"
