@@ -7,15 +7,24 @@ Session::run() over one session.
 
   value  output Mpx/s with the inputs already on the device when the timed
          region starts (sessions built beforehand); device time measured
-         with CUDA events on the launching stream inside run()
+         with CUDA events on the launching stream inside run(); L2 is
+         flushed (a 256 MB device write) between timed steps
   e2e    the same metric through the C ABI with host buffers: build (input
          upload, pyramids) + run + reading the image back, per step
   roofline  the resolve kernel (dominant) measured with per-launch CUDA
          events in a separate profiled pass
   cpu_baseline  the CPU oracle (a C port of the reference's algorithm) on
          the host cores, one full run of the same workload
+  batched  64 sessions of the batched mix (uneven sizes, k and m from
+         {8, 20, 50}, a quarter guided), one after another on the plain
+         path and together through the batched form: aggregate Mpx/s
+  served   a Poisson request stream from the batched mix (70%) and 512^2
+         inpainting requests (30%) through the served form and, for
+         comparison, through the plain path one request at a time:
+         p50/p99 latency from arrival to result and aggregate Mpx/s
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                [--workload remix|batched|served]
 """
 import argparse
 import importlib
@@ -50,31 +59,33 @@ class ClockSampler:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index=0):
+    def __init__(self, index=0, period_ms=50):
         self.index = index
+        self.period_ms = period_ms
         self.rows = []
-        self._stop = threading.Event()
-        self._t = None
-
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                for line in out.stdout.strip().splitlines():
-                    self.rows.append([c.strip() for c in line.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        self._p = None
 
     def __enter__(self):
-        self._t = threading.Thread(target=self._run, daemon=True)
-        self._t.start()
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                        "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
+                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.3)  # first sample before the timed region
+        except Exception:
+            self._p = None
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        self._t.join(timeout=10)
+        if self._p is None:
+            return
+        self._p.terminate()
+        try:
+            out, _ = self._p.communicate(timeout=10)
+        except Exception:
+            self._p.kill()
+            out, _ = self._p.communicate()
+        for line in (out or "").strip().splitlines():
+            self.rows.append([c.strip() for c in line.split(",")])
 
     def summary(self):
         sm = []
@@ -98,6 +109,131 @@ class ClockSampler:
 def workload():
     wl = importlib.import_module(PKG + ".workloads")
     return wl.config1()
+
+
+class L2Flush:
+    """Writes a 256 MB device buffer (L2 is 129 MB) between timed steps."""
+
+    def __init__(self):
+        self.buf = None
+        try:
+            import torch
+
+            if torch.cuda.is_available():
+                self.torch = torch
+                self.buf = torch.empty(64 << 20, dtype=torch.float32, device="cuda:0")
+        except Exception:
+            self.buf = None
+
+    def __call__(self):
+        if self.buf is not None:
+            self.buf.fill_(1.0)
+            self.torch.cuda.synchronize()
+
+
+def _pct(v, q):
+    import numpy as np
+
+    return float(np.percentile(np.asarray(v, dtype=np.float64), q))
+
+
+def measure_batched(ts, wl, n=64):
+    """Config 3: the plain path one session after another vs the batched
+    form, on the same 64 sessions (built before timing)."""
+    specs = wl.config3_sessions(n)
+    for s in specs[:2]:
+        ts.builder_from_spec(s).build().run()
+    px = sum(s["out_w"] * s["out_h"] for s in specs)
+    sess = [ts.builder_from_spec(s).build() for s in specs]
+    t0 = time.perf_counter()
+    gpu = 0.0
+    for s in sess:
+        gpu += s.run().stats()["gpu_ms"]
+    plain_wall = time.perf_counter() - t0
+    best = None
+    for _ in range(2):
+        b = ts.Batch()
+        for s in specs:
+            b.add(ts.builder_from_spec(s).build())
+        t1 = time.perf_counter()
+        b.run()
+        wall = time.perf_counter() - t1
+        st = b.stats()
+        if best is None or st["gpu_ms"] < best[0]["gpu_ms"]:
+            best = (st, wall)
+    st, wall = best
+    return {"workload": "batched_mix_64", "sessions": n, "output_mpx": px / 1e6,
+            "plain": {"mpx_s": px / (gpu / 1e3) / 1e6, "wall_mpx_s": px / plain_wall / 1e6, "gpu_ms": gpu},
+            "batched": {"mpx_s": px / (st["gpu_ms"] / 1e3) / 1e6, "wall_mpx_s": px / wall / 1e6,
+                        "gpu_ms": st["gpu_ms"], "steps": st["steps"], "launches": st["launches"],
+                        "plan_ms": st["plan_ms"]},
+            "cost_evals_per_s": st["cost_evals"] / (st["gpu_ms"] / 1e3)}
+
+
+def serve_stream(ts, reqs, served=True, max_active=64):
+    """A request stream [(arrival_s, spec)]: sessions are built at arrival on
+    a client thread; latency runs from the arrival to the result on the
+    host.  served=False: the plain path, one request at a time, FIFO."""
+    n = len(reqs)
+    lat = [0.0] * n
+    px = [0] * n
+    t_start = time.perf_counter() + 0.05
+    if served:
+        srv = ts.Server(max_active=max_active)
+        tickets = [None] * n
+        ready = [threading.Event() for _ in range(n)]
+        sub_py = [0.0] * n
+
+        def client():
+            for i, (t, spec) in enumerate(reqs):
+                d = t_start + t - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                s = ts.builder_from_spec(spec).build()
+                sub_py[i] = time.perf_counter()
+                tickets[i] = srv.submit(s)
+                ready[i].set()
+
+        th = threading.Thread(target=client)
+        th.start()
+        for i in range(n):
+            ready[i].wait()
+            g, times = srv.wait(tickets[i])
+            done = sub_py[i] + (times["done_ms"] - times["submit_ms"]) / 1e3
+            lat[i] = done - (t_start + reqs[i][0])
+            px[i] = g.width * g.height
+        th.join()
+        st = srv.stats()
+        srv.close()
+    else:
+        st = None
+        for i, (t, spec) in enumerate(reqs):
+            d = t_start + t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            g = ts.builder_from_spec(spec).build().run()
+            lat[i] = time.perf_counter() - (t_start + t)
+            px[i] = g.width * g.height
+    span = max(reqs[i][0] + lat[i] for i in range(n)) - reqs[0][0]
+    out = {"requests": n, "p50_ms": _pct(lat, 50) * 1e3, "p99_ms": _pct(lat, 99) * 1e3,
+           "mean_ms": sum(lat) / n * 1e3, "mpx_s": sum(px) / span / 1e6}
+    if st is not None:
+        out["peak_active"] = st["peak_active"]
+        out["ticks"] = st["ticks"]
+    return out
+
+
+def measure_served(ts, wl, lams=(50, 200), n=64):
+    """Config 4: the Poisson stream through the served form and through the
+    plain path, at each arrival rate."""
+    warm = wl.config4_requests(6, 1000.0, seed=99)
+    serve_stream(ts, warm, True)
+    rows = []
+    for lam in lams:
+        reqs = wl.config4_requests(n, float(lam))
+        rows.append({"lambda_req_s": lam, "served": serve_stream(ts, reqs, True),
+                     "plain": serve_stream(ts, reqs, False)})
+    return {"workload": "served_mix", "mix": "70% batched mix, 30% 512^2 inpainting", "rates": rows}
 
 
 def run_reference_arm(args):
@@ -133,11 +269,13 @@ def run_reference_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--once", action="store_true", help="build and run one session, print its stats (for profilers)")
+    ap.add_argument("--workload", default="remix", choices=["remix", "batched", "served"])
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched and served objects of the remix line")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -150,6 +288,14 @@ def main():
     ts = importlib.import_module(PKG)
     import numpy as np
 
+    wl = importlib.import_module(PKG + ".workloads")
+    if args.workload == "batched":
+        print(json.dumps({"metric": "aggregate output Mpx/s (batched form)", **measure_batched(ts, wl)}))
+        return
+    if args.workload == "served":
+        print(json.dumps({"metric": "request latency p50/p99 and aggregate Mpx/s (served form)",
+                          **measure_served(ts, wl, lams=(10, 25, 50, 100, 200), n=64)}))
+        return
     spec = workload()
     px = spec["out_w"] * spec["out_h"]
     if args.once:
@@ -160,16 +306,19 @@ def main():
     for _ in range(args.warmup):
         ts.builder_from_spec(spec).build().run()
     sessions = [ts.builder_from_spec(spec).build() for _ in range(args.steps)]
-    gpu_ms, evals, launches = [], [], []
+    flush = L2Flush()
+    gpu_ms, evals, launches, walls = [], [], [], []
     with ClockSampler(0) as clk:
-        t0 = time.perf_counter()
         for s in sessions:
+            flush()
+            t0 = time.perf_counter()
             g = s.run()
+            walls.append(time.perf_counter() - t0)
             st = g.stats()
             gpu_ms.append(st["gpu_ms"])
             evals.append(st["cost_evals"])
             launches.append(st["kernel_launches"])
-        wall = time.perf_counter() - t0
+    wall = sum(walls)
     ms = sum(gpu_ms) / len(gpu_ms)
     value = px * len(gpu_ms) / (sum(gpu_ms) / 1e3) / 1e6
     # --- end to end through the C ABI with host buffers
@@ -204,7 +353,9 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": {"workload": spec["name"], "out": [spec["out_w"], spec["out_h"]], "examples": 4, "k": 50,
-                   "m": 50, "batch_divisor": 8, "l2": "working set (examples 1.4 MB) L2-resident by design"},
+                   "m": 50, "batch_divisor": 8,
+                   "l2": "flushed between timed steps (256 MB device write)" if flush.buf is not None
+                   else "not flushed (no torch on this host)"},
         "cost_evals_per_s": sum(evals) / (sum(gpu_ms) / 1e3),
         "gpu_launches": int(sum(launches) / len(launches)),
         "wall_ms_per_step": wall / len(gpu_ms) * 1e3,
@@ -213,6 +364,9 @@ def main():
         "roofline": roofline,
         "cpu_baseline": None,
     }
+    if not args.no_extra:
+        line["batched"] = measure_batched(ts, wl)
+        line["served"] = measure_served(ts, wl)
     if not args.no_cpu_baseline and rank == 0:
         from oracle import oracle
 
