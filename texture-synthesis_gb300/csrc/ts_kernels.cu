@@ -156,10 +156,16 @@ __device__ __forceinline__ double neighbour_dist(const SessionDev &s, int px, in
   return __fma_rn(ddx, ddx, __dmul_rn(ddy, ddy));
 }
 
+__device__ __forceinline__ unsigned long long nb_key(uint32_t d2, int x, int y) {
+  return ((unsigned long long)d2 << 32) | ((uint32_t)(y + 32768) << 16) | (uint32_t)(x + 32768);
+}
+
 // ---------------------------------------------------------------------------
 // k-NN by walking the sorted offset table.  The table holds every lattice
 // offset with d2 <= its radius^2, in (d2, dy, dx) order, so the first k
 // occupied entries are exactly the k nearest points under the tie rule.
+// Items for which the table holds fewer than k points (sparse steps, image
+// edges) go to the exhaustive k-NN; sparse steps send every item there.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t vb,
                                               uint32_t vg) {
@@ -172,7 +178,7 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
     const double x2 = s.xdiv[px + s.xdiv_off], y2 = s.ydiv[py + s.ydiv_off];
     int32_t *nbo = b.nbuf + (size_t)local * s.k;
     uint32_t count = 0;
-    for (uint32_t c = 0; c < s.knn_tab_n; c += kWarp) {
+    for (uint32_t c = 0; c < (b.grid_first ? 0u : s.knn_tab_n); c += kWarp) {
       const uint32_t idx = c + lane;
       bool hit = false;
       int32_t off = 0;
@@ -214,7 +220,28 @@ struct ExhShared {
   uint32_t prefix;
   uint32_t rank;
   int overflow;
+  uint32_t flag, cnt;  // cell-grid search: a ring cell lies in the grid; keys below the bound
 };
+
+constexpr uint32_t kExhGridFrom = 4096;  // resolved points from which the cell grid is searched
+
+__device__ __forceinline__ void ring_cell(int r, int i, int &dx, int &dy) {
+  if (r == 0) {
+    dx = dy = 0;
+  } else if (i < 2 * r + 1) {
+    dx = -r + i;
+    dy = -r;
+  } else if (i < 4 * r + 2) {
+    dx = -r + (i - (2 * r + 1));
+    dy = r;
+  } else if (i < 6 * r + 1) {
+    dx = -r;
+    dy = -r + 1 + (i - (4 * r + 2));
+  } else {
+    dx = r;
+    dy = -r + 1 + (i - (6 * r + 1));
+  }
+}
 
 template <typename F>
 __device__ __forceinline__ void for_points(const SessionDev &s, uint32_t n_res, F &&f) {
@@ -233,10 +260,6 @@ __device__ __forceinline__ void for_points(const SessionDev &s, uint32_t n_res, 
         f(x, y - (int)s.H);
     }
   }
-}
-
-__device__ __forceinline__ unsigned long long nb_key(uint32_t d2, int x, int y) {
-  return ((unsigned long long)d2 << 32) | ((uint32_t)(y + 32768) << 16) | (uint32_t)(x + 32768);
 }
 
 __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
@@ -278,6 +301,88 @@ __device__ __forceinline__ void block_bitonic(unsigned long long *keys, uint32_t
   }
 }
 
+// The points of the cells in rings around the item's cell, as keys in
+// all[], until k keys lie below the rings' reach: after rings 0..r every
+// point with d2 < (r * kCell + 1)^2 has been seen (the cells beyond are that
+// far away in x or y), so the k smallest collected keys are then the k
+// nearest points under the tie rule; a ring wholly outside the grid means
+// every point has been seen.  Leaves the count in sh.total (above
+// kExhAllKeys: the buffer overflowed) and the OR of the d2 in sh.prefix.
+__device__ void grid_collect(const SessionDev &s, int px, int py, uint32_t k, ExhShared &sh,
+                             unsigned long long *all) {
+  if (threadIdx.x == 0) {
+    sh.total = 0;
+    sh.prefix = 0;
+    sh.flag = 0;
+    sh.cnt = 0;
+  }
+  __syncthreads();
+  const int qcx = (px - s.cox) / kCell, qcy = (py - s.coy) / kCell;
+  for (int r = 0;; ++r) {
+    const int ring = r == 0 ? 1 : 8 * r;
+    uint32_t dor = 0;
+    for (int i0 = 0; i0 < ring; i0 += (int)blockDim.x) {
+      const int i = i0 + (int)threadIdx.x;
+      if (i >= ring) continue;
+      int gx, gy;
+      ring_cell(r, i, gx, gy);
+      gx += qcx;
+      gy += qcy;
+      if ((unsigned)gx >= s.cgw || (unsigned)gy >= s.cgh) continue;
+      sh.flag = 1;
+      const uint32_t cnt = __ldg(&s.cells[(size_t)gy * s.cgw + gx]);
+      if (cnt == 0) continue;
+      const int x0 = s.cox + gx * kCell, y0 = s.coy + gy * kCell;
+      uint32_t found = 0;
+      for (int yy = 0; yy < kCell && found < cnt; ++yy) {
+        const int y = y0 + yy, dy = y - py;
+        uint32_t bits;
+        if ((unsigned)y < s.H && x0 >= 0 && x0 + kCell <= (int)s.W) {
+          const uint32_t wi = (uint32_t)x0 >> 5, sh5 = (uint32_t)x0 & 31u;
+          const uint32_t *row = s.occ + (size_t)y * s.wpr;
+          uint64_t wv = __ldg(&row[wi]);
+          if (sh5 + kCell > 32) wv |= (uint64_t)__ldg(&row[wi + 1]) << 32;
+          bits = (uint32_t)(wv >> sh5) & ((1u << kCell) - 1u);
+        } else {
+          bits = 0;
+          for (int xx = 0; xx < kCell; ++xx)
+            if (occupied(s, x0 + xx, y)) bits |= 1u << xx;
+        }
+        while (bits) {
+          const int bp = __ffs(bits) - 1;
+          bits &= bits - 1u;
+          const int x = x0 + bp, dx = x - px;
+          const uint32_t d2 = (uint32_t)(dx * dx + dy * dy);
+          dor |= d2;
+          const uint32_t slot = atomicAdd(&sh.total, 1u);
+          if (slot < (uint32_t)kExhAllKeys) all[slot] = nb_key(d2, x, y);
+          ++found;
+        }
+      }
+    }
+    if (dor) atomicOr(&sh.prefix, dor);
+    __syncthreads();
+    const uint32_t n = sh.total;
+    const bool any = sh.flag != 0;
+    if (n > (uint32_t)kExhAllKeys || !any) break;
+    const uint32_t lim = (uint32_t)(r * kCell + 1) * (uint32_t)(r * kCell + 1);
+    uint32_t c = 0;
+    for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) c += (uint32_t)(all[e] >> 32) < lim ? 1u : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(&sh.cnt, c);
+    __syncthreads();
+    const uint32_t lt = sh.cnt;
+    __syncthreads();  // every thread has read flag and cnt
+    if (lt >= k) break;
+    if (threadIdx.x == 0) {
+      sh.flag = 0;
+      sh.cnt = 0;
+    }
+    __syncthreads();
+  }
+}
+
 __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
                                     ExhShared &sh, unsigned long long *all, bool with_mean) {
   const uint32_t pixel = st.items[b.i0 + local];
@@ -297,9 +402,12 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
   }
   __syncthreads();
   // pass 1: every key into shared memory while it fits, and the count; one
-  // shared atomic per warp and round
+  // shared atomic per warp and round.  Many points: the cell grid's rings
+  // instead, which hold the k nearest.
   const int lane = threadIdx.x & 31;
-  for (uint32_t e0 = 0; e0 < n_res; e0 += blockDim.x) {
+  const bool grid = s.cells != nullptr && n_res > kExhGridFrom;
+  if (grid) grid_collect(s, px, py, k, sh, all);
+  for (uint32_t e0 = 0; e0 < (grid ? 0u : n_res); e0 += blockDim.x) {
     const uint32_t e = e0 + threadIdx.x;
     int xs[3], ys[3];
     uint32_t cnt = 0;
@@ -346,7 +454,12 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
     if (lane == 0 && dor) atomicOr(&sh.prefix, dor);  // prefix holds the OR of all d2 until the select
   }
   __syncthreads();
-  const uint32_t total = sh.total;
+  uint32_t total = sh.total;
+  if (!grid && total > (uint32_t)kExhAllKeys && s.cells != nullptr) {
+    __syncthreads();
+    grid_collect(s, px, py, k, sh, all);
+    total = sh.total;
+  }
   const unsigned long long *sorted;
   uint32_t n;
   if (total <= k || total <= (uint32_t)kExhAllKeys) {
@@ -1260,6 +1373,10 @@ __device__ __forceinline__ void resolve_team_body(const SessionDev &s, const Sta
 }
 
 // update + flush_resolved for a batch (ms.rs:296-377).
+__device__ __forceinline__ void add_cell_point(const SessionDev &s, int x, int y) {
+  atomicAdd(&s.cells[(size_t)((y - s.coy) / kCell) * s.cgw + (x - s.cox) / kCell], 1u);
+}
+
 __device__ __forceinline__ void commit_body(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t vb) {
   const uint32_t local = vb * blockDim.x + threadIdx.x;
   const uint32_t nb = b.i1 - b.i0;
@@ -1286,7 +1403,19 @@ __device__ __forceinline__ void commit_body(const SessionDev &s, const StageDev 
     s.rscore[pos] = r.score;
     const uint32_t x = p % s.W, y = p / s.W;
     atomicOr(&s.occ[(size_t)y * s.wpr + (x >> 5)], 1u << (x & 31));
-    if (s.tiling && (r.flags & kResMirrors)) atomicOr(&s.mir[(size_t)y * s.wpr + (x >> 5)], 1u << (x & 31));
+    add_cell_point(s, (int)x, (int)y);
+    if (s.tiling && (r.flags & kResMirrors)) {
+      atomicOr(&s.mir[(size_t)y * s.wpr + (x >> 5)], 1u << (x & 31));
+      // the tree's mirror copies (flush_resolved, ms.rs:306-328)
+      if ((int)x < s.x_l)
+        add_cell_point(s, (int)x + (int)s.W, (int)y);
+      else if ((int)x > s.x_r)
+        add_cell_point(s, (int)x - (int)s.W, (int)y);
+      if ((int)y < s.y_b)
+        add_cell_point(s, (int)x, (int)y + (int)s.H);
+      else if ((int)y > s.y_t)
+        add_cell_point(s, (int)x, (int)y - (int)s.H);
+    }
   }
 }
 

@@ -87,7 +87,14 @@ struct SessionDev {
   int tiling;
   int32_t x_l, x_r, y_b, y_t;
   uint32_t k, m;
+  // resolved points per kCell x kCell cell of the plane the tree spans
+  // (the image plus the tiling bands), origin (cox, coy): cells[gy * cgw + gx]
+  uint32_t *cells;
+  int32_t cox, coy;
+  uint32_t cgw, cgh;
 };
+
+constexpr int kCell = 8;
 
 struct StageDev {
   uint32_t level;
@@ -111,6 +118,7 @@ struct BatchDev {
   double *dist;          // [k][batch] squared normalised distances
   double *mean;          // [batch] mean of the 4x-duplicated distance list
   Result *res;           // [batch]
+  int grid_first;        // sparse step: search the cell grid without walking the offset table first
 };
 
 // One batch step of one session as the multi-session kernels read it.

@@ -817,6 +817,7 @@ namespace {
 struct BatchPlan {
   uint32_t i0, i1, n_res, append_from;
   bool exhaustive;
+  bool grid_first;
 };
 
 struct StagePlan {
@@ -929,7 +930,9 @@ struct RunCtx {
   std::vector<StagePlan> plan;
   std::vector<Step> steps;
   // host data uploaded at the start of the run
-  std::vector<uint32_t> color, resolved, items, occ, mir;
+  std::vector<uint32_t> color, resolved, items, occ, mir, cells;
+  int32_t cox = 0, coy = 0;
+  uint32_t cgw = 0, cgh = 0;
   std::vector<uint4> state;
   std::vector<float> luts;
   std::vector<int32_t> tab;
@@ -941,7 +944,7 @@ struct RunCtx {
   int32_t x_l = 0, y_b = 0;
   uint64_t dev_bytes = 0;  // device memory run_alloc takes
   // device state
-  DevBuf<uint32_t> d_color, d_occ, d_mir, d_res, d_items, d_ncnt, d_fbl, d_fbc;
+  DevBuf<uint32_t> d_color, d_occ, d_mir, d_res, d_items, d_ncnt, d_fbl, d_fbc, d_cells;
   DevBuf<uint4> d_state;
   DevBuf<float> d_rscore, d_lut;
   DevBuf<double> d_xdiv, d_ydiv, d_dist, d_dxt, d_dy2t, d_mean;
@@ -1101,6 +1104,9 @@ void run_plan(ts_session *s, RunCtx &c) {
       bp.append_from = k == 0 ? bp.i0 : std::max<uint32_t>(bp.i0, (uint32_t)std::min(redo, (size_t)bp.i1));
       // exhaustive k-NN when the table walk is unlikely to find k points
       bp.exhaustive = k > 0 && (R <= 4096 && (double)R * tab.size() < 2.0 * k * (double)N);
+      // fewer than k points expected within the offset table: straight to
+      // the cell grid
+      bp.grid_first = k > 0 && !bp.exhaustive && (double)R * tab.size() < (double)k * (double)N;
       const size_t appended = bp.i1 - bp.append_from;
       for (size_t t = bp.append_from; t < bp.i1; ++t) resolved.push_back(items[sp.items_off + t]);
       R += appended;
@@ -1146,6 +1152,27 @@ void run_plan(ts_session *s, RunCtx &c) {
     c.occ[(size_t)(q / W) * wpr + (q % W) / 32] |= 1u << ((q % W) & 31);
     if (p.tiling) c.mir[(size_t)(q / W) * wpr + (q % W) / 32] |= 1u << ((q % W) & 31);
   }
+  // resolved points per cell of the plane the tree spans (the image and,
+  // when tiling, its mirror bands)
+  c.cox = p.tiling ? -x_l : 0;
+  c.coy = p.tiling ? -y_b : 0;
+  c.cgw = (W + (p.tiling ? 2 * (uint32_t)x_l : 0) + kCell - 1) / kCell;
+  c.cgh = (H + (p.tiling ? 2 * (uint32_t)y_b : 0) + kCell - 1) / kCell;
+  c.cells.assign((size_t)c.cgw * c.cgh, 0);
+  auto add_cell = [&](int x, int y) { c.cells[(size_t)((y - c.coy) / kCell) * c.cgw + (x - c.cox) / kCell] += 1; };
+  for (size_t i = 0; i < locked; ++i) {
+    const int x = (int)(resolved[i] % W), y = (int)(resolved[i] / W);
+    add_cell(x, y);
+    if (!p.tiling || !((c.mir[(size_t)y * wpr + x / 32] >> (x & 31)) & 1u)) continue;
+    if (x < x_l)
+      add_cell(x + (int)W, y);
+    else if (x > (int)W - x_l)
+      add_cell(x - (int)W, y);
+    if (y < y_b)
+      add_cell(x, y + (int)H);
+    else if (y > (int)H - y_b)
+      add_cell(x, y - (int)H);
+  }
   // device memory the run will hold (run_alloc), for admission control
   const size_t kk = std::max<uint32_t>(k, 1), mb = max_batch_items;
   uint64_t steps_est = 0;
@@ -1153,7 +1180,8 @@ void run_plan(ts_session *s, RunCtx &c) {
   c.dev_bytes = N * 4 + N * sizeof(uint4) + 2 * (uint64_t)wpr * H * 4 + resolved.size() * 8 + items.size() * 4 +
                 c.luts.size() * 4 + c.tab.size() * 4 + mb * kk * 12 + mb * (4 + 8 + 4 + sizeof(Result)) +
                 c.n_batches * 4 + std::max<uint64_t>(c.rc_items, mb) * m * 8 +
-                (c.xdiv.size() + c.ydiv.size() + c.dxt.size() + c.dy2t.size()) * 8 + steps_est * sizeof(StepDev);
+                (c.xdiv.size() + c.ydiv.size() + c.dxt.size() + c.dy2t.size()) * 8 + steps_est * sizeof(StepDev) +
+                c.cells.size() * 4;
 }
 
 // Device buffers of a run and the step descriptors that point into them.
@@ -1196,6 +1224,7 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   CUDA_TRY(A(c.d_ydiv, c.ydiv.size()));
   CUDA_TRY(A(c.d_dxt, c.dxt.size()));
   CUDA_TRY(A(c.d_dy2t, c.dy2t.size()));
+  CUDA_TRY(A(c.d_cells, c.cells.size()));
   const std::vector<int32_t> &tab = c.tab;
 
   SessionDev &sd = c.sd;
@@ -1241,6 +1270,11 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   sd.y_t = (int32_t)H - y_b;
   sd.k = k;
   sd.m = m;
+  sd.cells = c.d_cells.p;
+  sd.cox = c.cox;
+  sd.coy = c.coy;
+  sd.cgw = c.cgw;
+  sd.cgh = c.cgh;
 
   // ---- the steps ----
   size_t fb_index = 0;
@@ -1299,6 +1333,7 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
         bd.res = c.d_result.p;
         stp.n = bp.i1 - bp.i0;
         stp.exhaustive = bp.exhaustive;
+        bd.grid_first = bp.grid_first ? 1 : 0;
         if (stp.n <= p.team_max_batch)
           stp.resolve = (stp.n <= p.team_full_max_batch && team_full_fits(k, m)) ? kPhaseTeamFull : kPhaseTeamPart;
         else
@@ -1328,6 +1363,7 @@ void run_upload(RunCtx &c, cudaStream_t st) {
   CUDA_TRY(cudaMemcpyAsync(c.d_ydiv.p, c.ydiv.data(), c.ydiv.size() * 8, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(c.d_dxt.p, c.dxt.data(), c.dxt.size() * 8, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(c.d_dy2t.p, c.dy2t.data(), c.dy2t.size() * 8, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(c.d_cells.p, c.cells.data(), c.cells.size() * 4, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemsetAsync(c.d_fbc.p, 0, c.n_batches * 4, st));
   CUDA_TRY(cudaMemsetAsync(c.d_err.p, 0, sizeof(int), st));
   CUDA_TRY(cudaMemsetAsync(c.d_evals.p, 0, sizeof(unsigned long long), st));
