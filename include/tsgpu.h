@@ -390,6 +390,43 @@ uint64_t ts_generated_launch_count(const ts_generated *g);
 int ts_generated_launches(const ts_generated *g, ts_launch_record *out);
 void ts_generated_free(ts_generated *g);
 
+/* Debug maps (GeneratedImage::save_debug, lib.rs:404-419; ms.rs:604-653),
+ * computed on the device: width*height*4 bytes each.  Patch-id and map-id
+ * colours of every pixel (channels drawn from Pcg32 streams seeded by the
+ * id), and the uncertainty map: (s, 255 - s, 0, 255) with
+ * s = (min(score, 1) * 255) as u8 at every resolved pixel, 0 elsewhere. */
+int ts_generated_debug_maps(const ts_generated *g, uint8_t *patch_id_rgba, uint8_t *map_id_rgba,
+                            uint8_t *uncertainty_rgba, int32_t device);
+
+/* ---- CoordinateTransform (lib.rs:162-325) -------------------------------- */
+typedef struct ts_transform ts_transform;
+/* A decoded RGBA8 image (row-major, 4 bytes per pixel). */
+typedef struct ts_image_desc {
+  const uint8_t *rgba;
+  uint32_t width, height;
+} ts_image_desc;
+/* GeneratedImage::get_coordinate_transform: the source (x, y, map) of every
+ * output pixel and the loaded size of every example. */
+ts_transform *ts_generated_coord_transform(const ts_generated *g);
+void ts_transform_free(ts_transform *t);
+void ts_transform_dims(const ts_transform *t, uint32_t *width, uint32_t *height, uint32_t *n_maps);
+int ts_transform_map_dims(const ts_transform *t, uint32_t index, uint32_t *width, uint32_t *height);
+/* CoordinateTransform::write: u32 little-endian words {0x12340001, width,
+ * height, n_maps}, n_maps (w, h) pairs, then width*height (x, y, map)
+ * triples.  out == NULL: *written receives the size only; TS_ERR_LIMIT if
+ * capacity is short. */
+int ts_transform_write(const ts_transform *t, uint8_t *out, size_t capacity, size_t *written);
+/* CoordinateTransform::read of that format (version 1); malformed or short
+ * data gives TS_ERR_INVALID_RANGE. */
+int ts_transform_read(const uint8_t *data, size_t len, ts_transform **out);
+/* CoordinateTransform::apply on the device: source i is resized (Catmull-Rom,
+ * as load_image) to original map i's size, then every output pixel takes
+ * texel (x, y) of source `map`.  Sources beyond n_maps are ignored, fewer
+ * give TS_ERR_MAPS_COUNT_MISMATCH; an entry outside its map (the reference
+ * panics) gives TS_ERR_INDEX.  out_rgba: width*height*4 bytes. */
+int ts_transform_apply(const ts_transform *t, const ts_image_desc *sources, uint32_t n_sources, uint8_t *out_rgba,
+                       int32_t device);
+
 #ifdef __cplusplus
 }
 #endif

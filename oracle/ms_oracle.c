@@ -1308,3 +1308,48 @@ size_t tso_knn(uint32_t W, uint32_t H, int tiling, const uint8_t *occ, const uin
   free(nb);
   return n;
 }
+
+
+/* ---- debug maps (ms.rs:604-653) ------------------------------------------
+ * Colour of an id: Pcg32::seed_from_u64(seed).gen_range(0..255) for u8
+ * (rand 0.8.5 UniformInt<u8>::sample_single: zone u32::MAX - (u32::MAX -
+ * 255 + 1) % 255, draw (v * 255) >> 32 of a u32 v). */
+uint8_t tso_id_colour(uint64_t seed) {
+  pcg32 r = pcg_seed_from_u64(seed);
+  const uint32_t range = 255u;
+  const uint32_t zone = 0xffffffffu - (uint32_t)((0x100000000ull - range) % range);
+  for (;;) {
+    uint64_t m = (uint64_t)pcg_next_u32(&r) * range;
+    if ((uint32_t)m <= zone) return (uint8_t)(m >> 32);
+  }
+}
+
+/* get_id_maps and get_uncertainty_map: RGBA8 per pixel; ids holds (patch,
+ * map) per pixel, (flat, score) the resolved list. */
+void tso_debug_maps(const uint32_t *ids, size_t n, const uint32_t *flat, const float *score, size_t n_res,
+                    uint8_t *patch, uint8_t *map, uint8_t *unc) {
+  for (size_t i = 0; i < n; i++) {
+    uint32_t p = ids[2 * i], m = ids[2 * i + 1];
+    patch[4 * i] = tso_id_colour(p);
+    patch[4 * i + 1] = tso_id_colour((uint32_t)(p * 5u + 21u));
+    patch[4 * i + 2] = tso_id_colour((uint32_t)(p / 4u + 12u));
+    patch[4 * i + 3] = 255;
+    map[4 * i] = tso_id_colour((uint64_t)m * 200u);
+    map[4 * i + 1] = tso_id_colour((uint32_t)(m * 5u + 341u));
+    map[4 * i + 2] = tso_id_colour((uint32_t)(m * 1200u - 35412u));
+    map[4 * i + 3] = 255;
+    unc[4 * i] = unc[4 * i + 1] = unc[4 * i + 2] = unc[4 * i + 3] = 0;
+  }
+  for (size_t i = 0; i < n_res; i++) {
+    float s = score[i];
+    float mn = (s != s) ? 1.0f : (s < 1.0f ? s : 1.0f); /* f32::min ignores NaN */
+    float v = mn * 255.0f;
+    uint32_t ns = v >= 255.0f ? 255u : (v > 0.0f ? (uint32_t)v : 0u); /* `as u8` truncates, saturates */
+    size_t f = flat[i];
+    if (f >= n) continue;
+    unc[4 * f] = (uint8_t)ns;
+    unc[4 * f + 1] = (uint8_t)(255u - ns);
+    unc[4 * f + 2] = 0;
+    unc[4 * f + 3] = 255;
+  }
+}

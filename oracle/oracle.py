@@ -75,6 +75,11 @@ def lib():
         L.tso_pyramid.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p]
         L.tso_pcg_seed.argtypes = [C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.tso_pcg_stream.argtypes = [C.c_uint64, C.c_uint32, C.c_void_p]
+        L.tso_id_colour.restype = C.c_uint8
+        L.tso_id_colour.argtypes = [C.c_uint64]
+        L.tso_debug_maps.restype = None
+        L.tso_debug_maps.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p,
+                                     C.c_void_p, C.c_void_p]
         L.tso_gen_range_u32.restype = C.c_uint32
         L.tso_gen_range_u32.argtypes = [C.c_uint64, C.c_uint32]
         L.tso_gen_range_u64.restype = C.c_uint64
@@ -189,3 +194,20 @@ def knn(W, H, tiling, occ, mir, px, py, k):
     out = np.zeros((max(k, 1), 2), np.int32)
     n = lib().tso_knn(W, H, int(tiling), _ptr(occ), _ptr(mir), px, py, k, _ptr(out))
     return out[:n].copy()
+
+
+def debug_maps(ids, flat, score):
+    """get_id_maps and get_uncertainty_map (ms.rs:604-653) on the CPU: ids is
+    H x W x 2 (patch, map), (flat, score) the resolved list."""
+    ids = np.ascontiguousarray(ids, np.uint32)
+    h, w = ids.shape[:2]
+    flat = np.ascontiguousarray(flat, np.uint32)
+    score = np.ascontiguousarray(score, np.float32)
+    outs = [np.empty((h, w, 4), np.uint8) for _ in range(3)]
+    lib().tso_debug_maps(ids.ctypes.data, h * w, flat.ctypes.data, score.ctypes.data, len(flat),
+                         outs[0].ctypes.data, outs[1].ctypes.data, outs[2].ctypes.data)
+    return tuple(outs)
+
+
+def id_colour(seed):
+    return int(lib().tso_id_colour(seed))

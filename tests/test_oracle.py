@@ -211,3 +211,36 @@ def test_errors(oracle, wl):
     spec["examples"][0]["mask"] = np.zeros((8, 8, 4), np.uint8)
     with pytest.raises(RuntimeError):
         oracle.run(spec)
+
+
+def id_colour_restated(seed):
+    """rand 0.8.5 UniformInt<u8>::sample_single(0, 255): zone for 8- and
+    16-bit types is u32::MAX - (u32::MAX - range + 1) % range."""
+    g = Pcg(seed)
+    rng = 255
+    zone = 0xFFFFFFFF - ((0x100000000 - rng) % rng)
+    while True:
+        m = g.u32() * rng
+        if (m & 0xFFFFFFFF) <= zone:
+            return m >> 32
+
+
+def test_id_colour_matches_restatement(oracle):
+    for seed in list(range(40)) + [21, 341, 200 * 7, (7 * 1200 - 35412) & 0xFFFFFFFF, 2 ** 32 - 1, 2 ** 40 + 3]:
+        assert oracle.id_colour(seed) == id_colour_restated(seed), seed
+
+
+def test_debug_maps_oracle_properties(oracle):
+    ids = np.zeros((3, 4, 2), np.uint32)
+    ids[..., 0] = np.arange(12).reshape(3, 4)
+    ids[..., 1] = 2
+    flat = np.array([0, 5, 11], np.uint32)
+    score = np.array([0.25, float("nan"), 3.0], np.float32)
+    patch, mapc, unc = oracle.debug_maps(ids, flat, score)
+    assert (patch[..., 3] == 255).all() and (mapc[..., 3] == 255).all()
+    assert patch[0, 1, 0] == id_colour_restated(1) and patch[0, 1, 1] == id_colour_restated(26)
+    assert mapc[0, 0, 2] == id_colour_restated((2 * 1200 - 35412) & 0xFFFFFFFF)
+    assert tuple(unc[0, 0]) == (63, 192, 0, 255)    # (0.25 * 255) as u8 = 63
+    assert tuple(unc[1, 1]) == (255, 0, 0, 255)     # NaN.min(1.0) = 1.0
+    assert tuple(unc[2, 3]) == (255, 0, 0, 255)
+    assert tuple(unc[0, 2]) == (0, 0, 0, 0)         # not resolved

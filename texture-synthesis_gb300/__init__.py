@@ -92,6 +92,10 @@ class _BatchStats(C.Structure):
                 ("phase_launches", C.c_uint64 * 9), ("phase_ms", C.c_double * 9)]
 
 
+class _ImageDesc(C.Structure):
+    _fields_ = [("rgba", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
 class _RequestTimes(C.Structure):
     _fields_ = [("submit_ms", C.c_double), ("admit_ms", C.c_double), ("done_ms", C.c_double)]
 
@@ -165,6 +169,14 @@ SIGNATURES = {
     "ts_batch_plan_threads": (C.c_int, [C.c_void_p, C.c_uint32]),
     "ts_batch_resolve_team": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
     "ts_batch_stats_get": (None, [C.c_void_p, C.POINTER(_BatchStats)]),
+    "ts_generated_debug_maps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]),
+    "ts_generated_coord_transform": (C.c_void_p, [C.c_void_p]),
+    "ts_transform_free": (None, [C.c_void_p]),
+    "ts_transform_dims": (None, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "ts_transform_map_dims": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "ts_transform_write": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "ts_transform_read": (C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(C.c_void_p)]),
+    "ts_transform_apply": (C.c_int, [C.c_void_p, C.POINTER(_ImageDesc), C.c_uint32, C.c_void_p, C.c_int32]),
     "ts_server_new": (C.c_void_p, [C.c_int32, C.c_uint64, C.c_uint32]),
     "ts_server_free": (None, [C.c_void_p]),
     "ts_server_last_error": (C.c_char_p, [C.c_void_p]),
@@ -483,6 +495,20 @@ class GeneratedImage:
         lib().ts_generated_stats(self._h, C.byref(st))
         return st.as_dict()
 
+    def debug_maps(self, device=0):
+        """save_debug's maps (lib.rs:404-419), computed on the device:
+        (patch_id, map_id, uncertainty), each H x W x 4 uint8."""
+        outs = [np.empty((self.height, self.width, 4), np.uint8) for _ in range(3)]
+        rc = lib().ts_generated_debug_maps(self._h, outs[0].ctypes.data, outs[1].ctypes.data,
+                                           outs[2].ctypes.data, device)
+        if rc:
+            raise Error(rc, "ts_generated_debug_maps")
+        return tuple(outs)
+
+    def coordinate_transform(self):
+        """get_coordinate_transform (lib.rs:441-443)."""
+        return CoordinateTransform(lib().ts_generated_coord_transform(self._h))
+
     def launches(self):
         """Per-launch timings of a profiled run: dicts of kernel, stage,
         batch_items, ms."""
@@ -598,6 +624,65 @@ class Server:
         st = _ServerStats()
         lib().ts_server_stats_get(self._h, C.byref(st))
         return {f: getattr(st, f) for f, _ in st._fields_}
+
+
+class CoordinateTransform:
+    """CoordinateTransform (lib.rs:162-325): the source coordinate of every
+    output pixel, written and read in the reference's binary format and
+    applied to new sources on the device."""
+
+    def __init__(self, handle):
+        if not handle:
+            raise Error(13, "coordinate transform")
+        self._h = handle
+        w, h, n = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        lib().ts_transform_dims(self._h, C.byref(w), C.byref(h), C.byref(n))
+        self.width, self.height, self.n_maps = w.value, h.value, n.value
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.ts_transform_free(self._h)
+            self._h = None
+
+    def original_maps(self):
+        out = []
+        for i in range(self.n_maps):
+            w, h = C.c_uint32(), C.c_uint32()
+            lib().ts_transform_map_dims(self._h, i, C.byref(w), C.byref(h))
+            out.append(Dims(w.value, h.value))
+        return out
+
+    def write(self):
+        """The serialised transform, as bytes."""
+        n = C.c_size_t()
+        rc = lib().ts_transform_write(self._h, None, 0, C.byref(n))
+        if rc:
+            raise Error(rc, "ts_transform_write")
+        buf = (C.c_uint8 * n.value)()
+        rc = lib().ts_transform_write(self._h, buf, n.value, C.byref(n))
+        if rc:
+            raise Error(rc, "ts_transform_write")
+        return bytes(buf)
+
+    @staticmethod
+    def read(data):
+        out = C.c_void_p()
+        rc = lib().ts_transform_read(data, len(data), C.byref(out))
+        if rc:
+            raise Error(rc, "ts_transform_read: malformed transform")
+        return CoordinateTransform(out.value)
+
+    def apply(self, sources, device=0):
+        """CoordinateTransform::apply: the output image (H x W x 4 uint8)."""
+        imgs = [_rgba(im) for im in sources]
+        descs = (_ImageDesc * max(1, len(imgs)))()
+        for d, im in zip(descs, imgs):
+            d.rgba, d.width, d.height = im.ctypes.data, im.shape[1], im.shape[0]
+        out = np.empty((self.height, self.width, 4), np.uint8)
+        rc = lib().ts_transform_apply(self._h, descs, len(imgs), out.ctypes.data, device)
+        if rc:
+            raise Error(rc, "ts_transform_apply")
+        return out
 
 
 def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0, profile=False, team_max_batch=None,

@@ -86,6 +86,23 @@ TS_HD uint64_t mulhi64(uint64_t a, uint64_t b) {
 
 // Rng::gen_range(0..n) for u32: widening multiply, rejection zone
 // (n << clz(n)) - 1.  n > 0.
+// rand 0.8.5 UniformInt<u8>::sample_single(0, 255) with a Pcg32 seeded by
+// seed_from_u64(seed): for 8- and 16-bit types the rejection zone is
+// u32::MAX - (u32::MAX - range + 1) % range (range = 255 here), the draw
+// (v * range) >> 32 of a u32 v.  The colour of an id in the debug maps
+// (ms.rs:604-636).
+TS_HD uint8_t id_colour(uint64_t seed) {
+  Pcg32 g = pcg_from_u64(seed);
+  const uint32_t range = 255u;
+  const uint32_t zone = 0xffffffffu - (uint32_t)((0x100000000ull - range) % range);
+  uint64_t m = 0;
+  for (int t = 0; t < 64; ++t) {  // a draw is rejected with probability 2^-32
+    m = (uint64_t)pcg_u32(g) * range;
+    if ((uint32_t)m <= zone) break;
+  }
+  return (uint8_t)(m >> 32);
+}
+
 TS_HD uint32_t gen_range_u32(Pcg32 &g, uint32_t n) {
   uint32_t zone = (n << clz32(n)) - 1u;
   for (;;) {

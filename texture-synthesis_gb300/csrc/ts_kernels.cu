@@ -1438,6 +1438,52 @@ __device__ __forceinline__ void level_switch_body(const SessionDev &s, uint32_t 
   s.color[p] = s.levels[md.off + (size_t)level * md.w * md.h + (size_t)y * md.w + x];
 }
 
+// CoordinateTransform::apply (lib.rs:176-212): output pixel i takes texel
+// (x, y) of source map `map`, (x, y, map) = buf[3i..3i+3].  maps[m] =
+// {texel offset low, high, width, height}.  An entry outside the maps (the
+// reference panics in get_pixel) writes 0 and sets *err.
+__global__ void k_transform_apply(const uint32_t *buf, size_t n, const uint32_t *texels, const uint4 *maps,
+                                  uint32_t n_maps, uint32_t *out, int *err) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t x = buf[3 * i], y = buf[3 * i + 1], m = buf[3 * i + 2];
+    uint32_t v = 0;
+    if (m < n_maps) {
+      const uint4 md = maps[m];
+      if (x < md.z && y < md.w)
+        v = texels[(((size_t)md.y << 32) | md.x) + (size_t)y * md.z + x];
+      else
+        set_err(err, 1);
+    } else {
+      set_err(err, 1);
+    }
+    out[i] = v;
+  }
+}
+
+// Debug maps (ms.rs:604-653): the patch-id and map-id colours of every
+// pixel, and the uncertainty colour of every resolved pixel (the others
+// stay 0).  Ids combine in u32 arithmetic, which wraps as the reference's
+// release build does.
+__global__ void k_id_maps(const uint32_t *ids, size_t n, uint32_t *patch_rgba, uint32_t *map_rgba) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t p = ids[2 * i], m = ids[2 * i + 1];
+    patch_rgba[i] = (uint32_t)id_colour(p) | ((uint32_t)id_colour(p * 5u + 21u) << 8) |
+                    ((uint32_t)id_colour(p / 4u + 12u) << 16) | 0xff000000u;
+    map_rgba[i] = (uint32_t)id_colour((uint64_t)m * 200u) | ((uint32_t)id_colour(m * 5u + 341u) << 8) |
+                  ((uint32_t)id_colour(m * 1200u - 35412u) << 16) | 0xff000000u;
+  }
+}
+
+__global__ void k_uncertainty(const uint32_t *flat, const float *score, size_t n_res, size_t n_px, uint32_t *out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n_res; i += (size_t)gridDim.x * blockDim.x) {
+    // (score.min(1.0) * 255.0) as u8: f32::min returns the other operand
+    // for NaN, and `as` truncates and saturates
+    const float v = __fmul_rn(fminf(score[i], 1.0f), 255.0f);
+    const uint32_t ns = v >= 255.0f ? 255u : (v > 0.0f ? (uint32_t)v : 0u);
+    if (flat[i] < n_px) out[flat[i]] = ns | ((255u - ns) << 8) | 0xff000000u;
+  }
+}
+
 // vertical_sample: u8 RGBA -> f32 RGBA, new height nh.
 __global__ void k_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uint32_t nh, const uint4 *taps,
                            const float *wts) {
@@ -1844,6 +1890,22 @@ void launch_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, ui
   const size_t n = (size_t)pitch * (h + 2 * kPad) * levels;
   if (n == 0) return;
   k_pad<<<(uint32_t)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, stream>>>(src, w, h, levels, pitch, dst);
+}
+
+void launch_transform_apply(const uint32_t *buf, size_t n, const uint32_t *texels, const uint4 *maps,
+                            uint32_t n_maps, uint32_t *out, int *err, cudaStream_t stream) {
+  if (n == 0) return;
+  k_transform_apply<<<(uint32_t)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, stream>>>(buf, n, texels, maps,
+                                                                                                n_maps, out, err);
+}
+
+void launch_debug_maps(const uint32_t *ids, size_t n, const uint32_t *flat, const float *score, size_t n_res,
+                       uint32_t *patch_rgba, uint32_t *map_rgba, uint32_t *unc_rgba, cudaStream_t stream) {
+  if (n > 0)
+    k_id_maps<<<(uint32_t)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, stream>>>(ids, n, patch_rgba, map_rgba);
+  if (n_res > 0)
+    k_uncertainty<<<(uint32_t)std::min<size_t>((n_res + 255) / 256, 152 * 16), 256, 0, stream>>>(flat, score, n_res, n,
+                                                                                                  unc_rgba);
 }
 
 void launch_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uint32_t nh, const uint4 *taps,

@@ -196,6 +196,16 @@ void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev
 void launch_commit(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
 void launch_level_switch(const SessionDev &s, uint32_t level, uint32_t n_res, cudaStream_t stream);
 
+// CoordinateTransform::apply: out[i] = texel buf[3i..3i+3] = (x, y, map) of
+// the maps {offset low, offset high, w, h}; *err set for entries outside.
+void launch_transform_apply(const uint32_t *buf, size_t n, const uint32_t *texels, const uint4 *maps,
+                            uint32_t n_maps, uint32_t *out, int *err, cudaStream_t stream);
+// Debug maps: patch-id and map-id colours of the n pixels' (patch, map) ids,
+// and the uncertainty colours of the n_res resolved entries (unc_rgba must
+// start zeroed).
+void launch_debug_maps(const uint32_t *ids, size_t n, const uint32_t *flat, const float *score, size_t n_res,
+                       uint32_t *patch_rgba, uint32_t *map_rgba, uint32_t *unc_rgba, cudaStream_t stream);
+
 // Separable resize (image 0.23 imageops::resize): taps[o] = {left, count,
 // weight offset}; vertical pass u8 -> f32, horizontal pass f32 -> u8.
 void launch_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uint32_t nh, const uint4 *taps,

@@ -320,6 +320,7 @@ struct ts_session {
 
 struct ts_generated {
   uint32_t W = 0, H = 0;
+  std::vector<uint32_t> in_dims;  // (w, h) of every example at its loaded size
   std::vector<uint8_t> image;
   std::vector<uint32_t> coord;  // 3 per pixel
   std::vector<uint32_t> ids;    // 2 per pixel
@@ -1470,6 +1471,11 @@ void run_finish(RunCtx &c) {
     g->ids[2 * i] = c.stv[i].y;
     g->ids[2 * i + 1] = c.stv[i].z;
   }
+  g->in_dims.clear();
+  for (const Image &im : c.s->bottoms) {
+    g->in_dims.push_back(im.w);
+    g->in_dims.push_back(im.h);
+  }
   g->stats.resolves = c.resolves;
   g->stats.batches = c.batches;
   g->stats.stages = c.plan.size();
@@ -2430,6 +2436,192 @@ void ts_server_stats_get(ts_server *S, ts_server_stats *out) {
   std::lock_guard<std::mutex> lk(S->mu);
   *out = S->stats;
   out->budget_bytes = S->budget;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// CoordinateTransform (lib.rs:162-325) and the debug maps (ms.rs:604-653).
+// ---------------------------------------------------------------------------
+struct ts_transform {
+  uint32_t W = 0, H = 0;
+  std::vector<uint32_t> maps;  // (w, h) per original example
+  std::vector<uint32_t> buf;   // (x, y, map) per output pixel
+};
+
+namespace {
+constexpr uint32_t kTransformMagic = 0x12340001u;  // TRANSFORM_MAGIC, lib.rs:168
+}
+
+extern "C" {
+
+ts_transform *ts_generated_coord_transform(const ts_generated *g) {
+  if (!g) return nullptr;
+  ts_transform *t = new (std::nothrow) ts_transform();
+  if (!t) return nullptr;
+  t->W = g->W;
+  t->H = g->H;
+  t->maps = g->in_dims;
+  t->buf = g->coord;
+  return t;
+}
+
+void ts_transform_free(ts_transform *t) { delete t; }
+
+void ts_transform_dims(const ts_transform *t, uint32_t *width, uint32_t *height, uint32_t *n_maps) {
+  if (!t) return;
+  if (width) *width = t->W;
+  if (height) *height = t->H;
+  if (n_maps) *n_maps = (uint32_t)(t->maps.size() / 2);
+}
+
+int ts_transform_map_dims(const ts_transform *t, uint32_t i, uint32_t *width, uint32_t *height) {
+  if (!t || !width || !height) return TS_ERR_NULL;
+  if ((size_t)i * 2 >= t->maps.size()) return TS_ERR_INDEX;
+  *width = t->maps[2 * (size_t)i];
+  *height = t->maps[2 * (size_t)i + 1];
+  return TS_OK;
+}
+
+int ts_transform_write(const ts_transform *t, uint8_t *out, size_t capacity, size_t *written) {
+  if (!t || !written) return TS_ERR_NULL;
+  if (t->buf.size() != (size_t)t->W * t->H * 3) return TS_ERR_SIZE_MISMATCH;
+  std::vector<uint32_t> words;
+  words.reserve(4 + t->maps.size() + t->buf.size());
+  words.push_back(kTransformMagic);
+  words.push_back(t->W);
+  words.push_back(t->H);
+  words.push_back((uint32_t)(t->maps.size() / 2));
+  words.insert(words.end(), t->maps.begin(), t->maps.end());
+  words.insert(words.end(), t->buf.begin(), t->buf.end());
+  *written = words.size() * 4;
+  if (!out) return TS_OK;  // size query
+  if (capacity < words.size() * 4) return TS_ERR_LIMIT;
+  for (size_t i = 0; i < words.size(); ++i) {  // little-endian u32, as the reference writes on its targets
+    out[4 * i] = (uint8_t)words[i];
+    out[4 * i + 1] = (uint8_t)(words[i] >> 8);
+    out[4 * i + 2] = (uint8_t)(words[i] >> 16);
+    out[4 * i + 3] = (uint8_t)(words[i] >> 24);
+  }
+  return TS_OK;
+}
+
+int ts_transform_read(const uint8_t *data, size_t len, ts_transform **out) {
+  if (!data || !out) return TS_ERR_NULL;
+  *out = nullptr;
+  size_t pos = 0;
+  auto word = [&](uint32_t &v) {
+    if (pos + 4 > len) return false;
+    v = (uint32_t)data[pos] | ((uint32_t)data[pos + 1] << 8) | ((uint32_t)data[pos + 2] << 16) |
+        ((uint32_t)data[pos + 3] << 24);
+    pos += 4;
+    return true;
+  };
+  uint32_t magic = 0, w = 0, h = 0, n = 0;
+  if (!word(magic) || (magic >> 16) != 0x1234u || (magic & 0xffffu) != 0x1u) return TS_ERR_INVALID_RANGE;
+  if (!word(w) || !word(h) || !word(n)) return TS_ERR_INVALID_RANGE;
+  if ((uint64_t)n * 8 > len || (uint64_t)w * h * 12 > len) return TS_ERR_INVALID_RANGE;
+  std::unique_ptr<ts_transform> t(new (std::nothrow) ts_transform());
+  if (!t) return TS_ERR_OUT_OF_MEMORY;
+  t->W = w;
+  t->H = h;
+  t->maps.resize((size_t)n * 2);
+  for (auto &v : t->maps)
+    if (!word(v)) return TS_ERR_INVALID_RANGE;
+  t->buf.resize((size_t)w * h * 3);
+  for (auto &v : t->buf)
+    if (!word(v)) return TS_ERR_INVALID_RANGE;
+  *out = t.release();
+  return TS_OK;
+}
+
+int ts_transform_apply(const ts_transform *t, const ts_image_desc *sources, uint32_t n_sources, uint8_t *out_rgba,
+                       int32_t device) {
+  if (!t || !out_rgba || (n_sources && !sources)) return TS_ERR_NULL;
+  const uint32_t n_maps = (uint32_t)(t->maps.size() / 2);
+  // the sources pair with the original maps; extra sources are dropped, too
+  // few are an error (lib.rs:183-198)
+  if (std::min(n_sources, n_maps) != n_maps) return TS_ERR_MAPS_COUNT_MISMATCH;
+  try {
+    CUDA_TRY(cudaSetDevice(device));
+    StreamGuard sg;
+    CUDA_TRY(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
+    const cudaStream_t st = sg.s;
+    std::vector<Image> maps(n_maps);
+    std::vector<uint4> desc(std::max<uint32_t>(n_maps, 1));
+    uint64_t texels = 0;
+    for (uint32_t i = 0; i < n_maps; ++i) {
+      if (!check_image(sources[i].rgba, sources[i].width, sources[i].height)) return TS_ERR_IMAGE;
+      // load_image with the original size: CatmullRom resize if it differs
+      maps[i] = load_image(copy_image(sources[i].rgba, sources[i].width, sources[i].height), true, t->maps[2 * i],
+                           t->maps[2 * i + 1], st);
+      desc[i] = make_uint4((uint32_t)texels, (uint32_t)(texels >> 32), maps[i].w, maps[i].h);
+      texels += (uint64_t)maps[i].w * maps[i].h;
+    }
+    const size_t n = (size_t)t->W * t->H;
+    DevBuf<uint32_t> d_tex, d_buf, d_out;
+    DevBuf<uint4> d_desc;
+    DevBuf<int> d_err;
+    CUDA_TRY(d_tex.alloc_on(texels, st));
+    CUDA_TRY(d_buf.alloc_on(t->buf.size(), st));
+    CUDA_TRY(d_out.alloc_on(n, st));
+    CUDA_TRY(d_desc.alloc_on(desc.size(), st));
+    CUDA_TRY(d_err.alloc_on(1, st));
+    for (uint32_t i = 0; i < n_maps; ++i)
+      CUDA_TRY(cudaMemcpyAsync(d_tex.p + ((uint64_t)desc[i].y << 32 | desc[i].x), maps[i].px.data(),
+                               maps[i].px.size(), cudaMemcpyHostToDevice, st));
+    if (!t->buf.empty())
+      CUDA_TRY(cudaMemcpyAsync(d_buf.p, t->buf.data(), t->buf.size() * 4, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_desc.p, desc.data(), desc.size() * sizeof(uint4), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(d_err.p, 0, sizeof(int), st));
+    launch_transform_apply(d_buf.p, n, d_tex.p, d_desc.p, n_maps, d_out.p, d_err.p, st);
+    CUDA_TRY(cudaGetLastError());
+    int err = 0;
+    if (n) CUDA_TRY(cudaMemcpyAsync(out_rgba, d_out.p, n * 4, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(&err, d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (err) return TS_ERR_INDEX;
+  } catch (const Failure &f) {
+    return f.status;
+  }
+  return TS_OK;
+}
+
+int ts_generated_debug_maps(const ts_generated *g, uint8_t *patch_id_rgba, uint8_t *map_id_rgba,
+                            uint8_t *uncertainty_rgba, int32_t device) {
+  if (!g || !patch_id_rgba || !map_id_rgba || !uncertainty_rgba) return TS_ERR_NULL;
+  try {
+    CUDA_TRY(cudaSetDevice(device));
+    StreamGuard sg;
+    CUDA_TRY(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
+    const cudaStream_t st = sg.s;
+    const size_t n = (size_t)g->W * g->H, nr = g->resolved.size();
+    DevBuf<uint32_t> d_ids, d_flat, d_patch, d_map, d_unc;
+    DevBuf<float> d_score;
+    CUDA_TRY(d_ids.alloc_on(n * 2, st));
+    CUDA_TRY(d_flat.alloc_on(nr, st));
+    CUDA_TRY(d_score.alloc_on(nr, st));
+    CUDA_TRY(d_patch.alloc_on(n, st));
+    CUDA_TRY(d_map.alloc_on(n, st));
+    CUDA_TRY(d_unc.alloc_on(n, st));
+    if (n) CUDA_TRY(cudaMemcpyAsync(d_ids.p, g->ids.data(), n * 8, cudaMemcpyHostToDevice, st));
+    if (nr) {
+      CUDA_TRY(cudaMemcpyAsync(d_flat.p, g->resolved.data(), nr * 4, cudaMemcpyHostToDevice, st));
+      CUDA_TRY(cudaMemcpyAsync(d_score.p, g->scores.data(), nr * 4, cudaMemcpyHostToDevice, st));
+    }
+    CUDA_TRY(cudaMemsetAsync(d_unc.p, 0, n * 4, st));
+    launch_debug_maps(d_ids.p, n, d_flat.p, d_score.p, nr, d_patch.p, d_map.p, d_unc.p, st);
+    CUDA_TRY(cudaGetLastError());
+    if (n) {
+      CUDA_TRY(cudaMemcpyAsync(patch_id_rgba, d_patch.p, n * 4, cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaMemcpyAsync(map_id_rgba, d_map.p, n * 4, cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaMemcpyAsync(uncertainty_rgba, d_unc.p, n * 4, cudaMemcpyDeviceToHost, st));
+    }
+    CUDA_TRY(cudaStreamSynchronize(st));
+  } catch (const Failure &f) {
+    return f.status;
+  }
+  return TS_OK;
 }
 
 }  // extern "C"
