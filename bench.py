@@ -290,6 +290,13 @@ def main():
 
     wl = importlib.import_module(PKG + ".workloads")
     if args.workload == "batched":
+        if args.once:  # one batched run of the 64-session mix (for profilers)
+            b = ts.Batch()
+            for sp in wl.config3_sessions(64):
+                b.add(ts.builder_from_spec(sp).build())
+            b.run()
+            print(json.dumps(b.stats()))
+            return
         print(json.dumps({"metric": "aggregate output Mpx/s (batched form)", **measure_batched(ts, wl)}))
         return
     if args.workload == "served":
