@@ -47,8 +47,7 @@ typedef enum ts_status {
   TS_ERR_NO_EXAMPLES = 4,
   TS_ERR_MAPS_COUNT_MISMATCH = 5,
   TS_ERR_IMAGE = 6,
-  /* A feature of the reference that this library does not provide
-   * (automatic guide maps for style transfer, lib.rs:575-582). */
+  /* A feature of the reference that this library does not provide. */
   TS_ERR_UNSUPPORTED = 7,
   /* A sample mask with no usable texel: the reference loops forever
    * (ms.rs:562-574); this library refuses it. */
@@ -152,6 +151,15 @@ void ts_get_limits(ts_limits *out);
  * guides. */
 int ts_image_pyramid(const uint8_t *rgba, uint32_t width, uint32_t height, uint32_t levels, uint8_t *out_rgba,
                      int32_t device);
+
+/* transform_to_guide_map + match_histograms (utils.rs:101-183) on the
+ * device: the automatic guide that build() makes for an example without a
+ * guide when a target guide is loaded (lib.rs:575-582).  imageops::blur with
+ * sigma 2, grayscale (0.2126 R + 0.7152 G + 0.0722 B, truncated), then the
+ * luma histogram matched to channel 0 of the target guide.  out_rgba:
+ * width*height*4 bytes of (v, v, v, 255). */
+int ts_guide_map(const uint8_t *rgba, uint32_t width, uint32_t height, const uint8_t *target_rgba,
+                 uint32_t target_width, uint32_t target_height, uint8_t *out_rgba, int32_t device);
 
 /* ts_image_pyramid_noalloc: no counterpart in the reference.  The same
  * pyramid as ts_image_pyramid, byte for byte, for callers that cannot let a

@@ -218,7 +218,15 @@ double tso_exp_export(double x) { return tso_exp(x); }
 /* image 0.23.12 imageops::resize restated (img_pyramid.rs:27-32 calls it     */
 /* with FilterType::Gaussian; utils.rs:67-72 with CatmullRom).                */
 /* ------------------------------------------------------------------------ */
-enum { TSO_FILTER_NEAREST = 0, TSO_FILTER_TRIANGLE = 1, TSO_FILTER_CATMULLROM = 2, TSO_FILTER_GAUSSIAN = 3 };
+enum { TSO_FILTER_NEAREST = 0, TSO_FILTER_TRIANGLE = 1, TSO_FILTER_CATMULLROM = 2, TSO_FILTER_GAUSSIAN = 3, TSO_FILTER_BLUR = 4 };
+
+/* imageops::blur's kernel: gaussian(x, sigma) = 1/(sqrt(2 pi) sigma) *
+ * exp(-x^2 / (2 sigma^2)), support 2 sigma */
+static float k_gauss_sigma(float x, float r) {
+  float a = 1.0f / (sqrtf(2.0f * 3.14159265358979323846f) * r);
+  float b = expf(-(x * x) / (2.0f * (r * r)));
+  return a * b;
+}
 
 static float k_gauss(float x) {
   /* gaussian(x, r = 0.5) = 1/(sqrt(2 pi) r) * exp(-x^2 / (2 r^2)) */
@@ -248,16 +256,18 @@ static float k_catmullrom(float x) {
 }
 static float k_box(float x) { return (x >= -0.5f && x < 0.5f) ? 1.0f : 0.0f; }
 
-static float filt_eval(int f, float x) {
+static float filt_eval(int f, float x, float sigma) {
   switch (f) {
+    case TSO_FILTER_BLUR: return k_gauss_sigma(x, sigma);
     case TSO_FILTER_TRIANGLE: return k_triangle(x);
     case TSO_FILTER_CATMULLROM: return k_catmullrom(x);
     case TSO_FILTER_GAUSSIAN: return k_gauss(x);
     default: return k_box(x);
   }
 }
-static float filt_support(int f) {
+static float filt_support(int f, float sigma) {
   switch (f) {
+    case TSO_FILTER_BLUR: return 2.0f * sigma;
     case TSO_FILTER_TRIANGLE: return 1.0f;
     case TSO_FILTER_CATMULLROM: return 2.0f;
     case TSO_FILTER_GAUSSIAN: return 3.0f;
@@ -273,11 +283,11 @@ static int64_t clamp_i64(int64_t a, int64_t lo, int64_t hi) {
 
 /* Taps of one output index along an axis: [left, right) and normalised
  * weights.  Returns the tap count; writes at most cap weights. */
-static int axis_taps(int f, uint32_t in_len, uint32_t out_len, uint32_t o, uint32_t *left_out, float *ws,
-                     int cap) {
+static int axis_taps(int f, float sigma, uint32_t in_len, uint32_t out_len, uint32_t o, uint32_t *left_out,
+                     float *ws, int cap) {
   float ratio = (float)in_len / (float)out_len;
   float sratio = ratio < 1.0f ? 1.0f : ratio;
-  float src_support = filt_support(f) * sratio;
+  float src_support = filt_support(f, sigma) * sratio;
   float c = ((float)o + 0.5f) * ratio;
   int64_t left = (int64_t)floorf(c - src_support);
   left = clamp_i64(left, 0, (int64_t)in_len - 1);
@@ -287,7 +297,7 @@ static int axis_taps(int f, uint32_t in_len, uint32_t out_len, uint32_t o, uint3
   int n = 0;
   float sum = 0.0f;
   for (int64_t i = left; i < right; i++) {
-    float w = filt_eval(f, ((float)i - c) / sratio);
+    float w = filt_eval(f, ((float)i - c) / sratio, sigma);
     if (n < cap) ws[n] = w;
     n++;
     sum += w;
@@ -299,13 +309,14 @@ static int axis_taps(int f, uint32_t in_len, uint32_t out_len, uint32_t o, uint3
 
 /* Resize an RGBA8 image: vertical pass into an f32 image, then horizontal
  * pass with clamping to [0,255] and rounding half away from zero. */
-int tso_resize(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uint32_t nw, uint32_t nh, int filter) {
+static int resize_sigma(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uint32_t nw, uint32_t nh, int filter,
+                        float sigma) {
   if (nw == 0 || nh == 0) return TSO_OK;
   float *tmp = (float *)calloc((size_t)w * nh * 4 + 4, sizeof(float));
   float rv = nh ? (float)h / (float)nh : 1.0f, rh = nw ? (float)w / (float)nw : 1.0f;
   float rmax = rv > rh ? rv : rh;
   if (rmax < 1.0f) rmax = 1.0f;
-  int cap = (int)(2.0f * filt_support(filter) * rmax) + 16;
+  int cap = (int)(2.0f * filt_support(filter, sigma) * rmax) + 16;
   float *ws = (float *)malloc(sizeof(float) * cap);
   if (!tmp || !ws) {
     free(tmp);
@@ -316,7 +327,7 @@ int tso_resize(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uint32_
   if (h > 0) {
     for (uint32_t oy = 0; oy < nh; oy++) {
       uint32_t left;
-      int n = axis_taps(filter, h, nh, oy, &left, ws, cap);
+      int n = axis_taps(filter, sigma, h, nh, oy, &left, ws, cap);
       if (n > cap) {
         free(tmp);
         free(ws);
@@ -345,7 +356,7 @@ int tso_resize(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uint32_
     uint32_t left = 0;
     int n = 0;
     if (w > 0) {
-      n = axis_taps(filter, w, nw, ox, &left, ws, cap);
+      n = axis_taps(filter, sigma, w, nw, ox, &left, ws, cap);
       if (n > cap) {
         free(tmp);
         free(ws);
@@ -373,6 +384,80 @@ int tso_resize(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uint32_
   }
   free(tmp);
   free(ws);
+  return TSO_OK;
+}
+
+int tso_resize(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uint32_t nw, uint32_t nh, int filter) {
+  return resize_sigma(src, w, h, dst, nw, nh, filter, 0.0f);
+}
+
+/* transform_to_guide_map + match_histograms (utils.rs:101-183, used by
+ * lib.rs:575-582 for examples without a guide when a target guide is set):
+ * imageops::blur (sigma 2: the resize passes at the same size with the
+ * kernel above), DynamicImage::grayscale (image 0.23 rgb_to_luma: 0.2126 R +
+ * 0.7152 G + 0.0722 B in f32, left to right, truncated to u8), then the
+ * histogram of that luma matched to channel 0 of the target guide:
+ * f32 cumulative distributions normalised by their last entry, and
+ * v -> (first index whose target cdf exceeds cdf_src[v], else v + 1 in u8)
+ * as u8 minus 1, both in wrapping u8 arithmetic (the reference's release
+ * build).  The transform's own resize discards its result (utils.rs:110-114)
+ * and is left out.  out: (n, n, n, 255) per texel. */
+int tso_guide_map(const uint8_t *src, uint32_t w, uint32_t h, const uint8_t *target, uint32_t tw, uint32_t th,
+                  uint8_t *out) {
+  size_t n = (size_t)w * h;
+  uint8_t *blur = (uint8_t *)malloc(n * 4 + 4);
+  uint8_t *luma = (uint8_t *)malloc(n + 1);
+  if (!blur || !luma) {
+    free(blur);
+    free(luma);
+    return TSO_ERR_ALLOC;
+  }
+  int rc = resize_sigma(src, w, h, blur, w, h, TSO_FILTER_BLUR, 2.0f);
+  if (rc != TSO_OK) {
+    free(blur);
+    free(luma);
+    return rc;
+  }
+  uint32_t hs[256] = {0}, ht[256] = {0};
+  for (size_t i = 0; i < n; i++) {
+    const uint8_t *p = blur + 4 * i;
+    float l = 0.2126f * (float)p[0];
+    l = l + 0.7152f * (float)p[1];
+    l = l + 0.0722f * (float)p[2];
+    luma[i] = (uint8_t)l;
+    hs[luma[i]]++;
+  }
+  for (size_t i = 0; i < (size_t)tw * th; i++) ht[target[4 * i]]++;
+  float cs[256], ct[256];
+  cs[0] = (float)hs[0];
+  ct[0] = (float)ht[0];
+  for (int i = 1; i < 256; i++) {
+    cs[i] = cs[i - 1] + (float)hs[i];
+    ct[i] = ct[i - 1] + (float)ht[i];
+  }
+  float ms = cs[255], mt = ct[255];
+  for (int i = 0; i < 256; i++) {
+    cs[i] /= ms;
+    ct[i] /= mt;
+  }
+  uint8_t map[256];
+  for (int v = 0; v < 256; v++) {
+    int pos = -1;
+    for (int i = 0; i < 256; i++)
+      if (ct[i] > cs[v]) {
+        pos = i;
+        break;
+      }
+    uint32_t idx = pos >= 0 ? (uint32_t)pos : (uint32_t)(uint8_t)(v + 1);
+    map[v] = (uint8_t)((uint8_t)idx - 1u);
+  }
+  for (size_t i = 0; i < n; i++) {
+    uint8_t v = map[luma[i]];
+    out[4 * i] = out[4 * i + 1] = out[4 * i + 2] = v;
+    out[4 * i + 3] = 255;
+  }
+  free(blur);
+  free(luma);
   return TSO_OK;
 }
 

@@ -75,6 +75,9 @@ def lib():
         L.tso_pyramid.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p]
         L.tso_pcg_seed.argtypes = [C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.tso_pcg_stream.argtypes = [C.c_uint64, C.c_uint32, C.c_void_p]
+        L.tso_guide_map.restype = C.c_int
+        L.tso_guide_map.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32,
+                                    C.c_void_p]
         L.tso_id_colour.restype = C.c_uint8
         L.tso_id_colour.argtypes = [C.c_uint64]
         L.tso_debug_maps.restype = None
@@ -211,3 +214,16 @@ def debug_maps(ids, flat, score):
 
 def id_colour(seed):
     return int(lib().tso_id_colour(seed))
+
+
+def guide_map(image, target):
+    """transform_to_guide_map + match_histograms (utils.rs:101-183): the
+    automatic guide of an example for a target guide, RGBA8."""
+    img = np.ascontiguousarray(image, np.uint8)
+    tgt = np.ascontiguousarray(target, np.uint8)
+    out = np.empty_like(img)
+    rc = lib().tso_guide_map(img.ctypes.data, img.shape[1], img.shape[0], tgt.ctypes.data, tgt.shape[1],
+                             tgt.shape[0], out.ctypes.data)
+    if rc:
+        raise RuntimeError("tso_guide_map failed: %d" % rc)
+    return out

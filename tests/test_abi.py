@@ -112,11 +112,14 @@ def test_limits_enforced(ts):
     assert e.value.kind == "Limit"
 
 
-def test_style_transfer_without_example_guides_is_reported(ts):
+def test_style_transfer_without_example_guides_passes_validation(ts):
+    # automatic guide maps are built for examples without a guide; the build
+    # can then only fail for want of a device
     b = ts.Session.builder().add_example(_img()).load_target_guide(_img())
-    with pytest.raises(ts.Error) as e:
+    try:
         b.build()
-    assert e.value.kind == "Unsupported"
+    except ts.Error as e:
+        assert e.kind == "Cuda", e
 
 
 def test_builder_is_consumed_by_build(ts):

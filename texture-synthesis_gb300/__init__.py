@@ -117,6 +117,8 @@ SIGNATURES = {
     "ts_status_str": (C.c_char_p, [C.c_int]),
     "ts_get_limits": (None, [C.POINTER(_Limits)]),
     "ts_image_pyramid": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_int32]),
+    "ts_guide_map": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+                               C.c_int32]),
     "ts_image_pyramid_noalloc": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p,
                                            C.c_void_p]),
     "ts_builder_new": (C.c_void_p, []),
@@ -224,6 +226,19 @@ def image_pyramid(image, levels, device=0):
     rc = lib().ts_image_pyramid(img.ctypes.data, w, h, levels, out.ctypes.data, device)
     if rc:
         raise Error(rc, "ts_image_pyramid")
+    return out
+
+
+def guide_map(image, target, device=0):
+    """The automatic guide of an example for a target guide
+    (transform_to_guide_map + match_histograms, utils.rs:101-183)."""
+    img = _rgba(image)
+    tgt = _rgba(target)
+    out = np.empty_like(img)
+    rc = lib().ts_guide_map(img.ctypes.data, img.shape[1], img.shape[0], tgt.ctypes.data, tgt.shape[1],
+                            tgt.shape[0], out.ctypes.data, device)
+    if rc:
+        raise Error(rc, "ts_guide_map")
     return out
 
 

@@ -1484,6 +1484,47 @@ __global__ void k_uncertainty(const uint32_t *flat, const float *score, size_t n
   }
 }
 
+// Automatic guide maps (utils.rs:101-183).  DynamicImage::grayscale of RGBA8
+// (image 0.23 rgb_to_luma): l = 0.2126 R + 0.7152 G + 0.0722 B in f32, left
+// to right, truncated to u8 (NumCast), with the histogram of l; the
+// histogram of channel 0 of an RGBA8 image; and the histogram-matching map
+// applied as (n, n, n, 255).
+__global__ void k_luma_hist(const uint32_t *src, size_t n, uint8_t *luma, uint32_t *hist) {
+  __shared__ uint32_t h[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t p = src[i];
+    float l = __fmul_rn(0.2126f, (float)(p & 0xffu));
+    l = __fadd_rn(l, __fmul_rn(0.7152f, (float)((p >> 8) & 0xffu)));
+    l = __fadd_rn(l, __fmul_rn(0.0722f, (float)((p >> 16) & 0xffu)));
+    const uint32_t v = l >= 255.0f ? 255u : (uint32_t)l;
+    luma[i] = (uint8_t)v;
+    atomicAdd(&h[v], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+__global__ void k_hist_r(const uint32_t *src, size_t n, uint32_t *hist) {
+  __shared__ uint32_t h[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    atomicAdd(&h[src[i] & 0xffu], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+__global__ void k_apply_map(const uint8_t *luma, size_t n, const uint8_t *map, uint32_t *out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t v = map[luma[i]];
+    out[i] = v | (v << 8) | (v << 16) | 0xff000000u;
+  }
+}
+
 // vertical_sample: u8 RGBA -> f32 RGBA, new height nh.
 __global__ void k_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uint32_t nh, const uint4 *taps,
                            const float *wts) {
@@ -1906,6 +1947,21 @@ void launch_debug_maps(const uint32_t *ids, size_t n, const uint32_t *flat, cons
   if (n_res > 0)
     k_uncertainty<<<(uint32_t)std::min<size_t>((n_res + 255) / 256, 152 * 16), 256, 0, stream>>>(flat, score, n_res, n,
                                                                                                   unc_rgba);
+}
+
+void launch_luma_hist(const uint32_t *src, size_t n, uint8_t *luma, uint32_t *hist, cudaStream_t stream) {
+  if (n == 0) return;
+  k_luma_hist<<<(uint32_t)std::min<size_t>((n + 255) / 256, 152 * 4), 256, 0, stream>>>(src, n, luma, hist);
+}
+
+void launch_hist_r(const uint32_t *src, size_t n, uint32_t *hist, cudaStream_t stream) {
+  if (n == 0) return;
+  k_hist_r<<<(uint32_t)std::min<size_t>((n + 255) / 256, 152 * 4), 256, 0, stream>>>(src, n, hist);
+}
+
+void launch_apply_map(const uint8_t *luma, size_t n, const uint8_t *map, uint32_t *out, cudaStream_t stream) {
+  if (n == 0) return;
+  k_apply_map<<<(uint32_t)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, stream>>>(luma, n, map, out);
 }
 
 void launch_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uint32_t nh, const uint4 *taps,

@@ -206,6 +206,12 @@ void launch_transform_apply(const uint32_t *buf, size_t n, const uint32_t *texel
 void launch_debug_maps(const uint32_t *ids, size_t n, const uint32_t *flat, const float *score, size_t n_res,
                        uint32_t *patch_rgba, uint32_t *map_rgba, uint32_t *unc_rgba, cudaStream_t stream);
 
+// Automatic guide maps: luma of RGBA8 with its histogram (hist: 256 zeroed
+// counters), the histogram of channel 0, and map[luma] as (n, n, n, 255).
+void launch_luma_hist(const uint32_t *src, size_t n, uint8_t *luma, uint32_t *hist, cudaStream_t stream);
+void launch_hist_r(const uint32_t *src, size_t n, uint32_t *hist, cudaStream_t stream);
+void launch_apply_map(const uint8_t *luma, size_t n, const uint8_t *map, uint32_t *out, cudaStream_t stream);
+
 // Separable resize (image 0.23 imageops::resize): taps[o] = {left, count,
 // weight offset}; vertical pass u8 -> f32, horizontal pass f32 -> u8.
 void launch_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uint32_t nh, const uint4 *taps,

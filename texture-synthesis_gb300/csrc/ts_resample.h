@@ -71,8 +71,17 @@ struct Taps {
   std::vector<float> weights;
 };
 
-// Taps along one axis of length in_len resampled to out_len.
-inline Taps axis_taps(Filter f, uint32_t in_len, uint32_t out_len) {
+// imageops::blur's kernel (image 0.23.12 sample.rs gaussian): the Gaussian
+// with standard deviation r, support 2r.
+inline float gaussian_sigma(float x, float r) {
+  const float norm = 1.0f / (sqrtf(2.0f * 3.14159265358979323846f) * r);
+  return norm * expf(-(x * x) / (2.0f * (r * r)));
+}
+
+// Taps along one axis of length in_len resampled to out_len with kernel k of
+// the given support.
+template <typename K>
+inline Taps axis_taps_k(float support, K k, uint32_t in_len, uint32_t out_len) {
   Taps t;
   t.left.resize(out_len);
   t.count.resize(out_len);
@@ -80,7 +89,7 @@ inline Taps axis_taps(Filter f, uint32_t in_len, uint32_t out_len) {
   if (in_len == 0) return t;  // every output is zero: no taps
   const float ratio = (float)in_len / (float)out_len;
   const float sratio = ratio < 1.0f ? 1.0f : ratio;
-  const float src_support = filter_support(f) * sratio;
+  const float src_support = support * sratio;
   for (uint32_t o = 0; o < out_len; ++o) {
     float c = ((float)o + 0.5f) * ratio;
     int64_t left = (int64_t)floorf(c - src_support);
@@ -93,7 +102,7 @@ inline Taps axis_taps(Filter f, uint32_t in_len, uint32_t out_len) {
     const size_t base = t.weights.size();
     float sum = 0.0f;
     for (int64_t i = left; i < right; ++i) {
-      const float w = filter_eval(f, ((float)i - c) / sratio);
+      const float w = k(((float)i - c) / sratio);
       t.weights.push_back(w);
       sum += w;
     }
@@ -103,6 +112,16 @@ inline Taps axis_taps(Filter f, uint32_t in_len, uint32_t out_len) {
     t.offset[o] = (uint32_t)base;
   }
   return t;
+}
+
+inline Taps axis_taps(Filter f, uint32_t in_len, uint32_t out_len) {
+  return axis_taps_k(filter_support(f), [f](float x) { return filter_eval(f, x); }, in_len, out_len);
+}
+
+// imageops::blur (sigma <= 0 means 1): the resize passes at the same size.
+inline Taps blur_taps(uint32_t len, float sigma) {
+  const float r = sigma <= 0.0f ? 1.0f : sigma;
+  return axis_taps_k(2.0f * r, [r](float x) { return gaussian_sigma(x, r); }, len, len);
 }
 
 // axis_taps written into caller storage: left/count/offset per output index

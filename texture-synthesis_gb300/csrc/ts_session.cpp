@@ -214,12 +214,12 @@ void upload_taps(const Taps &t, DevTaps &d, cudaStream_t st) {
 
 // imageops::resize on the device: src (device u8, w x h) -> dst (device u8,
 // nw x nh), enqueued on st (its temporaries are freed in stream order).
-void device_resize(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uint32_t nw, uint32_t nh, Filter f,
-                   cudaStream_t st) {
+void device_resample(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uint32_t nw, uint32_t nh,
+                     const Taps &taps_v, const Taps &taps_h, cudaStream_t st) {
   if (nw == 0 || nh == 0) return;
   DevTaps tv, th;
-  upload_taps(axis_taps(f, h, nh), tv, st);
-  upload_taps(axis_taps(f, w, nw), th, st);
+  upload_taps(taps_v, tv, st);
+  upload_taps(taps_h, th, st);
   DevBuf<float> tmp;
   CUDA_TRY(tmp.alloc_on((size_t)w * nh * 4, st));
   CUDA_TRY(cudaMemsetAsync(tmp.p, 0, (size_t)w * nh * 4 * sizeof(float), st));
@@ -230,6 +230,72 @@ void device_resize(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uin
     CUDA_TRY(cudaMemsetAsync(dst, 0, (size_t)nw * nh * 4, st));
   }
   CUDA_TRY(cudaGetLastError());
+}
+
+void device_resize(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uint32_t nw, uint32_t nh, Filter f,
+                   cudaStream_t st) {
+  if (nw == 0 || nh == 0) return;
+  device_resample(src, w, h, dst, nw, nh, axis_taps(f, h, nh), axis_taps(f, w, nw), st);
+}
+
+// transform_to_guide_map + match_histograms (utils.rs:101-183) on the device:
+// imageops::blur with sigma 2 (the resize passes at the same size),
+// grayscale, then the luma histogram matched to channel 0 of `target`.  The
+// transform's own resize discards its result (utils.rs:110-114) and is left
+// out.  The 256-entry map comes from the two histograms in the reference's
+// f32 arithmetic: v -> (first index whose target cdf exceeds cdf_src[v],
+// else v + 1 in u8) as u8 minus 1, wrapping as the reference's release
+// build does.
+Image device_guide_map(const Image &img, const Image &target, cudaStream_t st) {
+  const size_t n = (size_t)img.w * img.h, nt = (size_t)target.w * target.h;
+  DevBuf<uint8_t> d_src, d_blur, d_luma, d_map;
+  DevBuf<uint32_t> d_tgt, d_hist, d_out;
+  CUDA_TRY(d_src.alloc_on(n * 4, st));
+  CUDA_TRY(d_blur.alloc_on(n * 4, st));
+  CUDA_TRY(d_luma.alloc_on(n, st));
+  CUDA_TRY(d_map.alloc_on(256, st));
+  CUDA_TRY(d_tgt.alloc_on(nt, st));
+  CUDA_TRY(d_hist.alloc_on(512, st));
+  CUDA_TRY(d_out.alloc_on(n, st));
+  CUDA_TRY(cudaMemcpyAsync(d_src.p, img.px.data(), n * 4, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(d_tgt.p, target.px.data(), nt * 4, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemsetAsync(d_hist.p, 0, 512 * 4, st));
+  device_resample(d_src.p, img.w, img.h, d_blur.p, img.w, img.h, blur_taps(img.h, 2.0f), blur_taps(img.w, 2.0f), st);
+  launch_luma_hist((const uint32_t *)d_blur.p, n, d_luma.p, d_hist.p, st);
+  launch_hist_r(d_tgt.p, nt, d_hist.p + 256, st);
+  uint32_t hist[512];
+  CUDA_TRY(cudaMemcpyAsync(hist, d_hist.p, sizeof(hist), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  float cs[256], ct[256];
+  cs[0] = (float)hist[0];
+  ct[0] = (float)hist[256];
+  for (int i = 1; i < 256; ++i) {
+    cs[i] = cs[i - 1] + (float)hist[i];
+    ct[i] = ct[i - 1] + (float)hist[256 + i];
+  }
+  const float ms = cs[255], mt = ct[255];
+  for (int i = 0; i < 256; ++i) {
+    cs[i] /= ms;
+    ct[i] /= mt;
+  }
+  uint8_t map[256];
+  for (int v = 0; v < 256; ++v) {
+    int pos = -1;
+    for (int i = 0; i < 256 && pos < 0; ++i)
+      if (ct[i] > cs[v]) pos = i;
+    const uint32_t idx = pos >= 0 ? (uint32_t)pos : (uint32_t)(uint8_t)(v + 1);
+    map[v] = (uint8_t)((uint8_t)idx - 1u);
+  }
+  CUDA_TRY(cudaMemcpyAsync(d_map.p, map, 256, cudaMemcpyHostToDevice, st));
+  launch_apply_map(d_luma.p, n, d_map.p, d_out.p, st);
+  CUDA_TRY(cudaGetLastError());
+  Image out;
+  out.w = img.w;
+  out.h = img.h;
+  out.px.resize(n * 4);
+  CUDA_TRY(cudaMemcpyAsync(out.px.data(), d_out.p, n * 4, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return out;
 }
 
 // load_image (utils.rs:55-80): resize with CatmullRom when a size is given
@@ -373,6 +439,23 @@ int ts_image_pyramid(const uint8_t *rgba, uint32_t w, uint32_t h, uint32_t level
     CUDA_TRY(d.alloc((size_t)w * h * nl));
     device_pyramid(img, levels, d.p, 0);
     CUDA_TRY(cudaMemcpy(out, d.p, (size_t)w * h * nl * 4, cudaMemcpyDeviceToHost));
+  } catch (const Failure &f) {
+    return f.status;
+  }
+  return TS_OK;
+}
+
+int ts_guide_map(const uint8_t *rgba, uint32_t w, uint32_t h, const uint8_t *target_rgba, uint32_t tw, uint32_t th,
+                 uint8_t *out_rgba, int32_t device) {
+  if (!rgba || !target_rgba || !out_rgba) return TS_ERR_NULL;
+  if (w == 0 || h == 0 || tw == 0 || th == 0) return TS_ERR_IMAGE;
+  if (w > kMaxSide || h > kMaxSide || tw > kMaxSide || th > kMaxSide) return TS_ERR_LIMIT;
+  try {
+    CUDA_TRY(cudaSetDevice(device));
+    StreamGuard sg;
+    CUDA_TRY(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
+    const Image g = device_guide_map(copy_image(rgba, w, h), copy_image(target_rgba, tw, th), sg.s);
+    memcpy(out_rgba, g.px.data(), g.px.size());
   } catch (const Failure &f) {
     return f.status;
   }
@@ -659,11 +742,6 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
   }
   rc = check_limits(*b, W, H, b->err);
   if (rc) return rc;
-  if (b->has_target && num_guides == 0) {
-    b->err = "style transfer (a target guide without example guides) needs automatic guide maps, which this "
-             "library does not build; pass example guides";
-    return TS_ERR_UNSUPPORTED;
-  }
   std::unique_ptr<ts_session> s(new (std::nothrow) ts_session());
   if (!s) return TS_ERR_OUT_OF_MEMORY;
   s->prm = p;
@@ -678,14 +756,18 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
     CUDA_TRY(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
     const cudaStream_t st = sg.s;
     CUDA_TRY(configure_kernels(p.k, (uint32_t)p.m));
-    // inputs at their final sizes (Example::resolve, lib.rs:564-603)
+    // the target guide at the output size (session.rs:258-266), then the
+    // inputs at their final sizes (Example::resolve, lib.rs:564-603);
+    // examples without a guide get the automatic one (lib.rs:575-582)
+    Image tg;
+    if (s->guided) tg = load_image(b->target, true, W, H, st);
     std::vector<Image> imgs(s->n_ex), guides(s->n_ex), masks(s->n_ex);
     for (uint32_t e = 0; e < s->n_ex; ++e) {
       const ExampleIn &ex = b->examples[e];
       imgs[e] = load_image(ex.img, has_in, in_w, in_h, st);
       if (imgs[e].w > kMaxSide || imgs[e].h > kMaxSide) throw Failure{TS_ERR_LIMIT, "example side exceeds limit"};
       if (s->guided) {
-        guides[e] = load_image(ex.guide, has_in, in_w, in_h, st);
+        guides[e] = ex.has_guide ? load_image(ex.guide, has_in, in_w, in_h, st) : device_guide_map(imgs[e], tg, st);
         if (guides[e].w > kMaxSide || guides[e].h > kMaxSide) throw Failure{TS_ERR_LIMIT, "guide side exceeds limit"};
       }
       if (ex.method == TS_SAMPLE_IMAGE) {
@@ -792,7 +874,6 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
                      st);
       }
       CUDA_TRY(cudaGetLastError());
-      Image tg = load_image(b->target, true, W, H, st);
       CUDA_TRY(s->tguide.alloc((size_t)W * H * s->n_levels));
       device_pyramid(tg, p.backtrack_stages, s->tguide.p, st);
     }
