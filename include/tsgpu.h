@@ -138,6 +138,9 @@ typedef struct ts_run_stats {
    * kind, indexed by TS_KERNEL_*. */
   uint64_t kernel_count[8];
   double kernel_ms[8];
+  /* Host time of run(): schedule planning, device allocation, enqueueing
+   * uploads and launches, waiting for the device, converting the results. */
+  double host_plan_ms, host_alloc_ms, host_enqueue_ms, host_wait_ms, host_finish_ms;
 } ts_run_stats;
 
 const char *ts_status_str(int status);

@@ -76,7 +76,9 @@ KERNEL_KINDS = ("random_candidates", "knn_walk", "knn_exhaustive", "resolve", "c
 class RunStats(C.Structure):
     _fields_ = [("resolves", C.c_uint64), ("cost_evals", C.c_uint64), ("batches", C.c_uint64),
                 ("stages", C.c_uint64), ("kernel_launches", C.c_uint64), ("gpu_ms", C.c_double),
-                ("wall_ms", C.c_double), ("kernel_count", C.c_uint64 * 8), ("kernel_ms", C.c_double * 8)]
+                ("wall_ms", C.c_double), ("kernel_count", C.c_uint64 * 8), ("kernel_ms", C.c_double * 8),
+                ("host_plan_ms", C.c_double), ("host_alloc_ms", C.c_double), ("host_enqueue_ms", C.c_double),
+                ("host_wait_ms", C.c_double), ("host_finish_ms", C.c_double)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_ if not f.startswith("kernel_") or f == "kernel_launches"}

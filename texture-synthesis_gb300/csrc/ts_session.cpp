@@ -168,6 +168,21 @@ struct DevBuf {
   size_t bytes() const { return p ? n * sizeof(T) : 0; }
 };
 
+// Page-locked host memory (cudaMallocHost), for copies that must not wait.
+template <typename T>
+struct PinnedBuf {
+  T *p = nullptr;
+  PinnedBuf() = default;
+  PinnedBuf(const PinnedBuf &) = delete;
+  PinnedBuf &operator=(const PinnedBuf &) = delete;
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  cudaError_t alloc(size_t count) {
+    return cudaMallocHost((void **)&p, (count ? count : 1) * sizeof(T));
+  }
+};
+
 struct StreamGuard {
   cudaStream_t s = nullptr;
   ~StreamGuard() {
@@ -1023,6 +1038,9 @@ struct RunCtx {
   uint64_t overall_total = 0;
   uint32_t max_batch_items = 1;
   uint64_t rc_items = 1;
+  size_t res_total = 0;                // resolved-list length at the end of the run
+  std::vector<uint32_t> unresolved;    // pixels not yet picked (the pick chain's state)
+  size_t picked_stages = 0;            // stages whose items are known
   int32_t x_l = 0, y_b = 0;
   uint64_t dev_bytes = 0;  // device memory run_alloc takes
   // device state
@@ -1062,7 +1080,8 @@ void run_plan(ts_session *s, RunCtx &c) {
   std::vector<uint32_t> &resolved = c.resolved;
   color.assign(N, 0);
   state.assign(N, make_uint4(0, 0, 0, 0));
-  std::vector<uint32_t> unresolved;
+  std::vector<uint32_t> &unresolved = c.unresolved;
+  unresolved.clear();
   size_t locked = 0;
   if (s->inpaint) {
     for (size_t i = 0; i < N; ++i) {
@@ -1126,6 +1145,8 @@ void run_plan(ts_session *s, RunCtx &c) {
   std::vector<uint32_t> &items = c.items;
   std::vector<float> &luts = c.luts;
   size_t n_res = resolved.size();
+  size_t n_unresolved = unresolved.size();
+  size_t n_items_total = 0;
   int32_t pyramid_level = 0;
   uint32_t max_batch_items = 1, max_stage_items = 1;
   c.tab = knn_table(kKnnTabRadius);
@@ -1159,17 +1180,13 @@ void run_plan(ts_session *s, RunCtx &c) {
       slow |= !std::isfinite(gv);
     }
     sp.slow_lut = slow;
-    const size_t P_eff = std::min(P, redo + unresolved.size());
-    sp.items_off = (uint32_t)items.size();
+    const size_t P_eff = std::min(P, redo + n_unresolved);
+    sp.items_off = (uint32_t)n_items_total;
     sp.n_items = (uint32_t)P_eff;
     sp.redo = (uint32_t)redo;
     sp.n_res_start = (uint32_t)n_res;
-    for (size_t i = 0; i < P_eff; ++i) {
-      if (i < redo)
-        items.push_back(resolved[i + locked]);
-      else
-        items.push_back(pick(sp.seed + (uint64_t)i));
-    }
+    n_items_total += P_eff;
+    n_unresolved -= P_eff > redo ? P_eff - redo : 0;
     size_t i = 0, R = n_res;
     while (i < P_eff) {
       size_t bsz = 1;
@@ -1189,9 +1206,7 @@ void run_plan(ts_session *s, RunCtx &c) {
       // fewer than k points expected within the offset table: straight to
       // the cell grid
       bp.grid_first = k > 0 && !bp.exhaustive && (double)R * tab.size() < (double)k * (double)N;
-      const size_t appended = bp.i1 - bp.append_from;
-      for (size_t t = bp.append_from; t < bp.i1; ++t) resolved.push_back(items[sp.items_off + t]);
-      R += appended;
+      R += bp.i1 - bp.append_from;
       sp.batches.push_back(bp);
       max_batch_items = std::max<uint32_t>(max_batch_items, (uint32_t)bsz);
       i += bsz;
@@ -1200,6 +1215,10 @@ void run_plan(ts_session *s, RunCtx &c) {
     max_stage_items = std::max<uint32_t>(max_stage_items, (uint32_t)P_eff);
     plan.push_back(std::move(sp));
   }
+  // the items themselves come from the pick chain, stage by stage (run_pick)
+  items.assign(n_items_total, 0);
+  c.res_total = n_res;
+  c.picked_stages = 0;
   // ---- host tables ----
   const uint32_t wpr = (W + 31) / 32;
   for (auto &sp : plan) c.n_batches += sp.batches.size();
@@ -1259,11 +1278,37 @@ void run_plan(ts_session *s, RunCtx &c) {
   const size_t kk = std::max<uint32_t>(k, 1), mb = max_batch_items;
   uint64_t steps_est = 0;
   for (auto &sp : plan) steps_est += sp.batches.size() + 1;
-  c.dev_bytes = N * 4 + N * sizeof(uint4) + 2 * (uint64_t)wpr * H * 4 + resolved.size() * 8 + items.size() * 4 +
+  c.dev_bytes = N * 4 + N * sizeof(uint4) + 2 * (uint64_t)wpr * H * 4 + c.res_total * 8 + items.size() * 4 +
                 c.luts.size() * 4 + c.tab.size() * 4 + mb * kk * 12 + mb * (4 + 8 + 4 + sizeof(Result)) +
                 c.n_batches * 4 + std::max<uint64_t>(c.rc_items, mb) * m * 8 +
                 (c.xdiv.size() + c.ydiv.size() + c.dxt.size() + c.dy2t.size()) * 8 + steps_est * sizeof(StepDev) +
                 c.cells.size() * 4;
+}
+
+// The pick chain of the next stage (pick_random_unresolved, ms.rs:380-389,
+// redo items first, ms.rs:905-915): fills its items and extends the
+// resolved list with each batch's appended items, in the reference's order.
+void run_pick(RunCtx &c) {
+  const StagePlan &sp = c.plan[c.picked_stages++];
+  std::vector<uint32_t> &unresolved = c.unresolved;
+  uint32_t *it = c.items.data() + sp.items_off;
+  for (uint32_t i = 0; i < sp.n_items; ++i) {
+    if (i < sp.redo) {
+      it[i] = c.resolved[i + c.locked];
+    } else {
+      Pcg32 r = pcg_from_u64(sp.seed + (uint64_t)i);
+      const uint64_t idx = gen_range_u64(r, unresolved.size());
+      it[i] = unresolved[idx];
+      unresolved[idx] = unresolved.back();
+      unresolved.pop_back();
+    }
+  }
+  for (const BatchPlan &bp : sp.batches)
+    for (uint32_t t = bp.append_from; t < bp.i1; ++t) c.resolved.push_back(it[t]);
+}
+
+void run_pick_all(RunCtx &c) {
+  while (c.picked_stages < c.plan.size()) run_pick(c);
 }
 
 // Device buffers of a run and the step descriptors that point into them.
@@ -1287,8 +1332,8 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   CUDA_TRY(A(c.d_state, N));
   CUDA_TRY(A(c.d_occ, (size_t)wpr * H));
   CUDA_TRY(A(c.d_mir, (size_t)wpr * H));
-  CUDA_TRY(A(c.d_res, c.resolved.size()));
-  CUDA_TRY(A(c.d_rscore, c.resolved.size()));
+  CUDA_TRY(A(c.d_res, c.res_total));
+  CUDA_TRY(A(c.d_rscore, c.res_total));
   CUDA_TRY(A(c.d_items, c.items.size()));
   CUDA_TRY(A(c.d_lut, c.luts.size()));
   CUDA_TRY(A(c.d_tab, c.tab.size()));
@@ -1436,8 +1481,8 @@ void run_upload(RunCtx &c, cudaStream_t st) {
   CUDA_TRY(cudaMemcpyAsync(c.d_occ.p, c.occ.data(), c.occ.size() * 4, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(c.d_mir.p, c.mir.data(), c.mir.size() * 4, cudaMemcpyHostToDevice, st));
   if (c.locked) CUDA_TRY(cudaMemcpyAsync(c.d_res.p, c.resolved.data(), c.locked * 4, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemsetAsync(c.d_rscore.p, 0, c.resolved.size() * 4, st));
-  if (!c.items.empty())
+  CUDA_TRY(cudaMemsetAsync(c.d_rscore.p, 0, c.res_total * 4, st));
+  if (!c.items.empty() && c.picked_stages == c.plan.size())
     CUDA_TRY(cudaMemcpyAsync(c.d_items.p, c.items.data(), c.items.size() * 4, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(c.d_lut.p, c.luts.data(), c.luts.size() * 4, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(c.d_tab.p, c.tab.data(), c.tab.size() * 4, cudaMemcpyHostToDevice, st));
@@ -1451,13 +1496,18 @@ void run_upload(RunCtx &c, cudaStream_t st) {
   CUDA_TRY(cudaMemsetAsync(c.d_evals.p, 0, sizeof(unsigned long long), st));
 }
 
-// The plain path: one session's launches, step by step.
-void run_enqueue_plain(RunCtx &c, cudaStream_t st, LaunchTimer &lt, ts_progress_fn progress, void *user) {
+// The plain path: one session's launches, step by step (only those of
+// stage `stage` when it is not negative).
+void run_enqueue_plain(RunCtx &c, cudaStream_t st, LaunchTimer &lt, ts_progress_fn progress, void *user,
+                       int stage = -1) {
   const SessionDev &sd = c.sd;
   const uint32_t k = c.k;
   uint64_t overall_current = 0;
+  for (const StagePlan &sp : c.plan)
+    if (stage >= 0 && (&sp - c.plan.data()) < stage) overall_current += sp.n_items;
   std::vector<uint8_t> prog_img;
   for (const Step &stp : c.steps) {
+    if (stage >= 0 && stp.stage != stage) continue;
     const StagePlan &sp = c.plan[stp.stage];
     lt.stage = sp.p_stage;
     lt.items = sp.n_items;
@@ -1521,13 +1571,13 @@ void run_readback(RunCtx &c, cudaStream_t st) {
   ts_generated *g = c.g.get();
   c.col.resize(c.N);
   c.stv.resize(c.N);
-  g->resolved.resize(c.resolved.size());
-  g->scores.resize(c.resolved.size());
+  g->resolved.resize(c.res_total);
+  g->scores.resize(c.res_total);
   CUDA_TRY(cudaMemcpyAsync(&c.evals, c.d_evals.p, sizeof(c.evals), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaMemcpyAsync(c.col.data(), c.d_color.p, c.N * 4, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaMemcpyAsync(c.stv.data(), c.d_state.p, c.N * sizeof(uint4), cudaMemcpyDeviceToHost, st));
-  CUDA_TRY(cudaMemcpyAsync(g->resolved.data(), c.d_res.p, c.resolved.size() * 4, cudaMemcpyDeviceToHost, st));
-  CUDA_TRY(cudaMemcpyAsync(g->scores.data(), c.d_rscore.p, c.resolved.size() * 4, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(g->resolved.data(), c.d_res.p, c.res_total * 4, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(g->scores.data(), c.d_rscore.p, c.res_total * 4, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaMemcpyAsync(&c.derr, c.d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
 }
 
@@ -1598,8 +1648,21 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     StreamGuard sg;
     CUDA_TRY(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
     const cudaStream_t st = sg.s;
+    auto t = std::chrono::steady_clock::now();
+    auto lap = [&]() {
+      const auto n = std::chrono::steady_clock::now();
+      const double ms = std::chrono::duration<double, std::milli>(n - t).count();
+      t = n;
+      return ms;
+    };
     run_plan(s, c);
+    const double plan_ms = lap();
     run_alloc(c, nullptr);
+    // the items go up stage by stage from pinned memory, so that the device
+    // runs a stage while the host picks the next one
+    PinnedBuf<uint32_t> pitems;
+    CUDA_TRY(pitems.alloc(c.items.size()));
+    const double alloc_ms = lap();
     EventPair ev;
     ev.create();
     CUDA_TRY(cudaEventRecord(ev.a, st));
@@ -1607,11 +1670,27 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     LaunchTimer lt;
     lt.on = s->prm.profile;
     lt.st = st;
-    run_enqueue_plain(c, st, lt, progress, user);
+    for (size_t si = 0; si < c.plan.size(); ++si) {
+      run_pick(c);
+      const StagePlan &sp = c.plan[si];
+      if (sp.n_items) {
+        memcpy(pitems.p + sp.items_off, c.items.data() + sp.items_off, (size_t)sp.n_items * 4);
+        CUDA_TRY(cudaMemcpyAsync(c.d_items.p + sp.items_off, pitems.p + sp.items_off, (size_t)sp.n_items * 4,
+                                 cudaMemcpyHostToDevice, st));
+      }
+      run_enqueue_plain(c, st, lt, progress, user, (int)si);
+    }
     run_readback(c, st);
     CUDA_TRY(cudaEventRecord(ev.b, st));
+    const double enqueue_ms = lap();
     CUDA_TRY(cudaStreamSynchronize(st));
+    const double wait_ms = lap();
     run_finish(c);
+    c.g->stats.host_plan_ms = plan_ms;
+    c.g->stats.host_alloc_ms = alloc_ms;
+    c.g->stats.host_enqueue_ms = enqueue_ms;
+    c.g->stats.host_wait_ms = wait_ms;
+    c.g->stats.host_finish_ms = lap();
     c.g->stats.gpu_ms = ev.ms();
     lt.collect(c.g->stats, c.g->launches);
   } catch (const Failure &f) {
@@ -1825,6 +1904,7 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
           try {
             ctx[j].reset(new RunCtx());
             run_plan(sessions[j], *ctx[j]);
+            run_pick_all(*ctx[j]);
             run_alloc(*ctx[j], nullptr);
           } catch (const Failure &f) {
             fails[j] = f;
@@ -2455,6 +2535,7 @@ int ts_server_submit(ts_server *S, ts_session *s, uint64_t *ticket) {
   r->c.reset(new RunCtx());
   try {
     run_plan(r->s, *r->c);  // host schedule, on the caller's thread
+    run_pick_all(*r->c);
   } catch (const Failure &f) {
     S->err = f.msg;
     return f.status;
