@@ -48,6 +48,7 @@ constexpr int kResolveWarps = 4;
 constexpr int kWalkWarps = 8;
 constexpr int kExhThreads = 256;
 constexpr int kTeamThreads = 128;
+constexpr int kTeamFullThreads = 256;  // the full-evaluation form: batches of at most ~1000 items
 constexpr int kExhCap = 2048;      // keys kept by the exhaustive k-NN at the cut distance
 constexpr int kExhAllKeys = 8192;  // keys the exhaustive k-NN sorts in shared memory directly
 constexpr uint32_t kMaxDraws = 1u << 22;
@@ -306,8 +307,13 @@ __device__ __forceinline__ void block_bitonic(unsigned long long *keys, uint32_t
 // point with d2 < (r * kCell + 1)^2 has been seen (the cells beyond are that
 // far away in x or y), so the k smallest collected keys are then the k
 // nearest points under the tie rule; a ring wholly outside the grid means
-// every point has been seen.  Leaves the count in sh.total (above
-// kExhAllKeys: the buffer overflowed) and the OR of the d2 in sh.prefix.
+// every point has been seen.  The cells of consecutive rings are numbered
+// 0, 1.. (ring r starts at 4r(r-1) + 1) and taken blockDim.x at a time; the
+// bound is tested after each such round for the last ring it completed.
+// Leaves the count in sh.total (above kExhAllKeys: the buffer overflowed)
+// and the OR of the d2 in sh.prefix.
+__device__ __forceinline__ uint32_t ring_base(uint32_t r) { return r == 0 ? 0u : 4u * r * (r - 1u) + 1u; }
+
 __device__ void grid_collect(const SessionDev &s, int px, int py, uint32_t k, ExhShared &sh,
                              unsigned long long *all) {
   if (threadIdx.x == 0) {
@@ -318,54 +324,63 @@ __device__ void grid_collect(const SessionDev &s, int px, int py, uint32_t k, Ex
   }
   __syncthreads();
   const int qcx = (px - s.cox) / kCell, qcy = (py - s.coy) / kCell;
-  for (int r = 0;; ++r) {
-    const int ring = r == 0 ? 1 : 8 * r;
+  // rings wholly outside the grid start beyond the farthest grid edge
+  const uint32_t r_max = (uint32_t)max(max(qcx, (int)s.cgw - 1 - qcx), max(qcy, (int)s.cgh - 1 - qcy));
+  const uint32_t f_end_all = ring_base(r_max + 1);
+  for (uint32_t f0 = 0; f0 < f_end_all; f0 += blockDim.x) {
+    const uint32_t f = f0 + threadIdx.x;
     uint32_t dor = 0;
-    for (int i0 = 0; i0 < ring; i0 += (int)blockDim.x) {
-      const int i = i0 + (int)threadIdx.x;
-      if (i >= ring) continue;
+    if (f < f_end_all) {
+      // ring r of cell number f: 4r(r-1) + 1 <= f < 4r(r+1) + 1
+      uint32_t r = f == 0 ? 0u : (uint32_t)(sqrtf((float)(f - 1) * 0.25f + 0.25f) + 0.5f);
+      while (r > 0 && ring_base(r) > f) --r;
+      while (ring_base(r + 1) <= f) ++r;
       int gx, gy;
-      ring_cell(r, i, gx, gy);
+      ring_cell((int)r, (int)(f - ring_base(r)), gx, gy);
       gx += qcx;
       gy += qcy;
-      if ((unsigned)gx >= s.cgw || (unsigned)gy >= s.cgh) continue;
-      sh.flag = 1;
-      const uint32_t cnt = __ldg(&s.cells[(size_t)gy * s.cgw + gx]);
-      if (cnt == 0) continue;
-      const int x0 = s.cox + gx * kCell, y0 = s.coy + gy * kCell;
-      uint32_t found = 0;
-      for (int yy = 0; yy < kCell && found < cnt; ++yy) {
-        const int y = y0 + yy, dy = y - py;
-        uint32_t bits;
-        if ((unsigned)y < s.H && x0 >= 0 && x0 + kCell <= (int)s.W) {
-          const uint32_t wi = (uint32_t)x0 >> 5, sh5 = (uint32_t)x0 & 31u;
-          const uint32_t *row = s.occ + (size_t)y * s.wpr;
-          uint64_t wv = __ldg(&row[wi]);
-          if (sh5 + kCell > 32) wv |= (uint64_t)__ldg(&row[wi + 1]) << 32;
-          bits = (uint32_t)(wv >> sh5) & ((1u << kCell) - 1u);
-        } else {
-          bits = 0;
-          for (int xx = 0; xx < kCell; ++xx)
-            if (occupied(s, x0 + xx, y)) bits |= 1u << xx;
-        }
-        while (bits) {
-          const int bp = __ffs(bits) - 1;
-          bits &= bits - 1u;
-          const int x = x0 + bp, dx = x - px;
-          const uint32_t d2 = (uint32_t)(dx * dx + dy * dy);
-          dor |= d2;
-          const uint32_t slot = atomicAdd(&sh.total, 1u);
-          if (slot < (uint32_t)kExhAllKeys) all[slot] = nb_key(d2, x, y);
-          ++found;
+      const uint32_t cnt =
+          ((unsigned)gx < s.cgw && (unsigned)gy < s.cgh) ? __ldg(&s.cells[(size_t)gy * s.cgw + gx]) : 0u;
+      if (cnt) {
+        const int x0 = s.cox + gx * kCell, y0 = s.coy + gy * kCell;
+        uint32_t found = 0;
+        for (int yy = 0; yy < kCell && found < cnt; ++yy) {
+          const int y = y0 + yy, dy = y - py;
+          uint32_t bits;
+          if ((unsigned)y < s.H && x0 >= 0 && x0 + kCell <= (int)s.W) {
+            const uint32_t wi = (uint32_t)x0 >> 5, sh5 = (uint32_t)x0 & 31u;
+            const uint32_t *row = s.occ + (size_t)y * s.wpr;
+            uint64_t wv = __ldg(&row[wi]);
+            if (sh5 + kCell > 32) wv |= (uint64_t)__ldg(&row[wi + 1]) << 32;
+            bits = (uint32_t)(wv >> sh5) & ((1u << kCell) - 1u);
+          } else {
+            bits = 0;
+            for (int xx = 0; xx < kCell; ++xx)
+              if (occupied(s, x0 + xx, y)) bits |= 1u << xx;
+          }
+          while (bits) {
+            const int bp = __ffs(bits) - 1;
+            bits &= bits - 1u;
+            const int x = x0 + bp, dx = x - px;
+            const uint32_t d2 = (uint32_t)(dx * dx + dy * dy);
+            dor |= d2;
+            const uint32_t slot = atomicAdd(&sh.total, 1u);
+            if (slot < (uint32_t)kExhAllKeys) all[slot] = nb_key(d2, x, y);
+            ++found;
+          }
         }
       }
     }
     if (dor) atomicOr(&sh.prefix, dor);
     __syncthreads();
     const uint32_t n = sh.total;
-    const bool any = sh.flag != 0;
-    if (n > (uint32_t)kExhAllKeys || !any) break;
-    const uint32_t lim = (uint32_t)(r * kCell + 1) * (uint32_t)(r * kCell + 1);
+    if (n > (uint32_t)kExhAllKeys) break;
+    // the last ring this round completed
+    const uint32_t f_done = min(f0 + blockDim.x, f_end_all);
+    uint32_t r_done = 0;
+    while (ring_base(r_done + 2) <= f_done) ++r_done;
+    if (ring_base(r_done + 1) > f_done) continue;  // not even ring 0 complete (cannot happen)
+    const uint32_t lim = (uint32_t)(r_done * kCell + 1) * (uint32_t)(r_done * kCell + 1);
     uint32_t c = 0;
     for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) c += (uint32_t)(all[e] >> 32) < lim ? 1u : 0u;
 #pragma unroll
@@ -373,12 +388,9 @@ __device__ void grid_collect(const SessionDev &s, int px, int py, uint32_t k, Ex
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(&sh.cnt, c);
     __syncthreads();
     const uint32_t lt = sh.cnt;
-    __syncthreads();  // every thread has read flag and cnt
+    __syncthreads();  // every thread has read cnt
     if (lt >= k) break;
-    if (threadIdx.x == 0) {
-      sh.flag = 0;
-      sh.cnt = 0;
-    }
+    if (threadIdx.x == 0) sh.cnt = 0;
     __syncthreads();
   }
 }
@@ -1219,10 +1231,52 @@ __device__ __forceinline__ void resolve_team_body(const SessionDev &s, const Sta
     const uint32_t nc = ncoh + s.m;
     float best_s = FLT_MAX;
     uint32_t best_i = 0;
-    if (!slow && kFull) {
-      // every term nps(c, j) * w_j in parallel (consecutive threads take
-      // consecutive neighbours of one candidate), then each candidate's
-      // in-order sum on one thread: the reference's scores, all of them
+    if (!slow && kFull && padded) {
+      // every term nps(c, j) * w_j in parallel, then each candidate's
+      // in-order sum on one thread: the reference's scores, all of them.
+      // Padded planes: each candidate's plane offset once, then four texel
+      // loads in flight per thread before their terms are formed.
+      unsigned long long *cb = (unsigned long long *)(term + (((size_t)nk * nc + 1) & ~(size_t)1));
+      for (uint32_t c = tid; c < nc; c += T) {
+        const uint32_t cxy = w.cxy[c], aux = w.caux[c];
+        const MapDesc md = s.maps[aux & 0x7fffu];
+        const unsigned long long off = md.poff + (unsigned long long)st.level * md.pw * md.ph +
+                                       (unsigned long long)((cxy >> 16) + kPad) * md.pw + ((cxy & 0xffffu) + kPad);
+        cb[c] = off | ((aux & kAuxNeg) ? (1ull << 63) : 0ull);
+      }
+      __syncthreads();
+      const uint32_t total = nc * nk;
+      for (uint32_t i0 = tid; i0 < total; i0 += 4 * T) {
+        uint32_t tx[4], gx[4], ii[4], jj[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const uint32_t i = i0 + (uint32_t)u * T;
+          ii[u] = i;
+          if (i < total) {
+            const uint32_t c = i / nk;
+            jj[u] = i - c * nk;
+            const unsigned long long v = cb[c];
+            const int lin = (v >> 63) ? -w.lin[jj[u]] : w.lin[jj[u]];
+            const size_t off = (size_t)(v & 0x7fffffffffffffffull) + lin;
+            tx[u] = __ldg(s.plevels + off);
+            if (s.guided) gx[u] = __ldg(s.pguides + off);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (ii[u] < total) {
+            const uint4 nr = w.nbr[jj[u]];
+            float nps = lut4(lc, __vabsdiffu4(nr.y, tx[u]), 0.0f);
+            if (s.guided) nps = lut4(lg, __vabsdiffu4(nr.z, gx[u]), nps);
+            term[ii[u]] = __fmul_rn(nps, __uint_as_float(nr.w));
+          }
+        }
+      }
+    }
+    if (!slow && kFull && !padded) {
+      // the same with bounds-checked gathers (far neighbours or guides of
+      // other sizes); consecutive threads take consecutive neighbours of one
+      // candidate
       uint32_t c = tid / nk, j = tid - c * nk;
       const uint32_t dc = T / nk, dj = T - dc * nk;
       for (uint32_t i = tid; i < nc * nk; i += T) {
@@ -1252,6 +1306,8 @@ __device__ __forceinline__ void resolve_team_body(const SessionDev &s, const Sta
           ++c;
         }
       }
+    }
+    if (!slow && kFull) {
       __syncthreads();
       float my_s = FLT_MAX;
       uint32_t my_i = 0xffffffffu;
@@ -1768,7 +1824,8 @@ size_t resolve_smem_bytes(uint32_t k, uint32_t m, int) { return 2048 + (size_t)k
 static size_t team_smem_bytes(uint32_t k, uint32_t m) { return 2048 + warp_smem_bytes(k, m) + (size_t)(k ? k : 1) * 4; }
 // the full-evaluation team form keeps every (candidate, neighbour) term
 static size_t team_full_smem_bytes(uint32_t k, uint32_t m) {
-  return 2048 + warp_smem_bytes(k, m) + (size_t)(k ? k : 1) * (k + m) * 4;
+  const size_t kk = k ? k : 1;
+  return 2048 + warp_smem_bytes(k, m) + ((kk * (k + m) * 4 + 7) & ~(size_t)7) + (size_t)(k + m) * 8;
 }
 constexpr size_t kTeamFullMaxSmem = 96 * 1024;
 
@@ -1789,7 +1846,7 @@ cudaError_t configure_kernels(uint32_t k, uint32_t m) {
   }
   const size_t fsm = team_full_smem_bytes(k, m);
   if (fsm > 48 * 1024 && fsm <= kTeamFullMaxSmem)
-    return cudaFuncSetAttribute(k_resolve_team<kTeamThreads, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(k_resolve_team<kTeamFullThreads, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)fsm);
   return cudaSuccess;
 }
@@ -1802,7 +1859,7 @@ cudaError_t set_multi_smem(int phase, size_t bytes) {
     case kPhaseExhaustive: return cudaFuncSetAttribute(k_knn_exhaustive_multi, a, v);
     case kPhaseResolve: return cudaFuncSetAttribute(k_resolve_multi, a, v);
     case kPhaseTeamPart: return cudaFuncSetAttribute(k_resolve_team_multi<kTeamThreads, false>, a, v);
-    case kPhaseTeamFull: return cudaFuncSetAttribute(k_resolve_team_multi<kTeamThreads, true>, a, v);
+    case kPhaseTeamFull: return cudaFuncSetAttribute(k_resolve_team_multi<kTeamFullThreads, true>, a, v);
     default: return cudaSuccess;
   }
 }
@@ -1818,8 +1875,8 @@ uint32_t multi_threads(int phase) {
     case kPhaseExhaustive: return kExhThreads;
     case kPhaseMean: return 128;
     case kPhaseResolve: return kResolveWarps * kWarp;
-    case kPhaseTeamPart:
-    case kPhaseTeamFull: return kTeamThreads;
+    case kPhaseTeamPart: return kTeamThreads;
+    case kPhaseTeamFull: return kTeamFullThreads;
     default: return 256;
   }
 }
@@ -1866,7 +1923,7 @@ void launch_multi(int phase, const MultiLaunch &ml, uint32_t blocks, size_t smem
     case kPhaseMean: launch_pdl(k_mean_multi, blocks, t, 0, stream, ml); break;
     case kPhaseResolve: launch_pdl(k_resolve_multi, blocks, t, smem, stream, ml); break;
     case kPhaseTeamPart: launch_pdl(k_resolve_team_multi<kTeamThreads, false>, blocks, t, smem, stream, ml); break;
-    case kPhaseTeamFull: launch_pdl(k_resolve_team_multi<kTeamThreads, true>, blocks, t, smem, stream, ml); break;
+    case kPhaseTeamFull: launch_pdl(k_resolve_team_multi<kTeamFullThreads, true>, blocks, t, smem, stream, ml); break;
     case kPhaseCommit: launch_pdl(k_commit_multi, blocks, t, 0, stream, ml); break;
     default: break;
   }
@@ -1910,7 +1967,8 @@ void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev
   if (n == 0) return;
   const uint32_t grid = n < 152u * 16u ? n : 152u * 16u;
   if (full && team_full_smem_bytes(s.k, s.m) <= kTeamFullMaxSmem)
-    launch_pdl(k_resolve_team<kTeamThreads, true>, grid, kTeamThreads, team_full_smem_bytes(s.k, s.m), stream, s, st, b);
+    launch_pdl(k_resolve_team<kTeamFullThreads, true>, grid, kTeamFullThreads, team_full_smem_bytes(s.k, s.m), stream, s,
+               st, b);
   else
     launch_pdl(k_resolve_team<kTeamThreads, false>, grid, kTeamThreads, team_smem_bytes(s.k, s.m), stream, s, st, b);
 }
