@@ -179,21 +179,26 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
     const double x2 = s.xdiv[px + s.xdiv_off], y2 = s.ydiv[py + s.ydiv_off];
     int32_t *nbo = b.nbuf + (size_t)local * s.k;
     uint32_t count = 0;
-    for (uint32_t c = 0; c < (b.grid_first ? 0u : s.knn_tab_n); c += kWarp) {
-      const uint32_t idx = c + lane;
-      bool hit = false;
-      int32_t off = 0;
-      if (idx < s.knn_tab_n) {
-        off = __ldg(&s.knn_tab[idx]);
-        hit = occupied(s, px + off_dx(off), py + off_dy(off));
+    // 64 table entries per round, two per lane, both looked up before either
+    // is used
+    for (uint32_t c = 0; c < (b.grid_first ? 0u : s.knn_tab_n); c += 2 * kWarp) {
+      const uint32_t i0 = c + lane, i1 = c + kWarp + lane;
+      const int32_t o0 = i0 < s.knn_tab_n ? __ldg(&s.knn_tab[i0]) : 0;
+      const int32_t o1 = i1 < s.knn_tab_n ? __ldg(&s.knn_tab[i1]) : 0;
+      const bool h0 = i0 < s.knn_tab_n && occupied(s, px + off_dx(o0), py + off_dy(o0));
+      const bool h1 = i1 < s.knn_tab_n && occupied(s, px + off_dx(o1), py + off_dy(o1));
+      const uint32_t b0 = __ballot_sync(0xffffffffu, h0);
+      const uint32_t b1 = __ballot_sync(0xffffffffu, h1);
+      const uint32_t r0 = count + __popc(b0 & lt), r1 = count + __popc(b0) + __popc(b1 & lt);
+      if (h0 && r0 < s.k) {
+        nbo[r0] = o0;
+        b.dist[(size_t)r0 * nb + local] = neighbour_dist(s, px, py, off_dx(o0), off_dy(o0), x2, y2);
       }
-      const uint32_t bal = __ballot_sync(0xffffffffu, hit);
-      const uint32_t rank = count + __popc(bal & lt);
-      if (hit && rank < s.k) {
-        nbo[rank] = off;
-        b.dist[(size_t)rank * nb + local] = neighbour_dist(s, px, py, off_dx(off), off_dy(off), x2, y2);
+      if (h1 && r1 < s.k) {
+        nbo[r1] = o1;
+        b.dist[(size_t)r1 * nb + local] = neighbour_dist(s, px, py, off_dx(o1), off_dy(o1), x2, y2);
       }
-      count += __popc(bal);
+      count += __popc(b0) + __popc(b1);
       if (count >= s.k) break;
     }
     if (lane == 0) {
