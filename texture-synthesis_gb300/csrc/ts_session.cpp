@@ -183,6 +183,26 @@ struct PinnedBuf {
   }
 };
 
+// An owned CUDA event (movable).
+struct EventHandle {
+  cudaEvent_t e = nullptr;
+  EventHandle() = default;
+  EventHandle(const EventHandle &) = delete;
+  EventHandle &operator=(const EventHandle &) = delete;
+  EventHandle(EventHandle &&o) noexcept : e(o.e) { o.e = nullptr; }
+  EventHandle &operator=(EventHandle &&o) noexcept {
+    if (this != &o) {
+      if (e) cudaEventDestroy(e);
+      e = o.e;
+      o.e = nullptr;
+    }
+    return *this;
+  }
+  ~EventHandle() {
+    if (e) cudaEventDestroy(e);
+  }
+};
+
 struct StreamGuard {
   cudaStream_t s = nullptr;
   ~StreamGuard() {
@@ -212,35 +232,54 @@ Image copy_image(const uint8_t *p, uint32_t w, uint32_t h) {
   return im;
 }
 
-// Upload taps of one axis: {left, count, offset} per output + weights.
-struct DevTaps {
-  DevBuf<uint4> taps;
-  DevBuf<float> wts;
+// Device copies of filter taps, kept per (device, filter, sigma, lengths)
+// for the life of the process: the same resizes recur for every example of
+// a size and every level of a pyramid.  kBlurFilter marks imageops::blur's
+// Gaussian of standard deviation sigma.
+constexpr int kBlurFilter = -1;
+
+struct DevTapsRef {
+  const uint4 *taps;
+  const float *wts;
 };
-void upload_taps(const Taps &t, DevTaps &d, cudaStream_t st) {
+
+DevTapsRef cached_taps(int filter, float sigma, uint32_t in_len, uint32_t out_len) {
+  static std::mutex mu;
+  static std::unordered_map<std::string, DevTapsRef> cache;
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  uint32_t sb = 0;
+  memcpy(&sb, &sigma, 4);
+  const std::string key = std::to_string(dev) + "/" + std::to_string(filter) + "/" + std::to_string(sb) + "/" +
+                          std::to_string(in_len) + "/" + std::to_string(out_len);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  const Taps t = filter == kBlurFilter ? blur_taps(in_len, sigma) : axis_taps((Filter)filter, in_len, out_len);
   std::vector<uint4> v(t.left.size());
   for (size_t i = 0; i < v.size(); ++i) v[i] = make_uint4(t.left[i], t.count[i], t.offset[i], 0);
-  CUDA_TRY(d.taps.alloc_on(v.size(), st));
-  CUDA_TRY(d.wts.alloc_on(t.weights.size(), st));
-  if (!v.empty()) CUDA_TRY(cudaMemcpyAsync(d.taps.p, v.data(), v.size() * sizeof(uint4), cudaMemcpyHostToDevice, st));
+  uint4 *dt = nullptr;
+  float *dw = nullptr;
+  CUDA_TRY(cudaMalloc((void **)&dt, std::max<size_t>(1, v.size()) * sizeof(uint4)));
+  CUDA_TRY(cudaMalloc((void **)&dw, std::max<size_t>(1, t.weights.size()) * sizeof(float)));
+  if (!v.empty()) CUDA_TRY(cudaMemcpy(dt, v.data(), v.size() * sizeof(uint4), cudaMemcpyHostToDevice));
   if (!t.weights.empty())
-    CUDA_TRY(cudaMemcpyAsync(d.wts.p, t.weights.data(), t.weights.size() * 4, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpy(dw, t.weights.data(), t.weights.size() * sizeof(float), cudaMemcpyHostToDevice));
+  if (cache.size() > 4096) cache.clear();  // bounded; the dropped device copies stay allocated
+  return cache[key] = DevTapsRef{dt, dw};
 }
 
-// imageops::resize on the device: src (device u8, w x h) -> dst (device u8,
-// nw x nh), enqueued on st (its temporaries are freed in stream order).
-void device_resample(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uint32_t nw, uint32_t nh,
-                     const Taps &taps_v, const Taps &taps_h, cudaStream_t st) {
+void device_resample(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uint32_t nw, uint32_t nh, int filter,
+                     float sigma, cudaStream_t st) {
   if (nw == 0 || nh == 0) return;
-  DevTaps tv, th;
-  upload_taps(taps_v, tv, st);
-  upload_taps(taps_h, th, st);
+  const DevTapsRef tv = cached_taps(filter, sigma, h, nh);
+  const DevTapsRef th = cached_taps(filter, sigma, w, nw);
   DevBuf<float> tmp;
   CUDA_TRY(tmp.alloc_on((size_t)w * nh * 4, st));
   CUDA_TRY(cudaMemsetAsync(tmp.p, 0, (size_t)w * nh * 4 * sizeof(float), st));
-  if (h > 0) launch_resize_v(src, w, h, tmp.p, nh, tv.taps.p, tv.wts.p, st);
+  if (h > 0) launch_resize_v(src, w, h, tmp.p, nh, tv.taps, tv.wts, st);
   if (w > 0) {
-    launch_resize_h(tmp.p, w, nh, dst, nw, th.taps.p, th.wts.p, st);
+    launch_resize_h(tmp.p, w, nh, dst, nw, th.taps, th.wts, st);
   } else {
     CUDA_TRY(cudaMemsetAsync(dst, 0, (size_t)nw * nh * 4, st));
   }
@@ -249,8 +288,7 @@ void device_resample(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, u
 
 void device_resize(const uint8_t *src, uint32_t w, uint32_t h, uint8_t *dst, uint32_t nw, uint32_t nh, Filter f,
                    cudaStream_t st) {
-  if (nw == 0 || nh == 0) return;
-  device_resample(src, w, h, dst, nw, nh, axis_taps(f, h, nh), axis_taps(f, w, nw), st);
+  device_resample(src, w, h, dst, nw, nh, (int)f, 0.0f, st);
 }
 
 // transform_to_guide_map + match_histograms (utils.rs:101-183) on the device:
@@ -275,7 +313,7 @@ Image device_guide_map(const Image &img, const Image &target, cudaStream_t st) {
   CUDA_TRY(cudaMemcpyAsync(d_src.p, img.px.data(), n * 4, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(d_tgt.p, target.px.data(), nt * 4, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemsetAsync(d_hist.p, 0, 512 * 4, st));
-  device_resample(d_src.p, img.w, img.h, d_blur.p, img.w, img.h, blur_taps(img.h, 2.0f), blur_taps(img.w, 2.0f), st);
+  device_resample(d_src.p, img.w, img.h, d_blur.p, img.w, img.h, kBlurFilter, 2.0f, st);
   launch_luma_hist((const uint32_t *)d_blur.p, n, d_luma.p, d_hist.p, st);
   launch_hist_r(d_tgt.p, nt, d_hist.p + 256, st);
   uint32_t hist[512];
@@ -395,6 +433,7 @@ struct ts_session {
   DevBuf<uint8_t> masks;
   DevBuf<MapDesc> d_maps;
   DevBuf<GuideDesc> d_gdesc;
+  EventHandle ready;  // recorded after build()'s device work; runs wait for it
   bool consumed = false;
   std::string err;
 };
@@ -402,6 +441,21 @@ struct ts_session {
 struct ts_generated {
   uint32_t W = 0, H = 0;
   std::vector<uint32_t> in_dims;  // (w, h) of every example at its loaded size
+  std::vector<uint4> state;       // per pixel, until the maps below are first asked for
+  void ensure_maps() {
+    if (state.empty()) return;
+    const size_t N = state.size();
+    coord.resize(N * 3);
+    ids.resize(N * 2);
+    for (size_t i = 0; i < N; ++i) {
+      coord[3 * i] = state[i].x & 0xffffu;
+      coord[3 * i + 1] = state[i].x >> 16;
+      coord[3 * i + 2] = state[i].w;
+      ids[2 * i] = state[i].y;
+      ids[2 * i + 1] = state[i].z;
+    }
+    std::vector<uint4>().swap(state);
+  }
   std::vector<uint8_t> image;
   std::vector<uint32_t> coord;  // 3 per pixel
   std::vector<uint32_t> ids;    // 2 per pixel
@@ -894,7 +948,10 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
     }
     CUDA_TRY(s->d_gdesc.alloc(gd.size()));
     CUDA_TRY(cudaMemcpy(s->d_gdesc.p, gd.data(), gd.size() * sizeof(GuideDesc), cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaStreamSynchronize(st));
+    // the pyramids are still being built: run() waits for this event on the
+    // device, so its host planning overlaps them
+    CUDA_TRY(cudaEventCreateWithFlags(&s->ready.e, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventRecord(s->ready.e, st));
     s->dev_bytes = s->levels.bytes() + s->plevels.bytes() + s->guides.bytes() + s->pguides.bytes() +
                    s->tguide.bytes() + s->masks.bytes() + s->d_maps.bytes() + s->d_gdesc.bytes();
     s->bottoms = std::move(imgs);
@@ -1311,6 +1368,22 @@ void run_pick_all(RunCtx &c) {
   while (c.picked_stages < c.plan.size()) run_pick(c);
 }
 
+// Let the device's default stream-ordered pool keep freed memory (by
+// default it returns it at every synchronisation), so that each run's
+// buffers come from the pool without device calls.  Once per device.
+void keep_pool(int dev) {
+  static std::mutex mu;
+  static std::vector<int> done;
+  std::lock_guard<std::mutex> lk(mu);
+  if (std::find(done.begin(), done.end(), dev) != done.end()) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done.push_back(dev);
+}
+
 // Device buffers of a run and the step descriptors that point into them.
 // With a pool stream, the buffers are stream-ordered pool memory (freed
 // without waiting for the device); otherwise plain cudaMalloc.
@@ -1593,15 +1666,7 @@ void run_finish(RunCtx &c) {
   g->H = c.H;
   g->image.resize(N * 4);
   memcpy(g->image.data(), c.col.data(), N * 4);
-  g->coord.resize(N * 3);
-  g->ids.resize(N * 2);
-  for (size_t i = 0; i < N; ++i) {
-    g->coord[3 * i] = c.stv[i].x & 0xffffu;
-    g->coord[3 * i + 1] = c.stv[i].x >> 16;
-    g->coord[3 * i + 2] = c.stv[i].w;
-    g->ids[2 * i] = c.stv[i].y;
-    g->ids[2 * i + 1] = c.stv[i].z;
-  }
+  g->state = std::move(c.stv);  // the coordinate and id maps are made on first use
   g->in_dims.clear();
   for (const Image &im : c.s->bottoms) {
     g->in_dims.push_back(im.w);
@@ -1642,12 +1707,14 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
   }
   s->consumed = true;
   const auto t_wall0 = std::chrono::steady_clock::now();
+  StreamGuard sg;  // declared first: the run's pool buffers are freed on it before it goes
   RunCtx c;
   try {
     CUDA_TRY(cudaSetDevice(s->prm.device));
-    StreamGuard sg;
+    keep_pool(s->prm.device);
     CUDA_TRY(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
     const cudaStream_t st = sg.s;
+    if (s->ready.e) CUDA_TRY(cudaStreamWaitEvent(st, s->ready.e, 0));
     auto t = std::chrono::steady_clock::now();
     auto lap = [&]() {
       const auto n = std::chrono::steady_clock::now();
@@ -1657,7 +1724,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     };
     run_plan(s, c);
     const double plan_ms = lap();
-    run_alloc(c, nullptr);
+    run_alloc(c, st);
     // the items go up stage by stage from pinned memory, so that the device
     // runs a stage while the host picks the next one
     PinnedBuf<uint32_t> pitems;
@@ -1719,11 +1786,13 @@ int ts_generated_image(const ts_generated *g, uint8_t *out) {
 }
 int ts_generated_coord_map(const ts_generated *g, uint32_t *out) {
   if (!g || !out) return TS_ERR_NULL;
+  const_cast<ts_generated *>(g)->ensure_maps();  // made on first use (the object is not shared between threads)
   memcpy(out, g->coord.data(), g->coord.size() * 4);
   return TS_OK;
 }
 int ts_generated_id_map(const ts_generated *g, uint32_t *out) {
   if (!g || !out) return TS_ERR_NULL;
+  const_cast<ts_generated *>(g)->ensure_maps();
   memcpy(out, g->ids.data(), g->ids.size() * 4);
   return TS_OK;
 }
@@ -2011,7 +2080,10 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
     EventPair ev;
     ev.create();
     CUDA_TRY(cudaEventRecord(ev.a, st));
-    for (current = 0; current < n; ++current) run_upload(*ctx[current], st);
+    for (current = 0; current < n; ++current) {
+      if (sessions[current]->ready.e) CUDA_TRY(cudaStreamWaitEvent(st, sessions[current]->ready.e, 0));
+      run_upload(*ctx[current], st);
+    }
     CUDA_TRY(cudaMemcpyAsync(d_sess.p, h_sess.data(), n * sizeof(SessionDev), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_steps.p, h_steps.data(), n_steps * sizeof(StepDev), cudaMemcpyHostToDevice, st));
     std::vector<const StepDev *> h_tabs(n);
@@ -2198,6 +2270,7 @@ void server_fail(ts_server *S, ServerReq *r, const Failure &f) {
 // upload stream; the compute stream waits for them before its next tick.
 void server_admit(ts_server *S, ServerReq *r) {
   RunCtx &c = *r->c;
+  if (r->s->ready.e) CUDA_TRY(cudaStreamWaitEvent(S->ust, r->s->ready.e, 0));
   run_alloc(c, S->ust);
   run_upload(c, S->ust);
   std::vector<StepDev> h(c.steps.size());
@@ -2619,6 +2692,7 @@ extern "C" {
 
 ts_transform *ts_generated_coord_transform(const ts_generated *g) {
   if (!g) return nullptr;
+  const_cast<ts_generated *>(g)->ensure_maps();
   ts_transform *t = new (std::nothrow) ts_transform();
   if (!t) return nullptr;
   t->W = g->W;
@@ -2752,6 +2826,7 @@ int ts_transform_apply(const ts_transform *t, const ts_image_desc *sources, uint
 int ts_generated_debug_maps(const ts_generated *g, uint8_t *patch_id_rgba, uint8_t *map_id_rgba,
                             uint8_t *uncertainty_rgba, int32_t device) {
   if (!g || !patch_id_rgba || !map_id_rgba || !uncertainty_rgba) return TS_ERR_NULL;
+  const_cast<ts_generated *>(g)->ensure_maps();
   try {
     CUDA_TRY(cudaSetDevice(device));
     StreamGuard sg;
