@@ -141,6 +141,9 @@ typedef struct ts_run_stats {
   /* Host time of run(): schedule planning, device allocation, enqueueing
    * uploads and launches, waiting for the device, converting the results. */
   double host_plan_ms, host_alloc_ms, host_enqueue_ms, host_wait_ms, host_finish_ms;
+  /* Device time of the initial uploads and of reading the results back
+   * (CUDA events; part of gpu_ms). */
+  double upload_ms, readback_ms;
 } ts_run_stats;
 
 const char *ts_status_str(int status);

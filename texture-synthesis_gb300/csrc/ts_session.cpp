@@ -1730,10 +1730,13 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     PinnedBuf<uint32_t> pitems;
     CUDA_TRY(pitems.alloc(c.items.size()));
     const double alloc_ms = lap();
-    EventPair ev;
+    EventPair ev, ev_up, ev_rb;
     ev.create();
+    ev_up.create();
+    ev_rb.create();
     CUDA_TRY(cudaEventRecord(ev.a, st));
     run_upload(c, st);
+    CUDA_TRY(cudaEventRecord(ev_up.a, st));
     LaunchTimer lt;
     lt.on = s->prm.profile;
     lt.st = st;
@@ -1747,6 +1750,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
       }
       run_enqueue_plain(c, st, lt, progress, user, (int)si);
     }
+    CUDA_TRY(cudaEventRecord(ev_rb.a, st));
     run_readback(c, st);
     CUDA_TRY(cudaEventRecord(ev.b, st));
     const double enqueue_ms = lap();
@@ -1759,6 +1763,13 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     c.g->stats.host_wait_ms = wait_ms;
     c.g->stats.host_finish_ms = lap();
     c.g->stats.gpu_ms = ev.ms();
+    {
+      float up = 0.0f, rb = 0.0f;
+      CUDA_TRY(cudaEventElapsedTime(&up, ev.a, ev_up.a));
+      CUDA_TRY(cudaEventElapsedTime(&rb, ev_rb.a, ev.b));
+      c.g->stats.upload_ms = up;
+      c.g->stats.readback_ms = rb;
+    }
     lt.collect(c.g->stats, c.g->launches);
   } catch (const Failure &f) {
     s->err = f.msg;
