@@ -302,6 +302,10 @@ typedef struct ts_batch_stats {
    * resolve warp form, resolve team form, resolve full team form, commit). */
   uint64_t phase_launches[9];
   double phase_ms[9];
+  /* Device time from the run's start until every session's initial state
+   * is on the device, and from the last launch until the results are
+   * read back (both part of gpu_ms). */
+  double upload_ms, readback_ms;
 } ts_batch_stats;
 ts_batch *ts_batch_new(int32_t device);
 void ts_batch_free(ts_batch *b);

@@ -92,7 +92,8 @@ class _BatchStats(C.Structure):
     _fields_ = [("sessions", C.c_uint64), ("steps", C.c_uint64), ("launches", C.c_uint64),
                 ("output_pixels", C.c_uint64), ("resolves", C.c_uint64), ("cost_evals", C.c_uint64),
                 ("gpu_ms", C.c_double), ("wall_ms", C.c_double), ("plan_ms", C.c_double),
-                ("phase_launches", C.c_uint64 * 9), ("phase_ms", C.c_double * 9)]
+                ("phase_launches", C.c_uint64 * 9), ("phase_ms", C.c_double * 9), ("upload_ms", C.c_double),
+                ("readback_ms", C.c_double)]
 
 
 class _ImageDesc(C.Structure):

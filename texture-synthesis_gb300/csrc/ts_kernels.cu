@@ -1503,6 +1503,14 @@ __device__ __forceinline__ void level_switch_body(const SessionDev &s, uint32_t 
 // (x, y) of source map `map`, (x, y, map) = buf[3i..3i+3].  maps[m] =
 // {texel offset low, high, width, height}.  An entry outside the maps (the
 // reference panics in get_pixel) writes 0 and sets *err.
+__global__ void k_scatter_init(const uint32_t *list, uint32_t n, uint32_t *color, uint4 *state) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t *e = list + (size_t)i * 6;
+  color[e[0]] = e[1];
+  state[e[0]] = make_uint4(e[2], e[3], e[4], e[5]);
+}
+
 __global__ void k_transform_apply(const uint32_t *buf, size_t n, const uint32_t *texels, const uint4 *maps,
                                   uint32_t n_maps, uint32_t *out, int *err) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
@@ -1994,6 +2002,11 @@ void launch_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, ui
   const size_t n = (size_t)pitch * (h + 2 * kPad) * levels;
   if (n == 0) return;
   k_pad<<<(uint32_t)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, stream>>>(src, w, h, levels, pitch, dst);
+}
+
+void launch_scatter_init(const uint32_t *list, uint32_t n, uint32_t *color, uint4 *state, cudaStream_t stream) {
+  if (n == 0) return;
+  k_scatter_init<<<(n + 127) / 128, 128, 0, stream>>>(list, n, color, state);
 }
 
 void launch_transform_apply(const uint32_t *buf, size_t n, const uint32_t *texels, const uint4 *maps,

@@ -1088,6 +1088,11 @@ struct RunCtx {
   int32_t cox = 0, coy = 0;
   uint32_t cgw = 0, cgh = 0;
   std::vector<uint4> state;
+  // dense_init: colour and state are uploaded whole (inpainting); otherwise
+  // both start zeroed on the device and init_list holds the few set pixels
+  // as {pixel, colour, state.x, state.y, state.z, state.w}
+  bool dense_init = false;
+  std::vector<uint32_t> init_list;
   std::vector<float> luts;
   std::vector<int32_t> tab;
   std::vector<double> xdiv, ydiv, dxt, dy2t;
@@ -1101,7 +1106,7 @@ struct RunCtx {
   int32_t x_l = 0, y_b = 0;
   uint64_t dev_bytes = 0;  // device memory run_alloc takes
   // device state
-  DevBuf<uint32_t> d_color, d_occ, d_mir, d_res, d_items, d_ncnt, d_fbl, d_fbc, d_cells;
+  DevBuf<uint32_t> d_color, d_occ, d_mir, d_res, d_items, d_ncnt, d_fbl, d_fbc, d_cells, d_init;
   DevBuf<uint4> d_state;
   DevBuf<float> d_rscore, d_lut;
   DevBuf<double> d_xdiv, d_ydiv, d_dist, d_dxt, d_dy2t, d_mean;
@@ -1135,8 +1140,20 @@ void run_plan(ts_session *s, RunCtx &c) {
   std::vector<uint32_t> &color = c.color;
   std::vector<uint4> &state = c.state;
   std::vector<uint32_t> &resolved = c.resolved;
-  color.assign(N, 0);
-  state.assign(N, make_uint4(0, 0, 0, 0));
+  c.dense_init = s->inpaint;
+  c.init_list.clear();
+  if (c.dense_init) {
+    color.assign(N, 0);
+    state.assign(N, make_uint4(0, 0, 0, 0));
+  }
+  auto put = [&](uint32_t px, uint32_t col, uint4 sv) {
+    if (c.dense_init) {
+      color[px] = col;
+      state[px] = sv;
+    } else {
+      c.init_list.insert(c.init_list.end(), {px, col, sv.x, sv.y, sv.z, sv.w});
+    }
+  };
   std::vector<uint32_t> &unresolved = c.unresolved;
   unresolved.clear();
   size_t locked = 0;
@@ -1179,9 +1196,9 @@ void run_plan(ts_session *s, RunCtx &c) {
       r = pcg_from_u64(sd);
       const uint32_t y = gen_range_u32(r, im.h);
       if (x > 0xffffu || y > 0xffffu) throw Failure{TS_ERR_LIMIT, "example side exceeds limit"};
-      state[px] = make_uint4(x | (y << 16), px, map, map);
       const uint8_t *cc = &im.px[((size_t)y * im.w + x) * 4];
-      color[px] = (uint32_t)cc[0] | ((uint32_t)cc[1] << 8) | ((uint32_t)cc[2] << 16) | ((uint32_t)cc[3] << 24);
+      put(px, (uint32_t)cc[0] | ((uint32_t)cc[1] << 8) | ((uint32_t)cc[2] << 16) | ((uint32_t)cc[3] << 24),
+          make_uint4(x | (y << 16), px, map, map));
       resolved.push_back(px);
     }
     locked += p.random_init;
@@ -1339,7 +1356,7 @@ void run_plan(ts_session *s, RunCtx &c) {
                 c.luts.size() * 4 + c.tab.size() * 4 + mb * kk * 12 + mb * (4 + 8 + 4 + sizeof(Result)) +
                 c.n_batches * 4 + std::max<uint64_t>(c.rc_items, mb) * m * 8 +
                 (c.xdiv.size() + c.ydiv.size() + c.dxt.size() + c.dy2t.size()) * 8 + steps_est * sizeof(StepDev) +
-                c.cells.size() * 4;
+                c.cells.size() * 4 + c.init_list.size() * 4;
 }
 
 // The pick chain of the next stage (pick_random_unresolved, ms.rs:380-389,
@@ -1425,6 +1442,7 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   CUDA_TRY(A(c.d_dxt, c.dxt.size()));
   CUDA_TRY(A(c.d_dy2t, c.dy2t.size()));
   CUDA_TRY(A(c.d_cells, c.cells.size()));
+  CUDA_TRY(A(c.d_init, std::max<size_t>(c.init_list.size(), 1)));
   const std::vector<int32_t> &tab = c.tab;
 
   SessionDev &sd = c.sd;
@@ -1549,8 +1567,19 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
 
 // Uploads of the initial state, enqueued on st.
 void run_upload(RunCtx &c, cudaStream_t st) {
-  CUDA_TRY(cudaMemcpyAsync(c.d_color.p, c.color.data(), c.N * 4, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(c.d_state.p, c.state.data(), c.N * sizeof(uint4), cudaMemcpyHostToDevice, st));
+  if (c.dense_init) {
+    CUDA_TRY(cudaMemcpyAsync(c.d_color.p, c.color.data(), c.N * 4, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(c.d_state.p, c.state.data(), c.N * sizeof(uint4), cudaMemcpyHostToDevice, st));
+  } else {
+    CUDA_TRY(cudaMemsetAsync(c.d_color.p, 0, c.N * 4, st));
+    CUDA_TRY(cudaMemsetAsync(c.d_state.p, 0, c.N * sizeof(uint4), st));
+    if (!c.init_list.empty()) {
+      CUDA_TRY(cudaMemcpyAsync(c.d_init.p, c.init_list.data(), c.init_list.size() * 4, cudaMemcpyHostToDevice,
+                               st));
+      launch_scatter_init(c.d_init.p, (uint32_t)(c.init_list.size() / 6), c.d_color.p, c.d_state.p, st);
+      ++c.launches;
+    }
+  }
   CUDA_TRY(cudaMemcpyAsync(c.d_occ.p, c.occ.data(), c.occ.size() * 4, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(c.d_mir.p, c.mir.data(), c.mir.size() * 4, cudaMemcpyHostToDevice, st));
   if (c.locked) CUDA_TRY(cudaMemcpyAsync(c.d_res.p, c.resolved.data(), c.locked * 4, cudaMemcpyHostToDevice, st));
@@ -2029,7 +2058,18 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
       }
     std::vector<Segment> h_segs, h_fb;
     std::vector<PlannedLaunch> launches;
+    std::vector<size_t> last_launch(n, 0);  // a session's results are final after this launch
     size_t phase_smem[kPhases] = {};
+    // segments of a launch go heaviest session first (per-item resolve work
+    // grows with k (k + m), doubled by a guide), so that the blocks left for
+    // the end of a launch are the light ones
+    std::vector<size_t> heavy(n);
+    for (size_t j = 0; j < n; ++j) heavy[j] = j;
+    auto weight = [&](size_t j) {
+      const RunCtx &c = *ctx[j];
+      return (uint64_t)std::max<uint32_t>(c.k, 1) * (c.k + c.m) * (sessions[j]->guided ? 2 : 1);
+    };
+    std::stable_sort(heavy.begin(), heavy.end(), [&](size_t x, size_t y) { return weight(x) > weight(y); });
     for (size_t t = 0; t < max_steps; ++t) {
       // the resolve form follows the step's items over all sessions: the
       // team forms only pay while the whole launch is too small to fill
@@ -2053,7 +2093,7 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
         pl.n_segs = pl.blocks = 0;
         pl.smem = 0;
         pl.fb0 = (uint32_t)h_fb.size();
-        for (size_t j = 0; j < n; ++j) {
+        for (size_t j : heavy) {
           const RunCtx &c = *ctx[j];
           if (t >= c.steps.size()) continue;
           const Step &stp = c.steps[t];
@@ -2075,6 +2115,8 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
         if (pl.n_segs || pl.n_fb) {
           phase_smem[ph] = std::max(phase_smem[ph], pl.smem);
           launches.push_back(pl);
+          for (uint32_t q = pl.seg0; q < pl.seg0 + pl.n_segs; ++q) last_launch[h_segs[q].session] = launches.size() - 1;
+          for (uint32_t q = pl.fb0; q < pl.fb0 + pl.n_fb; ++q) last_launch[h_fb[q].session] = launches.size() - 1;
         }
       }
     }
@@ -2088,8 +2130,9 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
     CUDA_TRY(d_steps.alloc(n_steps));
     CUDA_TRY(d_segs.alloc(h_segs.size()));
     CUDA_TRY(d_fb.alloc(h_fb.size()));
-    EventPair ev;
+    EventPair ev, ev_io;
     ev.create();
+    ev_io.create();
     CUDA_TRY(cudaEventRecord(ev.a, st));
     for (current = 0; current < n; ++current) {
       if (sessions[current]->ready.e) CUDA_TRY(cudaStreamWaitEvent(st, sessions[current]->ready.e, 0));
@@ -2105,8 +2148,31 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
                                st));
     if (!h_fb.empty())
       CUDA_TRY(cudaMemcpyAsync(d_fb.p, h_fb.data(), h_fb.size() * sizeof(Segment), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaEventRecord(ev_io.a, st));
     std::vector<EventPair> pev(b->profile && !b->graph ? launches.size() : 0);
     for (auto &e : pev) e.create();
+    // sessions are read back on a copy stream as soon as their last launch
+    // is done, while the longer sessions still run
+    std::vector<size_t> order(n);
+    for (size_t j = 0; j < n; ++j) order[j] = j;
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return last_launch[x] < last_launch[y]; });
+    std::vector<EventHandle> done_ev(launches.size());
+    for (size_t j = 0; j < n; ++j)
+      if (!done_ev[last_launch[j]].e) CUDA_TRY(cudaEventCreateWithFlags(&done_ev[last_launch[j]].e, cudaEventDisableTiming));
+    StreamGuard cg;
+    CUDA_TRY(cudaStreamCreateWithFlags(&cg.s, cudaStreamNonBlocking));
+    EventHandle copies_done;
+    CUDA_TRY(cudaEventCreateWithFlags(&copies_done.e, cudaEventDisableTiming));
+    auto readbacks = [&] {
+      for (size_t q = 0; q < n; ++q) {
+        current = order[q];
+        if (q == 0 || last_launch[order[q - 1]] != last_launch[current])
+          CUDA_TRY(cudaStreamWaitEvent(cg.s, done_ev[last_launch[current]].e, 0));
+        run_readback(*ctx[current], cg.s);
+      }
+      CUDA_TRY(cudaEventRecord(copies_done.e, cg.s));
+      CUDA_TRY(cudaStreamWaitEvent(st, copies_done.e, 0));
+    };
     auto enqueue = [&](cudaStream_t s) {
       for (size_t li = 0; li < launches.size(); ++li) {
         const PlannedLaunch &pl = launches[li];
@@ -2121,6 +2187,8 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
         if (!pev.empty()) CUDA_TRY(cudaEventRecord(pev[li].a, s));
         launch_multi(pl.phase, ml, pl.blocks, pl.smem, s);
         if (!pev.empty()) CUDA_TRY(cudaEventRecord(pev[li].b, s));
+        if (done_ev[li].e)
+          CUDA_TRY(cudaEventRecordWithFlags(done_ev[li].e, s, b->graph ? cudaEventRecordExternal : cudaEventRecordDefault));
       }
       CUDA_TRY(cudaGetLastError());
     };
@@ -2146,12 +2214,14 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
       } gg{graph, exec};
       CUDA_TRY(cudaGraphInstantiate(&exec, graph, 0));
       CUDA_TRY(cudaGraphLaunch(exec, st));
-      for (current = 0; current < n; ++current) run_readback(*ctx[current], st);
+      CUDA_TRY(cudaEventRecord(ev_io.b, st));
+      readbacks();
       CUDA_TRY(cudaEventRecord(ev.b, st));
       CUDA_TRY(cudaStreamSynchronize(st));
     } else {
       enqueue(st);
-      for (current = 0; current < n; ++current) run_readback(*ctx[current], st);
+      CUDA_TRY(cudaEventRecord(ev_io.b, st));
+      readbacks();
       CUDA_TRY(cudaEventRecord(ev.b, st));
       CUDA_TRY(cudaStreamSynchronize(st));
     }
@@ -2161,6 +2231,13 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
     bs.steps = max_steps;
     bs.launches = launches.size();
     bs.plan_ms = plan_ms;
+    {
+      float up = 0.0f, rb = 0.0f;
+      CUDA_TRY(cudaEventElapsedTime(&up, ev.a, ev_io.a));
+      CUDA_TRY(cudaEventElapsedTime(&rb, ev_io.b, ev.b));
+      bs.upload_ms = up;
+      bs.readback_ms = rb;
+    }
     for (size_t li = 0; li < pev.size(); ++li) {
       bs.phase_launches[launches[li].phase] += 1;
       bs.phase_ms[launches[li].phase] += pev[li].ms();
