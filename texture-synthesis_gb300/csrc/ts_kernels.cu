@@ -1499,10 +1499,8 @@ __device__ __forceinline__ void level_switch_body(const SessionDev &s, uint32_t 
   s.color[p] = s.levels[md.off + (size_t)level * md.w * md.h + (size_t)y * md.w + x];
 }
 
-// CoordinateTransform::apply (lib.rs:176-212): output pixel i takes texel
-// (x, y) of source map `map`, (x, y, map) = buf[3i..3i+3].  maps[m] =
-// {texel offset low, high, width, height}.  An entry outside the maps (the
-// reference panics in get_pixel) writes 0 and sets *err.
+// Initial state of the random-init pixels (Generator::new, ms.rs:427-475):
+// list[6i..6i+6] = {pixel, colour, state.x, state.y, state.z, state.w}.
 __global__ void k_scatter_init(const uint32_t *list, uint32_t n, uint32_t *color, uint4 *state) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -1511,6 +1509,10 @@ __global__ void k_scatter_init(const uint32_t *list, uint32_t n, uint32_t *color
   state[e[0]] = make_uint4(e[2], e[3], e[4], e[5]);
 }
 
+// CoordinateTransform::apply (lib.rs:176-212): output pixel i takes texel
+// (x, y) of source map `map`, (x, y, map) = buf[3i..3i+3].  maps[m] =
+// {texel offset low, high, width, height}.  An entry outside the maps (the
+// reference panics in get_pixel) writes 0 and sets *err.
 __global__ void k_transform_apply(const uint32_t *buf, size_t n, const uint32_t *texels, const uint4 *maps,
                                   uint32_t n_maps, uint32_t *out, int *err) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {

@@ -47,6 +47,9 @@ constexpr float kTilingBoundary = 0.05f;  // TILING_BOUNDARY_PERCENTAGE, ms.rs:1
 constexpr int kKnnTabRadius = 36;
 constexpr int kDistTabRadius = 64;  // offsets the weight tables cover
 constexpr uint64_t kRcandBudget = 64ull << 20;  // random-candidate entries held at once
+// Runs whose random candidates for every stage fit this many entries make
+// them all ahead, on a side stream, while the first stages run.
+constexpr uint64_t kRcandWhole = 256ull << 20;
 
 struct Image {
   std::vector<uint8_t> px;  // RGBA8
@@ -1100,6 +1103,12 @@ struct RunCtx {
   uint64_t overall_total = 0;
   uint32_t max_batch_items = 1;
   uint64_t rc_items = 1;
+  // rc_ahead: every stage's random candidates are made on a side stream at
+  // the start (stage q's launch carried by step rc_step[q]); the main
+  // stream waits for rc_ev[q] instead of launching them itself
+  bool want_rc_ahead = false, rc_ahead = false;
+  std::vector<int> rc_step;
+  std::vector<EventHandle> rc_ev;
   size_t res_total = 0;                // resolved-list length at the end of the run
   std::vector<uint32_t> unresolved;    // pixels not yet picked (the pick chain's state)
   size_t picked_stages = 0;            // stages whose items are known
@@ -1298,6 +1307,7 @@ void run_plan(ts_session *s, RunCtx &c) {
   for (auto &sp : plan) c.n_batches += sp.batches.size();
   c.max_batch_items = max_batch_items;
   c.rc_items = std::max<uint64_t>(1, std::min<uint64_t>(max_stage_items, kRcandBudget / std::max(m, 1u)));
+  c.rc_ahead = c.want_rc_ahead && m > 0 && (uint64_t)n_items_total * m <= kRcandWhole;
   c.x_l = x_l;
   c.y_b = y_b;
   const int32_t xo = x_l + 2, yo = y_b + 2;
@@ -1354,7 +1364,7 @@ void run_plan(ts_session *s, RunCtx &c) {
   for (auto &sp : plan) steps_est += sp.batches.size() + 1;
   c.dev_bytes = N * 4 + N * sizeof(uint4) + 2 * (uint64_t)wpr * H * 4 + c.res_total * 8 + items.size() * 4 +
                 c.luts.size() * 4 + c.tab.size() * 4 + mb * kk * 12 + mb * (4 + 8 + 4 + sizeof(Result)) +
-                c.n_batches * 4 + std::max<uint64_t>(c.rc_items, mb) * m * 8 +
+                c.n_batches * 4 + (c.rc_ahead ? (uint64_t)items.size() : std::max<uint64_t>(c.rc_items, mb)) * m * 8 +
                 (c.xdiv.size() + c.ydiv.size() + c.dxt.size() + c.dy2t.size()) * 8 + steps_est * sizeof(StepDev) +
                 c.cells.size() * 4 + c.init_list.size() * 4;
 }
@@ -1436,7 +1446,7 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   CUDA_TRY(A(c.d_result, max_batch_items));
   CUDA_TRY(A(c.d_err, 1));
   CUDA_TRY(A(c.d_evals, 1));
-  CUDA_TRY(A(c.d_rcand, (size_t)std::max<uint64_t>(rc_items, max_batch_items) * m));
+  CUDA_TRY(A(c.d_rcand, c.rc_ahead ? c.items.size() * m : (size_t)std::max<uint64_t>(rc_items, max_batch_items) * m));
   CUDA_TRY(A(c.d_xdiv, c.xdiv.size()));
   CUDA_TRY(A(c.d_ydiv, c.ydiv.size()));
   CUDA_TRY(A(c.d_dxt, c.dxt.size()));
@@ -1496,10 +1506,12 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
 
   // ---- the steps ----
   size_t fb_index = 0;
+  c.rc_step.assign(plan.size(), -1);
   for (size_t si = 0; si < plan.size(); ++si) {
     const StagePlan &sp = plan[si];
     c.overall_total += sp.n_items;
     const size_t first = c.steps.size();
+    if (c.rc_ahead && !sp.batches.empty()) c.rc_step[si] = (int)first;
     Step pending;
     pending.stage = (int)si;
     if (sp.level_switch) {
@@ -1519,13 +1531,13 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
     while (bi < sp.batches.size()) {
       size_t bj = bi;
       const uint32_t c0 = sp.batches[bi].i0;
-      while (bj < sp.batches.size() && (bj == bi || sp.batches[bj].i1 - c0 <= rc_items)) ++bj;
+      while (bj < sp.batches.size() && (bj == bi || c.rc_ahead || sp.batches[bj].i1 - c0 <= rc_items)) ++bj;
       const uint32_t c1 = sp.batches[bj - 1].i1;
       StageDev chunk = sdv;
       chunk.items = sdv.items + c0;
       chunk.n_items = c1 - c0;
       chunk.stage_seed = sp.seed + c0;  // item i's stream is seeded with stage_seed + i + 1
-      chunk.rcand = c.d_rcand.p;
+      chunk.rcand = c.d_rcand.p + (c.rc_ahead ? (size_t)sp.items_off * m : 0);
       chunk.redo = sp.redo > c0 ? sp.redo - c0 : 0;
       pending.rc = true;
       pending.rc_st = chunk;
@@ -1618,8 +1630,12 @@ void run_enqueue_plain(RunCtx &c, cudaStream_t st, LaunchTimer &lt, ts_progress_
       ++c.launches;
     }
     if (stp.rc) {
-      lt.run(TS_KERNEL_RANDOM_CANDIDATES, [&] { launch_random_candidates(sd, stp.rc_st, st); });
-      ++c.launches;
+      if (c.rc_ahead) {
+        CUDA_TRY(cudaStreamWaitEvent(st, c.rc_ev[stp.stage].e, 0));
+      } else {
+        lt.run(TS_KERNEL_RANDOM_CANDIDATES, [&] { launch_random_candidates(sd, stp.rc_st, st); });
+        ++c.launches;
+      }
     }
     if (stp.batch) {
       lt.items = stp.n;
@@ -1737,6 +1753,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
   s->consumed = true;
   const auto t_wall0 = std::chrono::steady_clock::now();
   StreamGuard sg;  // declared first: the run's pool buffers are freed on it before it goes
+  StreamGuard rg;  // side stream of the random candidates made ahead
   RunCtx c;
   try {
     CUDA_TRY(cudaSetDevice(s->prm.device));
@@ -1751,6 +1768,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
       t = n;
       return ms;
     };
+    c.want_rc_ahead = true;
     run_plan(s, c);
     const double plan_ms = lap();
     run_alloc(c, st);
@@ -1768,6 +1786,27 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     CUDA_TRY(cudaEventRecord(ev_up.a, st));
     LaunchTimer lt;
     lt.on = s->prm.profile;
+    if (c.rc_ahead) {
+      // every stage's random candidates depend on the examples and the
+      // stage plan only: a side stream makes them while the first stages run
+      CUDA_TRY(cudaStreamCreateWithFlags(&rg.s, cudaStreamNonBlocking));
+      EventHandle fork;
+      CUDA_TRY(cudaEventCreateWithFlags(&fork.e, cudaEventDisableTiming));
+      CUDA_TRY(cudaEventRecord(fork.e, st));
+      CUDA_TRY(cudaStreamWaitEvent(rg.s, fork.e, 0));
+      c.rc_ev.resize(c.plan.size());
+      lt.st = rg.s;
+      for (size_t q = 0; q < c.plan.size(); ++q) {
+        if (c.rc_step[q] < 0) continue;
+        const Step &stp = c.steps[c.rc_step[q]];
+        lt.stage = c.plan[q].p_stage;
+        lt.items = stp.rc_st.n_items;
+        lt.run(TS_KERNEL_RANDOM_CANDIDATES, [&] { launch_random_candidates(c.sd, stp.rc_st, rg.s); });
+        ++c.launches;
+        CUDA_TRY(cudaEventCreateWithFlags(&c.rc_ev[q].e, cudaEventDisableTiming));
+        CUDA_TRY(cudaEventRecord(c.rc_ev[q].e, rg.s));
+      }
+    }
     lt.st = st;
     for (size_t si = 0; si < c.plan.size(); ++si) {
       run_pick(c);
@@ -1801,6 +1840,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     }
     lt.collect(c.g->stats, c.g->launches);
   } catch (const Failure &f) {
+    if (rg.s) cudaStreamSynchronize(rg.s);  // its kernels write buffers freed on the main stream
     s->err = f.msg;
     return f.status;
   }
@@ -1878,7 +1918,7 @@ uint32_t phase_units(const Step &stp, const RunCtx &c, int phase) {
   const bool knn = stp.batch && c.k > 0;
   switch (phase) {
     case kPhaseLevelSwitch: return stp.ls ? stp.ls_n_res : 0;
-    case kPhaseRandom: return (stp.rc && c.m > 0) ? stp.rc_st.n_items : 0;
+    case kPhaseRandom: return (stp.rc && c.m > 0 && !c.rc_ahead) ? stp.rc_st.n_items : 0;
     case kPhaseWalk: return (knn && !stp.exhaustive) ? stp.n : 0;
     case kPhaseExhaustive: return (knn && stp.exhaustive) ? stp.n : 0;
     case kPhaseMean: return (knn && !stp.exhaustive) ? stp.n : 0;
@@ -1907,6 +1947,7 @@ struct PlannedLaunch {
   uint32_t seg0, n_segs, blocks;
   size_t smem;
   uint32_t fb0 = 0, n_fb = 0, pool_block0 = 0;  // exhaustive k-NN: fallback lists drained by a block pool
+  int wait_rc = -1;  // first wait for the side stream's random candidates up to this launch of them
 };
 
 // Blocks of the exhaustive k-NN's fallback pool (three 64 KB CTAs per SM).
@@ -2012,6 +2053,7 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
         for (size_t j = next++; j < n; j = next++) {
           try {
             ctx[j].reset(new RunCtx());
+            ctx[j]->want_rc_ahead = true;
             run_plan(sessions[j], *ctx[j]);
             run_pick_all(*ctx[j]);
             run_alloc(*ctx[j], nullptr);
@@ -2070,7 +2112,45 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
       return (uint64_t)std::max<uint32_t>(c.k, 1) * (c.k + c.m) * (sessions[j]->guided ? 2 : 1);
     };
     std::stable_sort(heavy.begin(), heavy.end(), [&](size_t x, size_t y) { return weight(x) > weight(y); });
+    // random candidates made ahead on a side stream: launch q holds stage q
+    // of every session that makes them so (rc_pos[q] indexes rc_launches)
+    size_t max_stages = 0;
+    for (size_t j = 0; j < n; ++j) max_stages = std::max(max_stages, ctx[j]->plan.size());
+    std::vector<PlannedLaunch> rc_launches;
+    std::vector<int> rc_pos(max_stages, -1);
+    for (size_t q = 0; q < max_stages; ++q) {
+      PlannedLaunch pl;
+      pl.phase = kPhaseRandom;
+      pl.seg0 = (uint32_t)h_segs.size();
+      pl.n_segs = pl.blocks = 0;
+      pl.smem = 0;
+      for (size_t j : heavy) {
+        const RunCtx &c = *ctx[j];
+        if (!c.rc_ahead || q >= c.rc_step.size() || c.rc_step[q] < 0) continue;
+        const uint32_t t = (uint32_t)c.rc_step[q];
+        const uint32_t nb = multi_blocks(kPhaseRandom, c.steps[t].rc_st.n_items, 0);
+        if (nb == 0) continue;
+        h_segs.push_back(Segment{pl.blocks, nb, (uint32_t)j, t});
+        pl.blocks += nb;
+        pl.n_segs += 1;
+        pl.smem = std::max(pl.smem, multi_smem_bytes(kPhaseRandom, c.k, c.m));
+      }
+      pl.pool_block0 = pl.blocks;
+      if (pl.n_segs) {
+        phase_smem[kPhaseRandom] = std::max(phase_smem[kPhaseRandom], pl.smem);
+        rc_pos[q] = (int)rc_launches.size();
+        rc_launches.push_back(pl);
+      }
+    }
+    int rc_waited = -1;
     for (size_t t = 0; t < max_steps; ++t) {
+      // a session starting stage q at this step needs rc launch q done
+      int rc_need = -1;
+      for (size_t j = 0; j < n; ++j) {
+        const RunCtx &c = *ctx[j];
+        if (c.rc_ahead && t < c.steps.size() && c.steps[t].rc) rc_need = std::max(rc_need, rc_pos[c.steps[t].stage]);
+      }
+      const size_t launches_before = launches.size();
       // the resolve form follows the step's items over all sessions: the
       // team forms only pay while the whole launch is too small to fill
       // the GPU with warps
@@ -2118,6 +2198,10 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
           for (uint32_t q = pl.seg0; q < pl.seg0 + pl.n_segs; ++q) last_launch[h_segs[q].session] = launches.size() - 1;
           for (uint32_t q = pl.fb0; q < pl.fb0 + pl.n_fb; ++q) last_launch[h_fb[q].session] = launches.size() - 1;
         }
+      }
+      if (rc_need > rc_waited && launches.size() > launches_before) {
+        launches[launches_before].wait_rc = rc_need;
+        rc_waited = rc_need;
       }
     }
     for (int ph = 0; ph < kPhases; ++ph) CUDA_TRY(set_multi_smem(ph, phase_smem[ph]));
@@ -2173,9 +2257,35 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
       CUDA_TRY(cudaEventRecord(copies_done.e, cg.s));
       CUDA_TRY(cudaStreamWaitEvent(st, copies_done.e, 0));
     };
+    StreamGuard rg;  // side stream of the random candidates made ahead
+    std::vector<EventHandle> rc_ev(rc_launches.size());
+    if (!rc_launches.empty()) {
+      CUDA_TRY(cudaStreamCreateWithFlags(&rg.s, cudaStreamNonBlocking));
+      for (auto &e : rc_ev) CUDA_TRY(cudaEventCreateWithFlags(&e.e, cudaEventDisableTiming));
+    }
+    EventHandle fork;
+    CUDA_TRY(cudaEventCreateWithFlags(&fork.e, cudaEventDisableTiming));
     auto enqueue = [&](cudaStream_t s) {
+      if (!rc_launches.empty()) {
+        CUDA_TRY(cudaEventRecord(fork.e, s));
+        CUDA_TRY(cudaStreamWaitEvent(rg.s, fork.e, 0));
+        for (size_t i = 0; i < rc_launches.size(); ++i) {
+          const PlannedLaunch &pl = rc_launches[i];
+          MultiLaunch ml;
+          ml.segs = d_segs.p + pl.seg0;
+          ml.n_segs = pl.n_segs;
+          ml.sessions = d_sess.p;
+          ml.step_tabs = d_tabs.p;
+          ml.fb = d_fb.p;
+          ml.n_fb = 0;
+          ml.pool_block0 = pl.blocks;
+          launch_multi(kPhaseRandom, ml, pl.blocks, pl.smem, rg.s);
+          CUDA_TRY(cudaEventRecord(rc_ev[i].e, rg.s));
+        }
+      }
       for (size_t li = 0; li < launches.size(); ++li) {
         const PlannedLaunch &pl = launches[li];
+        if (pl.wait_rc >= 0) CUDA_TRY(cudaStreamWaitEvent(s, rc_ev[pl.wait_rc].e, 0));
         MultiLaunch ml;
         ml.segs = d_segs.p + pl.seg0;
         ml.n_segs = pl.n_segs;
@@ -2190,6 +2300,7 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
         if (done_ev[li].e)
           CUDA_TRY(cudaEventRecordWithFlags(done_ev[li].e, s, b->graph ? cudaEventRecordExternal : cudaEventRecordDefault));
       }
+      if (!rc_launches.empty()) CUDA_TRY(cudaStreamWaitEvent(s, rc_ev.back().e, 0));  // joins the side stream
       CUDA_TRY(cudaGetLastError());
     };
     if (b->graph) {
@@ -2229,7 +2340,8 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
     ts_batch_stats bs{};
     bs.sessions = n;
     bs.steps = max_steps;
-    bs.launches = launches.size();
+    bs.launches = launches.size() + rc_launches.size();
+    bs.phase_launches[kPhaseRandom] += rc_launches.size();
     bs.plan_ms = plan_ms;
     {
       float up = 0.0f, rb = 0.0f;
