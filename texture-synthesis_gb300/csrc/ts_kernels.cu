@@ -1501,12 +1501,13 @@ __device__ __forceinline__ void level_switch_body(const SessionDev &s, uint32_t 
 
 // Initial state of the random-init pixels (Generator::new, ms.rs:427-475):
 // list[6i..6i+6] = {pixel, colour, state.x, state.y, state.z, state.w}.
-__global__ void k_scatter_init(const uint32_t *list, uint32_t n, uint32_t *color, uint4 *state) {
+__global__ void k_scatter_init(const uint32_t *list, uint32_t n, uint32_t *color, uint4 *state, uint32_t *res) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint32_t *e = list + (size_t)i * 6;
   color[e[0]] = e[1];
   state[e[0]] = make_uint4(e[2], e[3], e[4], e[5]);
+  res[i] = e[0];
 }
 
 // CoordinateTransform::apply (lib.rs:176-212): output pixel i takes texel
@@ -2006,9 +2007,10 @@ void launch_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, ui
   k_pad<<<(uint32_t)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, stream>>>(src, w, h, levels, pitch, dst);
 }
 
-void launch_scatter_init(const uint32_t *list, uint32_t n, uint32_t *color, uint4 *state, cudaStream_t stream) {
+void launch_scatter_init(const uint32_t *list, uint32_t n, uint32_t *color, uint4 *state, uint32_t *res,
+                         cudaStream_t stream) {
   if (n == 0) return;
-  k_scatter_init<<<(n + 127) / 128, 128, 0, stream>>>(list, n, color, state);
+  k_scatter_init<<<(n + 127) / 128, 128, 0, stream>>>(list, n, color, state, res);
 }
 
 void launch_transform_apply(const uint32_t *buf, size_t n, const uint32_t *texels, const uint4 *maps,

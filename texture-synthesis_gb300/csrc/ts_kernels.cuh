@@ -197,8 +197,10 @@ void launch_commit(const SessionDev &s, const StageDev &st, const BatchDev &b, c
 void launch_level_switch(const SessionDev &s, uint32_t level, uint32_t n_res, cudaStream_t stream);
 
 // Initial state of the pixels set before the first stage (random init):
-// list[6i..6i+6] = {pixel, colour, state.x, state.y, state.z, state.w}.
-void launch_scatter_init(const uint32_t *list, uint32_t n, uint32_t *color, uint4 *state, cudaStream_t stream);
+// list[6i..6i+6] = {pixel, colour, state.x, state.y, state.z, state.w};
+// res[i] = pixel (the resolved list starts with them, in list order).
+void launch_scatter_init(const uint32_t *list, uint32_t n, uint32_t *color, uint4 *state, uint32_t *res,
+                         cudaStream_t stream);
 
 // CoordinateTransform::apply: out[i] = texel buf[3i..3i+3] = (x, y, map) of
 // the maps {offset low, offset high, w, h}; *err set for entries outside.

@@ -106,17 +106,19 @@ std::string fmt_float(float v) {
 // A device array.  alloc() uses cudaMalloc (freed with cudaFree, which
 // waits for the device); alloc_on(stream) takes stream-ordered pool memory,
 // freed with cudaFreeAsync on the stream set by free_on (at first the
-// allocating one), so that freeing never stalls the device.
+// allocating one), so that freeing never stalls the device.  view() makes
+// it a non-owning window into another array.
 template <typename T>
 struct DevBuf {
   T *p = nullptr;
   size_t n = 0;
   bool pooled = false;
+  bool owned = true;
   cudaStream_t fs = nullptr;
   DevBuf() = default;
   DevBuf(const DevBuf &) = delete;
   DevBuf &operator=(const DevBuf &) = delete;
-  DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n), pooled(o.pooled), fs(o.fs) {
+  DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n), pooled(o.pooled), owned(o.owned), fs(o.fs) {
     o.p = nullptr;
     o.n = 0;
   }
@@ -126,6 +128,7 @@ struct DevBuf {
       p = o.p;
       n = o.n;
       pooled = o.pooled;
+      owned = o.owned;
       fs = o.fs;
       o.p = nullptr;
       o.n = 0;
@@ -134,7 +137,7 @@ struct DevBuf {
   }
   ~DevBuf() { reset(); }
   void reset() {
-    if (p) {
+    if (p && owned) {
       if (pooled)
         cudaFreeAsync(p, fs);
       else
@@ -143,6 +146,13 @@ struct DevBuf {
     p = nullptr;
     n = 0;
     pooled = false;
+    owned = true;
+  }
+  void view(void *base, size_t count) {
+    reset();
+    p = (T *)base;
+    n = count;
+    owned = false;
   }
   cudaError_t alloc(size_t count) {
     reset();
@@ -171,18 +181,84 @@ struct DevBuf {
   size_t bytes() const { return p ? n * sizeof(T) : 0; }
 };
 
-// Page-locked host memory (cudaMallocHost), for copies that must not wait.
+// Process-wide cache of page-locked host blocks: cudaMallocHost costs about
+// as much host time as the copies it speeds up, so blocks are kept and
+// reused (at most kKeep bytes idle; sizes rounded up to 2 MiB).  Never
+// destroyed: the CUDA context may be gone at process exit.
+class PinnedPool {
+ public:
+  static PinnedPool &get() {
+    static PinnedPool *pool = new PinnedPool();
+    return *pool;
+  }
+  cudaError_t take(size_t bytes, void **p, size_t *got) {
+    bytes = (std::max<size_t>(bytes, 1) + kRound - 1) / kRound * kRound;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      size_t best = idle_.size();
+      for (size_t i = 0; i < idle_.size(); ++i)
+        if (idle_[i].second >= bytes && (best == idle_.size() || idle_[i].second < idle_[best].second)) best = i;
+      if (best < idle_.size() && idle_[best].second <= 2 * bytes) {
+        *p = idle_[best].first;
+        *got = idle_[best].second;
+        idle_bytes_ -= *got;
+        idle_.erase(idle_.begin() + best);
+        return cudaSuccess;
+      }
+    }
+    *got = bytes;
+    return cudaMallocHost(p, bytes);
+  }
+  void give(void *p, size_t bytes) {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      if (idle_bytes_ + bytes <= kKeep) {
+        idle_.emplace_back(p, bytes);
+        idle_bytes_ += bytes;
+        return;
+      }
+    }
+    cudaFreeHost(p);
+  }
+
+ private:
+  static constexpr size_t kRound = 2u << 20;
+  static constexpr size_t kKeep = 1ull << 30;
+  std::mutex mu_;
+  std::vector<std::pair<void *, size_t>> idle_;
+  size_t idle_bytes_ = 0;
+};
+
+// Page-locked host memory from the pool, for copies that must not wait.
+// The owner makes sure no copy from it is in flight when it goes.
 template <typename T>
 struct PinnedBuf {
   T *p = nullptr;
+  size_t got = 0;
   PinnedBuf() = default;
   PinnedBuf(const PinnedBuf &) = delete;
   PinnedBuf &operator=(const PinnedBuf &) = delete;
-  ~PinnedBuf() {
-    if (p) cudaFreeHost(p);
+  PinnedBuf(PinnedBuf &&o) noexcept : p(o.p), got(o.got) { o.p = nullptr; }
+  PinnedBuf &operator=(PinnedBuf &&o) noexcept {
+    if (this != &o) {
+      reset();
+      p = o.p;
+      got = o.got;
+      o.p = nullptr;
+    }
+    return *this;
+  }
+  ~PinnedBuf() { reset(); }
+  void reset() {
+    if (p) PinnedPool::get().give(p, got);
+    p = nullptr;
   }
   cudaError_t alloc(size_t count) {
-    return cudaMallocHost((void **)&p, (count ? count : 1) * sizeof(T));
+    reset();
+    void *v = nullptr;
+    const cudaError_t e = PinnedPool::get().take((count ? count : 1) * sizeof(T), &v, &got);
+    p = e == cudaSuccess ? (T *)v : nullptr;
+    return e;
   }
 };
 
@@ -1096,6 +1172,9 @@ struct RunCtx {
   // as {pixel, colour, state.x, state.y, state.z, state.w}
   bool dense_init = false;
   std::vector<uint32_t> init_list;
+  // items_async: the caller uploads the items from pitems itself
+  bool items_async = false;
+  PinnedBuf<uint32_t> pitems;
   std::vector<float> luts;
   std::vector<int32_t> tab;
   std::vector<double> xdiv, ydiv, dxt, dy2t;
@@ -1115,6 +1194,17 @@ struct RunCtx {
   int32_t x_l = 0, y_b = 0;
   uint64_t dev_bytes = 0;  // device memory run_alloc takes
   // device state
+  // three allocations: zeroed at the start (zero), uploaded from the pinned
+  // block ptab (tabs) and scratch (work); the arrays below are views
+  DevBuf<uint8_t> d_zero, d_tabs, d_work;
+  size_t zero_bytes = 0, tabs_bytes = 0;
+  struct TabPart {
+    size_t off;
+    const void *src;
+    size_t bytes;
+  };
+  std::vector<TabPart> tab_parts;
+  PinnedBuf<uint8_t> ptab;
   DevBuf<uint32_t> d_color, d_occ, d_mir, d_res, d_items, d_ncnt, d_fbl, d_fbc, d_cells, d_init;
   DevBuf<uint4> d_state;
   DevBuf<float> d_rscore, d_lut;
@@ -1428,31 +1518,64 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   const int32_t R = kDistTabRadius;
   const uint32_t wpr = (W + 31) / 32;
   auto A = [&](auto &buf, size_t n) { return pool ? buf.alloc_on(n, pool) : buf.alloc(n); };
-  CUDA_TRY(A(c.d_color, N));
-  CUDA_TRY(A(c.d_state, N));
-  CUDA_TRY(A(c.d_occ, (size_t)wpr * H));
-  CUDA_TRY(A(c.d_mir, (size_t)wpr * H));
-  CUDA_TRY(A(c.d_res, c.res_total));
-  CUDA_TRY(A(c.d_rscore, c.res_total));
-  CUDA_TRY(A(c.d_items, c.items.size()));
-  CUDA_TRY(A(c.d_lut, c.luts.size()));
-  CUDA_TRY(A(c.d_tab, c.tab.size()));
-  CUDA_TRY(A(c.d_nbuf, (size_t)max_batch_items * std::max<uint32_t>(k, 1)));
-  CUDA_TRY(A(c.d_ncnt, max_batch_items));
-  CUDA_TRY(A(c.d_dist, (size_t)max_batch_items * std::max<uint32_t>(k, 1)));
-  CUDA_TRY(A(c.d_mean, max_batch_items));
-  CUDA_TRY(A(c.d_fbl, max_batch_items));
-  CUDA_TRY(A(c.d_fbc, c.n_batches));
-  CUDA_TRY(A(c.d_result, max_batch_items));
-  CUDA_TRY(A(c.d_err, 1));
-  CUDA_TRY(A(c.d_evals, 1));
-  CUDA_TRY(A(c.d_rcand, c.rc_ahead ? c.items.size() * m : (size_t)std::max<uint64_t>(rc_items, max_batch_items) * m));
-  CUDA_TRY(A(c.d_xdiv, c.xdiv.size()));
-  CUDA_TRY(A(c.d_ydiv, c.ydiv.size()));
-  CUDA_TRY(A(c.d_dxt, c.dxt.size()));
-  CUDA_TRY(A(c.d_dy2t, c.dy2t.size()));
-  CUDA_TRY(A(c.d_cells, c.cells.size()));
-  CUDA_TRY(A(c.d_init, std::max<size_t>(c.init_list.size(), 1)));
+  struct Layout {
+    size_t off = 0;
+    size_t add(size_t bytes) {
+      const size_t o = off;
+      off += (std::max<size_t>(bytes, 1) + 255) / 256 * 256;
+      return o;
+    }
+  } zl, tl, wl;
+  const size_t kk = std::max<uint32_t>(k, 1), mb = max_batch_items;
+  const size_t rc_n = c.rc_ahead ? c.items.size() * m : (size_t)std::max<uint64_t>(rc_items, mb) * m;
+  // zeroed: colour and state first (uploaded instead when dense_init)
+  const size_t z_color = zl.add(N * 4), z_state = zl.add(N * sizeof(uint4)), z_rscore = zl.add(c.res_total * 4),
+               z_fbc = zl.add(c.n_batches * 4), z_err = zl.add(sizeof(int)), z_evals = zl.add(8);
+  // uploaded tables
+  c.tab_parts.clear();
+  auto T = [&](const auto &v) {
+    const size_t bytes = v.size() * sizeof(v[0]);
+    const size_t o = tl.add(bytes);
+    c.tab_parts.push_back(RunCtx::TabPart{o, v.data(), bytes});
+    return o;
+  };
+  const size_t t_lut = T(c.luts), t_tab = T(c.tab), t_xdiv = T(c.xdiv), t_ydiv = T(c.ydiv), t_dxt = T(c.dxt),
+               t_dy2t = T(c.dy2t), t_cells = T(c.cells), t_occ = T(c.occ), t_mir = T(c.mir), t_init = T(c.init_list);
+  // scratch
+  const size_t w_res = wl.add(c.res_total * 4), w_items = wl.add(c.items.size() * 4), w_nbuf = wl.add(mb * kk * 4),
+               w_ncnt = wl.add(mb * 4), w_dist = wl.add(mb * kk * 8), w_mean = wl.add(mb * 8), w_fbl = wl.add(mb * 4),
+               w_result = wl.add(mb * sizeof(Result)), w_rcand = wl.add(rc_n * 8);
+  CUDA_TRY(A(c.d_zero, zl.off));
+  CUDA_TRY(A(c.d_tabs, tl.off));
+  CUDA_TRY(A(c.d_work, wl.off));
+  c.zero_bytes = zl.off;
+  c.tabs_bytes = tl.off;
+  uint8_t *z = c.d_zero.p, *tb = c.d_tabs.p, *wk = c.d_work.p;
+  c.d_color.view(z + z_color, N);
+  c.d_state.view(z + z_state, N);
+  c.d_rscore.view(z + z_rscore, c.res_total);
+  c.d_fbc.view(z + z_fbc, c.n_batches);
+  c.d_err.view(z + z_err, 1);
+  c.d_evals.view(z + z_evals, 1);
+  c.d_lut.view(tb + t_lut, c.luts.size());
+  c.d_tab.view(tb + t_tab, c.tab.size());
+  c.d_xdiv.view(tb + t_xdiv, c.xdiv.size());
+  c.d_ydiv.view(tb + t_ydiv, c.ydiv.size());
+  c.d_dxt.view(tb + t_dxt, c.dxt.size());
+  c.d_dy2t.view(tb + t_dy2t, c.dy2t.size());
+  c.d_cells.view(tb + t_cells, c.cells.size());
+  c.d_occ.view(tb + t_occ, c.occ.size());
+  c.d_mir.view(tb + t_mir, c.mir.size());
+  c.d_init.view(tb + t_init, c.init_list.size());
+  c.d_res.view(wk + w_res, c.res_total);
+  c.d_items.view(wk + w_items, c.items.size());
+  c.d_nbuf.view(wk + w_nbuf, mb * kk);
+  c.d_ncnt.view(wk + w_ncnt, mb);
+  c.d_dist.view(wk + w_dist, mb * kk);
+  c.d_mean.view(wk + w_mean, mb);
+  c.d_fbl.view(wk + w_fbl, mb);
+  c.d_result.view(wk + w_result, mb);
+  c.d_rcand.view(wk + w_rcand, rc_n);
   const std::vector<int32_t> &tab = c.tab;
 
   SessionDev &sd = c.sd;
@@ -1578,36 +1701,39 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
 }
 
 // Uploads of the initial state, enqueued on st.
+// The session's tables in a pinned block laid out as the device's table
+// arena (ready for one copy); the batched form makes it on its planning
+// threads, the other paths in run_upload.
+void run_stage_tables(RunCtx &c) {
+  if (c.ptab.p) return;
+  CUDA_TRY(c.ptab.alloc(c.tabs_bytes));
+  for (const RunCtx::TabPart &t : c.tab_parts)
+    if (t.bytes) memcpy(c.ptab.p + t.off, t.src, t.bytes);
+}
+
+// Uploads of the initial state, enqueued on st: one zero fill, one copy of
+// the tables (colour and state too when dense_init), the random-init
+// pixels; the items unless the caller sends them (items_async).
 void run_upload(RunCtx &c, cudaStream_t st) {
+  run_stage_tables(c);
   if (c.dense_init) {
+    const size_t cs = (size_t)((uint8_t *)c.d_rscore.p - c.d_zero.p);
     CUDA_TRY(cudaMemcpyAsync(c.d_color.p, c.color.data(), c.N * 4, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(c.d_state.p, c.state.data(), c.N * sizeof(uint4), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(c.d_zero.p + cs, 0, c.zero_bytes - cs, st));
   } else {
-    CUDA_TRY(cudaMemsetAsync(c.d_color.p, 0, c.N * 4, st));
-    CUDA_TRY(cudaMemsetAsync(c.d_state.p, 0, c.N * sizeof(uint4), st));
-    if (!c.init_list.empty()) {
-      CUDA_TRY(cudaMemcpyAsync(c.d_init.p, c.init_list.data(), c.init_list.size() * 4, cudaMemcpyHostToDevice,
-                               st));
-      launch_scatter_init(c.d_init.p, (uint32_t)(c.init_list.size() / 6), c.d_color.p, c.d_state.p, st);
-      ++c.launches;
-    }
+    CUDA_TRY(cudaMemsetAsync(c.d_zero.p, 0, c.zero_bytes, st));
   }
-  CUDA_TRY(cudaMemcpyAsync(c.d_occ.p, c.occ.data(), c.occ.size() * 4, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(c.d_mir.p, c.mir.data(), c.mir.size() * 4, cudaMemcpyHostToDevice, st));
-  if (c.locked) CUDA_TRY(cudaMemcpyAsync(c.d_res.p, c.resolved.data(), c.locked * 4, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemsetAsync(c.d_rscore.p, 0, c.res_total * 4, st));
-  if (!c.items.empty() && c.picked_stages == c.plan.size())
+  CUDA_TRY(cudaMemcpyAsync(c.d_tabs.p, c.ptab.p, c.tabs_bytes, cudaMemcpyHostToDevice, st));
+  if (c.dense_init) {
+    if (c.locked) CUDA_TRY(cudaMemcpyAsync(c.d_res.p, c.resolved.data(), c.locked * 4, cudaMemcpyHostToDevice, st));
+  } else if (!c.init_list.empty()) {
+    // the resolved list starts with the random-init pixels, in list order
+    launch_scatter_init(c.d_init.p, (uint32_t)(c.init_list.size() / 6), c.d_color.p, c.d_state.p, c.d_res.p, st);
+    ++c.launches;
+  }
+  if (!c.items.empty() && c.picked_stages == c.plan.size() && !c.items_async)
     CUDA_TRY(cudaMemcpyAsync(c.d_items.p, c.items.data(), c.items.size() * 4, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(c.d_lut.p, c.luts.data(), c.luts.size() * 4, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(c.d_tab.p, c.tab.data(), c.tab.size() * 4, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(c.d_xdiv.p, c.xdiv.data(), c.xdiv.size() * 8, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(c.d_ydiv.p, c.ydiv.data(), c.ydiv.size() * 8, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(c.d_dxt.p, c.dxt.data(), c.dxt.size() * 8, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(c.d_dy2t.p, c.dy2t.data(), c.dy2t.size() * 8, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(c.d_cells.p, c.cells.data(), c.cells.size() * 4, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemsetAsync(c.d_fbc.p, 0, c.n_batches * 4, st));
-  CUDA_TRY(cudaMemsetAsync(c.d_err.p, 0, sizeof(int), st));
-  CUDA_TRY(cudaMemsetAsync(c.d_evals.p, 0, sizeof(unsigned long long), st));
 }
 
 // The plain path: one session's launches, step by step (only those of
@@ -1754,6 +1880,9 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
   const auto t_wall0 = std::chrono::steady_clock::now();
   StreamGuard sg;  // declared first: the run's pool buffers are freed on it before it goes
   StreamGuard rg;  // side stream of the random candidates made ahead
+  // the items go up stage by stage from pinned memory, so that the device
+  // runs a stage while the host picks the next one
+  PinnedBuf<uint32_t> pitems;
   RunCtx c;
   try {
     CUDA_TRY(cudaSetDevice(s->prm.device));
@@ -1772,9 +1901,6 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     run_plan(s, c);
     const double plan_ms = lap();
     run_alloc(c, st);
-    // the items go up stage by stage from pinned memory, so that the device
-    // runs a stage while the host picks the next one
-    PinnedBuf<uint32_t> pitems;
     CUDA_TRY(pitems.alloc(c.items.size()));
     const double alloc_ms = lap();
     EventPair ev, ev_up, ev_rb;
@@ -1840,7 +1966,9 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     }
     lt.collect(c.g->stats, c.g->launches);
   } catch (const Failure &f) {
-    if (rg.s) cudaStreamSynchronize(rg.s);  // its kernels write buffers freed on the main stream
+    // nothing of the run may be in flight when its buffers go
+    if (rg.s) cudaStreamSynchronize(rg.s);
+    if (sg.s) cudaStreamSynchronize(sg.s);
     s->err = f.msg;
     return f.status;
   }
@@ -1948,6 +2076,7 @@ struct PlannedLaunch {
   size_t smem;
   uint32_t fb0 = 0, n_fb = 0, pool_block0 = 0;  // exhaustive k-NN: fallback lists drained by a block pool
   int wait_rc = -1;  // first wait for the side stream's random candidates up to this launch of them
+  int wait_items = -1;  // first wait for the side stream's item uploads up to this part
 };
 
 // Blocks of the exhaustive k-NN's fallback pool (three 64 KB CTAs per SM).
@@ -2033,11 +2162,14 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
       for (ts_session *s : v) delete s;
     }
   } owned{sessions};
+  // main stream, side stream (item uploads, random candidates made ahead)
+  // and copy stream (read-backs); outside the try so that a failure can
+  // drain them before the sessions' buffers go
+  StreamGuard sg, rg, cg;
   std::vector<std::unique_ptr<RunCtx>> ctx(n);
   size_t current = 0;
   try {
     CUDA_TRY(cudaSetDevice(b->device));
-    StreamGuard sg;
     CUDA_TRY(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
     const cudaStream_t st = sg.s;
     size_t max_steps = 0;
@@ -2057,6 +2189,11 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
             run_plan(sessions[j], *ctx[j]);
             run_pick_all(*ctx[j]);
             run_alloc(*ctx[j], nullptr);
+            RunCtx &c = *ctx[j];
+            run_stage_tables(c);
+            if (cudaSuccess != c.pitems.alloc(c.items.size())) throw Failure{TS_ERR_CUDA, "pinned host memory"};
+            memcpy(c.pitems.p, c.items.data(), c.items.size() * 4);
+            c.items_async = true;
           } catch (const Failure &f) {
             fails[j] = f;
           } catch (const std::bad_alloc &) {
@@ -2142,7 +2279,7 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
         rc_launches.push_back(pl);
       }
     }
-    int rc_waited = -1;
+    int rc_waited = -1, items_waited = -1;
     for (size_t t = 0; t < max_steps; ++t) {
       // a session starting stage q at this step needs rc launch q done
       int rc_need = -1;
@@ -2203,6 +2340,15 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
         launches[launches_before].wait_rc = rc_need;
         rc_waited = rc_need;
       }
+      // stage 0 items before the first launch, the rest before any session
+      // gets past stage 0
+      int items_need = t == 0 ? 0 : -1;
+      for (size_t j = 0; j < n; ++j)
+        if (t < ctx[j]->steps.size() && ctx[j]->steps[t].stage >= 1) items_need = 1;
+      if (items_need > items_waited && launches.size() > launches_before) {
+        launches[launches_before].wait_items = items_need;
+        items_waited = items_need;
+      }
     }
     for (int ph = 0; ph < kPhases; ++ph) CUDA_TRY(set_multi_smem(ph, phase_smem[ph]));
     DevBuf<SessionDev> d_sess;
@@ -2243,7 +2389,6 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
     std::vector<EventHandle> done_ev(launches.size());
     for (size_t j = 0; j < n; ++j)
       if (!done_ev[last_launch[j]].e) CUDA_TRY(cudaEventCreateWithFlags(&done_ev[last_launch[j]].e, cudaEventDisableTiming));
-    StreamGuard cg;
     CUDA_TRY(cudaStreamCreateWithFlags(&cg.s, cudaStreamNonBlocking));
     EventHandle copies_done;
     CUDA_TRY(cudaEventCreateWithFlags(&copies_done.e, cudaEventDisableTiming));
@@ -2257,34 +2402,54 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
       CUDA_TRY(cudaEventRecord(copies_done.e, cg.s));
       CUDA_TRY(cudaStreamWaitEvent(st, copies_done.e, 0));
     };
-    StreamGuard rg;  // side stream of the random candidates made ahead
     std::vector<EventHandle> rc_ev(rc_launches.size());
-    if (!rc_launches.empty()) {
-      CUDA_TRY(cudaStreamCreateWithFlags(&rg.s, cudaStreamNonBlocking));
-      for (auto &e : rc_ev) CUDA_TRY(cudaEventCreateWithFlags(&e.e, cudaEventDisableTiming));
-    }
-    EventHandle fork;
+    CUDA_TRY(cudaStreamCreateWithFlags(&rg.s, cudaStreamNonBlocking));
+    for (auto &e : rc_ev) CUDA_TRY(cudaEventCreateWithFlags(&e.e, cudaEventDisableTiming));
+    EventHandle fork, side_done, items_ev[2];
     CUDA_TRY(cudaEventCreateWithFlags(&fork.e, cudaEventDisableTiming));
-    auto enqueue = [&](cudaStream_t s) {
-      if (!rc_launches.empty()) {
-        CUDA_TRY(cudaEventRecord(fork.e, s));
-        CUDA_TRY(cudaStreamWaitEvent(rg.s, fork.e, 0));
-        for (size_t i = 0; i < rc_launches.size(); ++i) {
-          const PlannedLaunch &pl = rc_launches[i];
-          MultiLaunch ml;
-          ml.segs = d_segs.p + pl.seg0;
-          ml.n_segs = pl.n_segs;
-          ml.sessions = d_sess.p;
-          ml.step_tabs = d_tabs.p;
-          ml.fb = d_fb.p;
-          ml.n_fb = 0;
-          ml.pool_block0 = pl.blocks;
-          launch_multi(kPhaseRandom, ml, pl.blocks, pl.smem, rg.s);
-          CUDA_TRY(cudaEventRecord(rc_ev[i].e, rg.s));
-        }
+    CUDA_TRY(cudaEventCreateWithFlags(&side_done.e, cudaEventDisableTiming));
+    for (auto &e : items_ev) CUDA_TRY(cudaEventCreateWithFlags(&e.e, cudaEventDisableTiming));
+    // the items of stage 0 (part 0) and of the later stages (part 1), every
+    // session's, from its pinned copy
+    auto upload_items = [&](int part) {
+      for (size_t j = 0; j < n; ++j) {
+        RunCtx &c = *ctx[j];
+        if (c.items.empty()) continue;
+        const size_t split = c.plan.size() > 1 ? c.plan[1].items_off : c.items.size();
+        const size_t a = part == 0 ? 0 : split, e = part == 0 ? split : c.items.size();
+        if (e > a)
+          CUDA_TRY(cudaMemcpyAsync(c.d_items.p + a, c.pitems.p + a, (e - a) * 4, cudaMemcpyHostToDevice, rg.s));
       }
+      CUDA_TRY(cudaEventRecord(items_ev[part].e, rg.s));
+    };
+    auto launch_rc = [&](size_t i) {
+      const PlannedLaunch &pl = rc_launches[i];
+      MultiLaunch ml;
+      ml.segs = d_segs.p + pl.seg0;
+      ml.n_segs = pl.n_segs;
+      ml.sessions = d_sess.p;
+      ml.step_tabs = d_tabs.p;
+      ml.fb = d_fb.p;
+      ml.n_fb = 0;
+      ml.pool_block0 = pl.blocks;
+      launch_multi(kPhaseRandom, ml, pl.blocks, pl.smem, rg.s);
+      CUDA_TRY(cudaEventRecord(rc_ev[i].e, rg.s));
+    };
+    auto enqueue = [&](cudaStream_t s) {
+      // side stream: stage 0's items and random candidates first (the
+      // first steps wait for them), then the later stages' while those
+      // first steps run
+      CUDA_TRY(cudaEventRecord(fork.e, s));
+      CUDA_TRY(cudaStreamWaitEvent(rg.s, fork.e, 0));
+      upload_items(0);
+      size_t rci = 0;
+      if (!rc_launches.empty() && rc_pos[0] == 0) launch_rc(rci++);
+      upload_items(1);
+      for (; rci < rc_launches.size(); ++rci) launch_rc(rci);
+      CUDA_TRY(cudaEventRecord(side_done.e, rg.s));
       for (size_t li = 0; li < launches.size(); ++li) {
         const PlannedLaunch &pl = launches[li];
+        if (pl.wait_items >= 0) CUDA_TRY(cudaStreamWaitEvent(s, items_ev[pl.wait_items].e, 0));
         if (pl.wait_rc >= 0) CUDA_TRY(cudaStreamWaitEvent(s, rc_ev[pl.wait_rc].e, 0));
         MultiLaunch ml;
         ml.segs = d_segs.p + pl.seg0;
@@ -2300,7 +2465,7 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
         if (done_ev[li].e)
           CUDA_TRY(cudaEventRecordWithFlags(done_ev[li].e, s, b->graph ? cudaEventRecordExternal : cudaEventRecordDefault));
       }
-      if (!rc_launches.empty()) CUDA_TRY(cudaStreamWaitEvent(s, rc_ev.back().e, 0));  // joins the side stream
+      CUDA_TRY(cudaStreamWaitEvent(s, side_done.e, 0));  // joins the side stream
       CUDA_TRY(cudaGetLastError());
     };
     if (b->graph) {
@@ -2372,6 +2537,9 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
     bs.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
     b->stats = bs;
   } catch (const Failure &f) {
+    // nothing may be in flight when the sessions' buffers go
+    for (cudaStream_t q : {sg.s, rg.s, cg.s})
+      if (q) cudaStreamSynchronize(q);
     b->err = "session " + std::to_string(current < n ? current : 0) + ": " + f.msg;
     return f.status;
   }
