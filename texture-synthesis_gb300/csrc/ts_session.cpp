@@ -2191,6 +2191,12 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
             run_alloc(*ctx[j], nullptr);
             RunCtx &c = *ctx[j];
             run_stage_tables(c);
+            // touch the read-back destinations here, in parallel, rather
+            // than in the copies at the end of the run
+            c.col.resize(c.N);
+            c.stv.resize(c.N);
+            c.g->resolved.resize(c.res_total);
+            c.g->scores.resize(c.res_total);
             if (cudaSuccess != c.pitems.alloc(c.items.size())) throw Failure{TS_ERR_CUDA, "pinned host memory"};
             memcpy(c.pitems.p, c.items.data(), c.items.size() * 4);
             c.items_async = true;
