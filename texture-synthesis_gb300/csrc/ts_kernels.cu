@@ -1052,26 +1052,46 @@ __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev
     }
     const int32_t *nbo = b.nbuf + (size_t)local * s.k;
     const double avg = b.mean[local];
-    // neighbours: offsets, weights, own pattern, coherence candidates
+    // neighbours: offsets, weights, own pattern, coherence candidates.
+    // With `dedupe`, a coherence candidate equal to an earlier one (same
+    // source and map) is left out: its cost equals the earlier one's, so it
+    // can neither beat it nor tie it with a lower index, and the reference's
+    // winner is the same without it.  The exact sequential form for
+    // non-finite costs keeps every candidate.
     bool nan_w = false;
     int maxoff = 0;
-    uint32_t ncoh = 0;
+    uint32_t ncoh = 0, ncoh_all = 0;
     bool bad_map = false;
-    for (uint32_t j0 = 0; j0 < nk; j0 += kWarp) {
-      const uint32_t j = j0 + lane;
-      bool valid = false;
-      uint32_t cxy = 0, aux = 0;
-      if (j < nk)
-        valid = neighbour_setup(s, st, b, local, nb, px, py, j, nbo[j], avg, tab, tab_ff, w, cxy, aux, nan_w,
-                                maxoff, bad_map);
-      const uint32_t bal = __ballot_sync(0xffffffffu, valid);
-      if (valid) {
-        const uint32_t slot = ncoh + __popc(bal & lt);
-        w.cxy[slot] = cxy;
-        w.caux[slot] = aux;
+    auto coherence = [&](bool dedupe) {
+      ncoh = ncoh_all = 0;
+      for (uint32_t j0 = 0; j0 < nk; j0 += kWarp) {
+        const uint32_t j = j0 + lane;
+        bool valid = false;
+        uint32_t cxy = 0, aux = 0;
+        if (j < nk)
+          valid = neighbour_setup(s, st, b, local, nb, px, py, j, nbo[j], avg, tab, tab_ff, w, cxy, aux, nan_w,
+                                  maxoff, bad_map);
+        bool keep = valid;
+        if (dedupe) {
+          const unsigned long long key =
+              valid ? (((unsigned long long)(aux & 0x7fffu) << 32) | cxy) : ((1ull << 63) | (unsigned long long)lane);
+          if (__match_any_sync(0xffffffffu, key) & lt) keep = false;  // a lower lane holds it
+          for (uint32_t i = 0; keep && i < ncoh; ++i)
+            if (w.cxy[i] == cxy && (w.caux[i] & 0x7fffu) == (aux & 0x7fffu)) keep = false;
+        }
+        ncoh_all += __popc(__ballot_sync(0xffffffffu, valid));
+        const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+          const uint32_t slot = ncoh + __popc(bal & lt);
+          w.cxy[slot] = cxy;
+          w.caux[slot] = aux;
+        }
+        ncoh += __popc(bal);
+        __syncwarp();
       }
-      ncoh += __popc(bal);
-    }
+    };
+    coherence(!st.slow_lut);
+    if (!st.slow_lut && __any_sync(0xffffffffu, nan_w)) coherence(false);
     if (__any_sync(0xffffffffu, bad_map)) {
       // the reference panics on this index; record the error and leave the
       // pixel untouched (commit skips results with an invalid map)
@@ -1132,7 +1152,7 @@ __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev
     } else if (lane == 0) {
       sequential_best(s, st, w, lc, lg, nk, nc, best_s, best_i);
     }
-    if (lane == 0) write_result(s, w, b, local, pixel, px, py, is_new, nc, best_s, best_i);
+    if (lane == 0) write_result(s, w, b, local, pixel, px, py, is_new, ncoh_all + s.m, best_s, best_i);
   }
 }
 
