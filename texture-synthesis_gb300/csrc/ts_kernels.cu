@@ -34,6 +34,8 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <utility>
 
 #include "ts_common.h"
@@ -1865,37 +1867,43 @@ static size_t team_full_smem_bytes(uint32_t k, uint32_t m) {
 }
 constexpr size_t kTeamFullMaxSmem = 96 * 1024;
 
-cudaError_t configure_kernels(uint32_t k, uint32_t m) {
-  const size_t smem = resolve_smem_bytes(k, m, 0);
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
-  cudaError_t e = cudaFuncSetAttribute(k_knn_exhaustive, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       kExhAllKeys * 8);
+// Raises (never lowers) a kernel's dynamic shared-memory limit on the
+// current device, so that sessions with different (k, m) can be built in
+// any order and run later.
+template <typename K>
+static cudaError_t raise_smem(K *kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> cur;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  const size_t tsm = team_smem_bytes(k, m);
-  if (tsm > 48 * 1024) {
-    e = cudaFuncSetAttribute(k_resolve_team<kTeamThreads, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)tsm);
-    if (e != cudaSuccess) return e;
-  }
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &c = cur[{dev, (const void *)kernel}];
+  if (bytes <= c) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) c = bytes;
+  return e;
+}
+
+cudaError_t configure_kernels(uint32_t k, uint32_t m) {
+  cudaError_t e = raise_smem(k_resolve, resolve_smem_bytes(k, m, 0));
+  if (e != cudaSuccess) return e;
+  e = raise_smem(k_knn_exhaustive, kExhAllKeys * 8);
+  if (e != cudaSuccess) return e;
+  e = raise_smem(k_resolve_team<kTeamThreads, false>, team_smem_bytes(k, m));
+  if (e != cudaSuccess) return e;
   const size_t fsm = team_full_smem_bytes(k, m);
-  if (fsm > 48 * 1024 && fsm <= kTeamFullMaxSmem)
-    return cudaFuncSetAttribute(k_resolve_team<kTeamFullThreads, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)fsm);
+  if (fsm <= kTeamFullMaxSmem) return raise_smem(k_resolve_team<kTeamFullThreads, true>, fsm);
   return cudaSuccess;
 }
 
 cudaError_t set_multi_smem(int phase, size_t bytes) {
-  if (bytes <= 48 * 1024) return cudaSuccess;
-  const int v = (int)bytes;
-  const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
   switch (phase) {
-    case kPhaseExhaustive: return cudaFuncSetAttribute(k_knn_exhaustive_multi, a, v);
-    case kPhaseResolve: return cudaFuncSetAttribute(k_resolve_multi, a, v);
-    case kPhaseTeamPart: return cudaFuncSetAttribute(k_resolve_team_multi<kTeamThreads, false>, a, v);
-    case kPhaseTeamFull: return cudaFuncSetAttribute(k_resolve_team_multi<kTeamFullThreads, true>, a, v);
+    case kPhaseExhaustive: return raise_smem(k_knn_exhaustive_multi, bytes);
+    case kPhaseResolve: return raise_smem(k_resolve_multi, bytes);
+    case kPhaseTeamPart: return raise_smem(k_resolve_team_multi<kTeamThreads, false>, bytes);
+    case kPhaseTeamFull: return raise_smem(k_resolve_team_multi<kTeamFullThreads, true>, bytes);
     default: return cudaSuccess;
   }
 }

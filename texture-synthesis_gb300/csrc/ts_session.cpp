@@ -1391,6 +1391,7 @@ void run_plan(ts_session *s, RunCtx &c) {
   // the items themselves come from the pick chain, stage by stage (run_pick)
   items.assign(n_items_total, 0);
   c.res_total = n_res;
+  resolved.reserve(n_res);  // the picks append without moving the locked entries
   c.picked_stages = 0;
   // ---- host tables ----
   const uint32_t wpr = (W + 31) / 32;
@@ -1736,12 +1737,51 @@ void run_upload(RunCtx &c, cudaStream_t st) {
     CUDA_TRY(cudaMemcpyAsync(c.d_items.p, c.items.data(), c.items.size() * 4, cudaMemcpyHostToDevice, st));
 }
 
+// The launches of one step of one session, with the single-session
+// kernels (parameters by value).
+void enqueue_step(RunCtx &c, const Step &stp, cudaStream_t st, LaunchTimer &lt) {
+  const SessionDev &sd = c.sd;
+  if (stp.ls) {
+    lt.run(TS_KERNEL_LEVEL_SWITCH, [&] { launch_level_switch(sd, stp.ls_level, stp.ls_n_res, st); });
+    ++c.launches;
+  }
+  if (stp.rc) {
+    if (c.rc_ahead) {
+      CUDA_TRY(cudaStreamWaitEvent(st, c.rc_ev[stp.stage].e, 0));
+    } else {
+      lt.run(TS_KERNEL_RANDOM_CANDIDATES, [&] { launch_random_candidates(sd, stp.rc_st, st); });
+      ++c.launches;
+    }
+  }
+  if (stp.batch) {
+    lt.items = stp.n;
+    if (c.k > 0) {
+      if (stp.exhaustive) {
+        lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, stp.st, stp.bd, true, st); });
+        ++c.launches;
+      } else {
+        lt.run(TS_KERNEL_KNN_WALK, [&] { launch_knn_walk(sd, stp.st, stp.bd, st); });
+        lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, stp.st, stp.bd, false, st); });
+        c.launches += 2;
+      }
+    }
+    if (c.k > 0 && !stp.exhaustive) {  // the exhaustive k-NN over a whole batch computes the mean itself
+      lt.run(TS_KERNEL_MEAN, [&] { launch_mean(sd, stp.st, stp.bd, st); });
+      ++c.launches;
+    }
+    if (stp.resolve == kPhaseResolve)
+      lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve(sd, stp.st, stp.bd, st); });
+    else
+      lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve_team(sd, stp.st, stp.bd, stp.resolve == kPhaseTeamFull, st); });
+    lt.run(TS_KERNEL_COMMIT, [&] { launch_commit(sd, stp.st, stp.bd, st); });
+    c.launches += 2;
+  }
+}
+
 // The plain path: one session's launches, step by step (only those of
 // stage `stage` when it is not negative).
 void run_enqueue_plain(RunCtx &c, cudaStream_t st, LaunchTimer &lt, ts_progress_fn progress, void *user,
                        int stage = -1) {
-  const SessionDev &sd = c.sd;
-  const uint32_t k = c.k;
   uint64_t overall_current = 0;
   for (const StagePlan &sp : c.plan)
     if (stage >= 0 && (&sp - c.plan.data()) < stage) overall_current += sp.n_items;
@@ -1751,41 +1791,8 @@ void run_enqueue_plain(RunCtx &c, cudaStream_t st, LaunchTimer &lt, ts_progress_
     const StagePlan &sp = c.plan[stp.stage];
     lt.stage = sp.p_stage;
     lt.items = sp.n_items;
-    if (stp.ls) {
-      lt.run(TS_KERNEL_LEVEL_SWITCH, [&] { launch_level_switch(sd, stp.ls_level, stp.ls_n_res, st); });
-      ++c.launches;
-    }
-    if (stp.rc) {
-      if (c.rc_ahead) {
-        CUDA_TRY(cudaStreamWaitEvent(st, c.rc_ev[stp.stage].e, 0));
-      } else {
-        lt.run(TS_KERNEL_RANDOM_CANDIDATES, [&] { launch_random_candidates(sd, stp.rc_st, st); });
-        ++c.launches;
-      }
-    }
+    enqueue_step(c, stp, st, lt);
     if (stp.batch) {
-      lt.items = stp.n;
-      if (k > 0) {
-        if (stp.exhaustive) {
-          lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, stp.st, stp.bd, true, st); });
-          ++c.launches;
-        } else {
-          lt.run(TS_KERNEL_KNN_WALK, [&] { launch_knn_walk(sd, stp.st, stp.bd, st); });
-          lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, stp.st, stp.bd, false, st); });
-          c.launches += 2;
-        }
-      }
-      if (k > 0 && !stp.exhaustive) {  // the exhaustive k-NN over a whole batch computes the mean itself
-        lt.run(TS_KERNEL_MEAN, [&] { launch_mean(sd, stp.st, stp.bd, st); });
-        ++c.launches;
-      }
-      if (stp.resolve == kPhaseResolve)
-        lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve(sd, stp.st, stp.bd, st); });
-      else
-        lt.run(TS_KERNEL_RESOLVE,
-               [&] { launch_resolve_team(sd, stp.st, stp.bd, stp.resolve == kPhaseTeamFull, st); });
-      lt.run(TS_KERNEL_COMMIT, [&] { launch_commit(sd, stp.st, stp.bd, st); });
-      c.launches += 2;
       ++c.batches;
       c.resolves += stp.n;
     }
@@ -2587,6 +2594,13 @@ struct ServerReq {
   std::string err;
   ts_generated *result = nullptr;
   bool done = false;
+  // The pick chain runs ahead of the device: stage 0 on the submitting
+  // thread, the rest on a picker thread, into c->pitems; `picked` counts the
+  // stages whose items are there, `uploaded` those the driver has copied
+  // to the device (driver only), `picks_done` guards c against the picker.
+  std::atomic<uint32_t> picked{0};
+  uint32_t uploaded = 0;
+  bool picks_done = false;  // under the server mutex
   cudaEvent_t up_ev = nullptr, ev = nullptr;  // uploads done; last kernels done
   ~ServerReq() {
     if (up_ev) cudaEventDestroy(up_ev);
@@ -2596,7 +2610,7 @@ struct ServerReq {
   }
 };
 
-constexpr uint32_t kServerRing = 4;  // ticks in flight
+constexpr uint32_t kServerRing = 8;  // ticks in flight
 
 }  // namespace
 
@@ -2607,24 +2621,25 @@ struct ts_server {
   uint32_t team_max_items = 8192, team_full_max_items = 1024;
   double t0 = 0;
   std::mutex mu;
-  std::condition_variable cv_work, cv_done, cv_complete;
+  std::condition_variable cv_work, cv_done, cv_complete, cv_pick, cv_picked;
+  std::deque<ServerReq *> to_pick;  // requests whose later stages are still to be picked
   std::deque<ServerReq *> pending;
   std::unordered_map<uint64_t, ServerReq *> reqs;  // submitted, not yet collected
   std::deque<ServerReq *> completing;              // steps done, waiting for read-back
   std::vector<uint32_t> free_slots;
   uint64_t used = 0;
   uint64_t next_ticket = 1;
-  bool stop = false, stop_completer = false;
+  bool stop = false, stop_completer = false, stop_pickers = false;
   int fatal = TS_OK;
   std::string err;
   std::vector<ServerReq *> active;  // driver thread only
   std::thread driver, completer;
+  std::vector<std::thread> pickers;
   cudaStream_t st = nullptr, ust = nullptr, cst = nullptr;  // compute, upload, completion
   DevBuf<SessionDev> d_sess;
   DevBuf<const StepDev *> d_tabs;
   struct Ring {
-    Segment *h = nullptr;
-    DevBuf<Segment> d;
+    Segment *h = nullptr;  // pinned, read by the tick's kernels
     cudaEvent_t ev = nullptr;
     bool used = false;
   };
@@ -2638,6 +2653,37 @@ namespace {
 void server_fail(ts_server *S, ServerReq *r, const Failure &f) {
   r->status = f.status;
   r->err = f.msg;
+}
+
+// The next stage of a request's pick chain, into its pinned items.
+void server_pick_stage(ServerReq &r) {
+  RunCtx &c = *r.c;
+  const size_t q = c.picked_stages;
+  run_pick(c);
+  const StagePlan &sp = c.plan[q];
+  if (sp.n_items) memcpy(c.pitems.p + sp.items_off, c.items.data() + sp.items_off, (size_t)sp.n_items * 4);
+  r.picked.store((uint32_t)q + 1, std::memory_order_release);
+}
+
+void server_picker(ts_server *S) {
+  for (;;) {
+    ServerReq *r = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_pick.wait(lk, [&] { return S->stop_pickers || !S->to_pick.empty(); });
+      if (S->to_pick.empty()) return;
+      r = S->to_pick.front();
+      S->to_pick.pop_front();
+    }
+    while (r->picked.load(std::memory_order_relaxed) < r->c->plan.size()) {
+      server_pick_stage(*r);
+      std::lock_guard<std::mutex> lk(S->mu);  // the driver may be waiting for this stage
+      S->cv_picked.notify_all();
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    r->picks_done = true;
+    S->cv_picked.notify_all();
+  }
 }
 
 // Device buffers, uploads and slot entries of an admitted request, on the
@@ -2672,6 +2718,7 @@ void server_admit(ts_server *S, ServerReq *r) {
 
 void server_driver(ts_server *S) {
   if (cudaSetDevice(S->device) != cudaSuccess) return;
+  std::vector<ServerReq *> ready_buf;
   std::vector<Segment> segs, fb;
   std::vector<PlannedLaunch> launches;
   size_t phase_smem[kPhases] = {};
@@ -2715,13 +2762,34 @@ void server_driver(ts_server *S) {
       S->stats.peak_active = std::max<uint64_t>(S->stats.peak_active, S->active.size());
     }
     if (S->active.empty()) continue;
-    // ---- one tick: the next step of every active session ----
+    // ---- one tick: the next step of every active session whose items are
+    // picked (the others wait for their picker) ----
+    std::vector<ServerReq *> &ready = ready_buf;
+    ready.clear();
+    for (ServerReq *r : S->active)
+      if (r->c->steps[r->cursor].stage < (int)r->picked.load(std::memory_order_acquire)) ready.push_back(r);
+    if (ready.empty()) {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_picked.wait_for(lk, std::chrono::microseconds(500));
+      continue;
+    }
     try {
       ts_server::Ring &R = S->ring[ri];
       if (R.used) CUDA_TRY(cudaEventSynchronize(R.ev));  // the slot's previous tick is done
+      for (ServerReq *r : ready) {
+        // items of the stages picked so far, in stream order before the launches
+        RunCtx &c = *r->c;
+        const uint32_t upto = r->picked.load(std::memory_order_acquire);
+        for (; r->uploaded < upto; ++r->uploaded) {
+          const StagePlan &sp = c.plan[r->uploaded];
+          if (sp.n_items)
+            CUDA_TRY(cudaMemcpyAsync(c.d_items.p + sp.items_off, c.pitems.p + sp.items_off,
+                                     (size_t)sp.n_items * 4, cudaMemcpyHostToDevice, S->st));
+        }
+      }
       uint64_t step_items = 0;
       bool all_team_full = true;
-      for (ServerReq *r : S->active) {
+      for (ServerReq *r : ready) {
         const Step &stp = r->c->steps[r->cursor];
         if (stp.batch) {
           step_items += stp.n;
@@ -2734,55 +2802,67 @@ void server_driver(ts_server *S) {
       segs.clear();
       fb.clear();
       launches.clear();
-      for (ServerReq *r : S->active) r->c->steps[r->cursor].resolve = form;
-      for (int ph = 0; ph < kPhases; ++ph) {
-        PlannedLaunch pl;
-        pl.phase = ph;
-        pl.seg0 = (uint32_t)segs.size();
-        pl.n_segs = pl.blocks = 0;
-        pl.smem = 0;
-        pl.fb0 = (uint32_t)fb.size();
-        for (ServerReq *r : S->active) {
-          const RunCtx &c = *r->c;
-          const Step &stp = c.steps[r->cursor];
-          if (ph == kPhaseExhaustive && stp.batch && c.k > 0 && !stp.exhaustive) {
-            fb.push_back(Segment{0, 0, r->slot, (uint32_t)r->cursor});
-            pl.n_fb += 1;
+      for (ServerReq *r : ready) r->c->steps[r->cursor].resolve = form;
+      uint64_t tick_launches = 0;
+      if (ready.size() == 1) {
+        // one session in the tick: its step with the single-session kernels
+        // (no segment lookups at the start of every block)
+        RunCtx &c = *ready[0]->c;
+        const uint64_t before = c.launches;
+        LaunchTimer lt;
+        enqueue_step(c, c.steps[ready[0]->cursor], S->st, lt);
+        tick_launches = c.launches - before;
+      } else {
+        for (int ph = 0; ph < kPhases; ++ph) {
+          PlannedLaunch pl;
+          pl.phase = ph;
+          pl.seg0 = (uint32_t)segs.size();
+          pl.n_segs = pl.blocks = 0;
+          pl.smem = 0;
+          pl.fb0 = (uint32_t)fb.size();
+          for (ServerReq *r : ready) {
+            const RunCtx &c = *r->c;
+            const Step &stp = c.steps[r->cursor];
+            if (ph == kPhaseExhaustive && stp.batch && c.k > 0 && !stp.exhaustive) {
+              fb.push_back(Segment{0, 0, r->slot, (uint32_t)r->cursor});
+              pl.n_fb += 1;
+              pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
+            }
+            const uint32_t nb = multi_blocks(ph, phase_units(stp, c, ph), phase_cap(stp, ph));
+            if (nb == 0) continue;
+            segs.push_back(Segment{pl.blocks, nb, r->slot, (uint32_t)r->cursor});
+            pl.blocks += nb;
+            pl.n_segs += 1;
             pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
           }
-          const uint32_t nb = multi_blocks(ph, phase_units(stp, c, ph), phase_cap(stp, ph));
-          if (nb == 0) continue;
-          segs.push_back(Segment{pl.blocks, nb, r->slot, (uint32_t)r->cursor});
-          pl.blocks += nb;
-          pl.n_segs += 1;
-          pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
-        }
-        pl.pool_block0 = pl.blocks;
-        if (pl.n_fb) pl.blocks += kFallbackPool;
-        if (pl.n_segs || pl.n_fb) {
-          if (pl.smem > phase_smem[ph]) {
-            CUDA_TRY(set_multi_smem(ph, pl.smem));
-            phase_smem[ph] = pl.smem;
+          pl.pool_block0 = pl.blocks;
+          if (pl.n_fb) pl.blocks += kFallbackPool;
+          if (pl.n_segs || pl.n_fb) {
+            if (pl.smem > phase_smem[ph]) {
+              CUDA_TRY(set_multi_smem(ph, pl.smem));
+              phase_smem[ph] = pl.smem;
+            }
+            launches.push_back(pl);
           }
-          launches.push_back(pl);
         }
-      }
-      const size_t nseg = segs.size() + fb.size();
-      if (nseg > S->seg_cap) throw Failure{TS_ERR_LIMIT, "segment table overflow"};
-      std::copy(segs.begin(), segs.end(), R.h);
-      std::copy(fb.begin(), fb.end(), R.h + segs.size());
-      if (nseg)
-        CUDA_TRY(cudaMemcpyAsync(R.d.p, R.h, nseg * sizeof(Segment), cudaMemcpyHostToDevice, S->st));
-      for (const PlannedLaunch &pl : launches) {
-        MultiLaunch ml;
-        ml.segs = R.d.p + pl.seg0;
-        ml.n_segs = pl.n_segs;
-        ml.sessions = S->d_sess.p;
-        ml.step_tabs = S->d_tabs.p;
-        ml.fb = R.d.p + segs.size() + pl.fb0;
-        ml.n_fb = pl.n_fb;
-        ml.pool_block0 = pl.n_fb ? pl.pool_block0 : pl.blocks;
-        launch_multi(pl.phase, ml, pl.blocks, pl.smem, S->st);
+        const size_t nseg = segs.size() + fb.size();
+        if (nseg > S->seg_cap) throw Failure{TS_ERR_LIMIT, "segment table overflow"};
+        // the kernels read the tick's segment table straight from pinned host
+        // memory (no copy in the stream between ticks)
+        std::copy(segs.begin(), segs.end(), R.h);
+        std::copy(fb.begin(), fb.end(), R.h + segs.size());
+        for (const PlannedLaunch &pl : launches) {
+          MultiLaunch ml;
+          ml.segs = R.h + pl.seg0;
+          ml.n_segs = pl.n_segs;
+          ml.sessions = S->d_sess.p;
+          ml.step_tabs = S->d_tabs.p;
+          ml.fb = R.h + segs.size() + pl.fb0;
+          ml.n_fb = pl.n_fb;
+          ml.pool_block0 = pl.n_fb ? pl.pool_block0 : pl.blocks;
+          launch_multi(pl.phase, ml, pl.blocks, pl.smem, S->st);
+        }
+        tick_launches = launches.size();
       }
       CUDA_TRY(cudaGetLastError());
       CUDA_TRY(cudaEventRecord(R.ev, S->st));
@@ -2792,6 +2872,10 @@ void server_driver(ts_server *S) {
       std::vector<ServerReq *> still;
       std::vector<ServerReq *> finished;
       for (ServerReq *r : S->active) {
+        if (std::find(ready.begin(), ready.end(), r) == ready.end()) {
+          still.push_back(r);
+          continue;
+        }
         RunCtx &c = *r->c;
         const Step &stp = c.steps[r->cursor];
         if (stp.batch) {
@@ -2809,7 +2893,7 @@ void server_driver(ts_server *S) {
       {
         std::lock_guard<std::mutex> lk(S->mu);
         S->stats.ticks += 1;
-        S->stats.launches += launches.size();
+        S->stats.launches += tick_launches;
         for (ServerReq *r : finished) S->completing.push_back(r);
         if (!finished.empty()) S->cv_complete.notify_one();
       }
@@ -2857,6 +2941,10 @@ void server_completer(ts_server *S) {
     }
     const bool admitted = r->slotted;
     if (r->ev) cudaEventSynchronize(r->ev);  // no kernel of the request is left
+    {
+      std::unique_lock<std::mutex> lk(S->mu);  // nor is its picker (after a failure)
+      S->cv_picked.wait(lk, [&] { return r->picks_done; });
+    }
     // the run's buffers are pool memory (freed in stream order, no device
     // wait); the session's pyramids are freed with it
     r->c.reset();
@@ -2908,7 +2996,6 @@ ts_server *ts_server_new(int32_t device, uint64_t hbm_budget_bytes, uint32_t max
     S->seg_cap = S->max_active * (kPhases + 1);
     for (auto &R : S->ring) {
       CUDA_TRY(cudaMallocHost((void **)&R.h, S->seg_cap * sizeof(Segment)));
-      CUDA_TRY(R.d.alloc(S->seg_cap));
       CUDA_TRY(cudaEventCreateWithFlags(&R.ev, cudaEventDisableTiming));
     }
   } catch (const Failure &) {
@@ -2919,6 +3006,8 @@ ts_server *ts_server_new(int32_t device, uint64_t hbm_budget_bytes, uint32_t max
   S->t0 = host_ms();
   S->driver = std::thread(server_driver, S.get());
   S->completer = std::thread(server_completer, S.get());
+  const unsigned hc = std::max(1u, std::thread::hardware_concurrency());
+  for (unsigned i = 0; i < std::min(4u, std::max(1u, hc / 4)); ++i) S->pickers.emplace_back(server_picker, S.get());
   return S.release();
 }
 
@@ -2936,12 +3025,18 @@ void ts_server_free(ts_server *S) {
     S->cv_complete.notify_all();
   }
   if (S->completer.joinable()) S->completer.join();
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop_pickers = true;
+    S->cv_pick.notify_all();
+  }
+  for (auto &t : S->pickers)
+    if (t.joinable()) t.join();
   for (auto &kv : S->reqs) delete kv.second;
   if (S->st) cudaStreamSynchronize(S->st);
   for (auto &R : S->ring) {
     if (R.h) cudaFreeHost(R.h);
     if (R.ev) cudaEventDestroy(R.ev);
-    R.d.reset();
   }
   S->d_sess.reset();
   S->d_tabs.reset();
@@ -2981,13 +3076,18 @@ int ts_server_submit(ts_server *S, ts_session *s, uint64_t *ticket) {
   r->t_submit = host_ms() - S->t0;
   r->c.reset(new RunCtx());
   try {
-    run_plan(r->s, *r->c);  // host schedule, on the caller's thread
-    run_pick_all(*r->c);
+    RunCtx &c = *r->c;
+    run_plan(r->s, c);  // host schedule, on the caller's thread
+    c.items_async = true;
+    if (cudaSuccess != c.pitems.alloc(c.items.size())) throw Failure{TS_ERR_CUDA, "pinned host memory"};
+    if (!c.plan.empty()) server_pick_stage(*r);  // stage 0 here, the rest on a picker thread
   } catch (const Failure &f) {
     S->err = f.msg;
     return f.status;
   }
   r->bytes = r->c->dev_bytes + r->s->dev_bytes;
+  const bool more = r->picked.load() < r->c->plan.size();
+  r->picks_done = !more;
   std::lock_guard<std::mutex> lk(S->mu);
   if (S->fatal) {
     S->err = "server stopped after a device error";
@@ -2996,6 +3096,10 @@ int ts_server_submit(ts_server *S, ts_session *s, uint64_t *ticket) {
   r->ticket = S->next_ticket++;
   *ticket = r->ticket;
   S->reqs[r->ticket] = r.get();
+  if (more) {
+    S->to_pick.push_back(r.get());
+    S->cv_pick.notify_one();
+  }
   S->pending.push_back(r.release());
   S->stats.submitted += 1;
   S->cv_work.notify_one();
