@@ -170,6 +170,64 @@ __device__ __forceinline__ unsigned long long nb_key(uint32_t d2, int x, int y) 
 // Items for which the table holds fewer than k points (sparse steps, image
 // edges) go to the exhaustive k-NN; sparse steps send every item there.
 // ---------------------------------------------------------------------------
+// Walk window: the bitmap square [-R, R]^2 around an item (R the table
+// radius), kWinWords 32-bit words per row, bit i of word w of row r = point
+// (px - R + 32w + i, py - R + r).
+constexpr int kWinRows = 2 * kKnnTabRadius + 1;
+constexpr int kWinWords = (2 * kKnnTabRadius + 1 + 31) / 32;
+constexpr uint32_t kWalkDirect = 128;  // expected entries still to scan above which the window is built
+constexpr size_t kWalkWinBytes = (size_t)kWalkWarps * kWinRows * kWinWords * 4;  // dynamic shared memory
+
+// Bits of bitmap row `row` for x in [x0, x0 + 32) (bit i = x0 + i), zero
+// outside [0, W).
+__device__ __forceinline__ uint32_t row_bits(const uint32_t *row, int x0, const SessionDev &s) {
+  const int W = (int)s.W;
+  if (x0 >= W || x0 + 32 <= 0) return 0u;
+  const int q = x0 >> 5, sh = x0 & 31;  // floor division
+  const uint32_t lo = (q >= 0 && q < (int)s.wpr) ? __ldg(&row[q]) : 0u;
+  const uint32_t hi = (sh && q + 1 >= 0 && q + 1 < (int)s.wpr) ? __ldg(&row[q + 1]) : 0u;
+  uint32_t v = sh ? (lo >> sh) | (hi << (32 - sh)) : lo;
+  if (x0 < 0) v &= ~0u << (-x0);
+  if (x0 + 32 > W) v &= (1u << (W - x0)) - 1u;
+  return v;
+}
+
+// Bits i with lo <= i < hi of a 32-bit word (lo, hi clamped to [0, 32]).
+__device__ __forceinline__ uint32_t bit_range(int lo, int hi) {
+  lo = max(lo, 0);
+  hi = min(hi, 32);
+  if (hi <= lo) return 0u;
+  const uint32_t upto_hi = hi >= 32 ? ~0u : ((1u << hi) - 1u);
+  return upto_hi & (~0u << lo);
+}
+
+// occupied() for the 32 points (x0 + i, y), i = 0..31, as a word.
+__device__ __forceinline__ uint32_t window_word(const SessionDev &s, int x0, int y) {
+  const int W = (int)s.W, H = (int)s.H;
+  if ((unsigned)y < s.H) {
+    uint32_t v = row_bits(s.occ + (size_t)y * s.wpr, x0, s);
+    if (s.tiling) {
+      const uint32_t *mr = s.mir + (size_t)y * s.wpr;
+      // x >= W: mirror of xs = x - W when xs < x_l
+      v |= row_bits(mr, x0 - W, s) & bit_range(0, s.x_l - (x0 - W));
+      // x < 0: mirror of xs = x + W when xs > x_r
+      v |= row_bits(mr, x0 + W, s) & bit_range(s.x_r + 1 - (x0 + W), 32);
+    }
+    return v;
+  }
+  if (!s.tiling) return 0u;
+  if (y >= H) {
+    const int ys = y - H;
+    return ys < s.y_b ? row_bits(s.mir + (size_t)ys * s.wpr, x0, s) : 0u;
+  }
+  const int ys = y + H;
+  return (ys >= 0 && ys > s.y_t) ? row_bits(s.mir + (size_t)ys * s.wpr, x0, s) : 0u;
+}
+
+// kWin: small (latency-bound) steps, whose sparse items switch to a
+// window in dynamic shared memory (kWalkWinBytes) once the hits so far say
+// more than two further rounds are needed.
+template <bool kWin>
 __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t vb,
                                               uint32_t vg) {
   const int lane = threadIdx.x & 31;
@@ -181,14 +239,15 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
     const double x2 = s.xdiv[px + s.xdiv_off], y2 = s.ydiv[py + s.ydiv_off];
     int32_t *nbo = b.nbuf + (size_t)local * s.k;
     uint32_t count = 0;
+    const uint32_t tab_n = b.grid_first ? 0u : s.knn_tab_n;
     // 64 table entries per round, two per lane, both looked up before either
-    // is used
-    for (uint32_t c = 0; c < (b.grid_first ? 0u : s.knn_tab_n); c += 2 * kWarp) {
+    // is used; `hit` answers membership for an offset
+    auto round = [&](uint32_t c, auto &&hit) {
       const uint32_t i0 = c + lane, i1 = c + kWarp + lane;
-      const int32_t o0 = i0 < s.knn_tab_n ? __ldg(&s.knn_tab[i0]) : 0;
-      const int32_t o1 = i1 < s.knn_tab_n ? __ldg(&s.knn_tab[i1]) : 0;
-      const bool h0 = i0 < s.knn_tab_n && occupied(s, px + off_dx(o0), py + off_dy(o0));
-      const bool h1 = i1 < s.knn_tab_n && occupied(s, px + off_dx(o1), py + off_dy(o1));
+      const int32_t o0 = i0 < tab_n ? __ldg(&s.knn_tab[i0]) : 0;
+      const int32_t o1 = i1 < tab_n ? __ldg(&s.knn_tab[i1]) : 0;
+      const bool h0 = i0 < tab_n && hit(off_dx(o0), off_dy(o0));
+      const bool h1 = i1 < tab_n && hit(off_dx(o1), off_dy(o1));
       const uint32_t b0 = __ballot_sync(0xffffffffu, h0);
       const uint32_t b1 = __ballot_sync(0xffffffffu, h1);
       const uint32_t r0 = count + __popc(b0 & lt), r1 = count + __popc(b0) + __popc(b1 & lt);
@@ -201,7 +260,35 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
         b.dist[(size_t)r1 * nb + local] = neighbour_dist(s, px, py, off_dx(o1), off_dy(o1), x2, y2);
       }
       count += __popc(b0) + __popc(b1);
+    };
+    // rounds look the bitmap up directly while the hits so far say that
+    // two more rounds or fewer will do (dense steps end here)
+    uint32_t c = 0;
+    while (c < tab_n) {
+      round(c, [&](int dx, int dy) { return occupied(s, px + dx, py + dy); });
+      c += 2 * kWarp;
       if (count >= s.k) break;
+      if (kWin && (count == 0 || (uint64_t)(s.k - count) * c > (uint64_t)count * kWalkDirect)) break;
+    }
+    if (kWin && count < s.k && c < tab_n) {
+      // sparse: the membership bits of the whole table's square, built in
+      // one pass of independent loads, then the rest of the walk from
+      // shared memory
+      extern __shared__ uint32_t walk_win[];
+      uint32_t *win = walk_win + (threadIdx.x >> 5) * (kWinRows * kWinWords);
+      for (uint32_t wi = lane; wi < kWinRows * kWinWords; wi += kWarp) {
+        const int row = (int)(wi / kWinWords), word = (int)(wi - row * kWinWords);
+        win[wi] = window_word(s, px - kKnnTabRadius + 32 * word, py - kKnnTabRadius + row);
+      }
+      __syncwarp();
+      for (; c < tab_n; c += 2 * kWarp) {
+        round(c, [&](int dx, int dy) {
+          const int i = dx + kKnnTabRadius;
+          return ((win[(dy + kKnnTabRadius) * kWinWords + (i >> 5)] >> (i & 31)) & 1u) != 0u;
+        });
+        if (count >= s.k) break;
+      }
+      __syncwarp();  // the window is rebuilt for the warp's next item
     }
     if (lane == 0) {
       if (count >= s.k) {
@@ -1731,14 +1818,15 @@ __global__ void k_random_candidates_multi(MultiLaunch ml) {
   random_candidates_body(*v.s, v.d->rc, v.vb);
 }
 
+template <bool kWin>
 __global__ void __launch_bounds__(kWalkWarps *kWarp, 4) k_knn_walk(SessionDev s, StageDev st, BatchDev b) {
   pdl_enter();
-  knn_walk_body(s, st, b, blockIdx.x, gridDim.x);
+  knn_walk_body<kWin>(s, st, b, blockIdx.x, gridDim.x);
 }
 __global__ void __launch_bounds__(kWalkWarps *kWarp, 4) k_knn_walk_multi(MultiLaunch ml) {
   pdl_enter();
   const SegView v = find_segment(ml);
-  knn_walk_body(*v.s, v.d->st, v.d->b, v.vb, v.vg);
+  knn_walk_body<false>(*v.s, v.d->st, v.d->b, v.vb, v.vg);
 }
 
 __global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive(SessionDev s, StageDev st, BatchDev b,
@@ -1981,7 +2069,10 @@ void launch_random_candidates(const SessionDev &s, const StageDev &st, cudaStrea
 void launch_knn_walk(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
   const uint32_t n = b.i1 - b.i0;
   if (n == 0) return;
-  launch_pdl(k_knn_walk, cdiv(n, kWalkWarps), kWalkWarps * kWarp, 0, stream, s, st, b);
+  if (b.walk_window)
+    launch_pdl(k_knn_walk<true>, cdiv(n, kWalkWarps), kWalkWarps * kWarp, kWalkWinBytes, stream, s, st, b);
+  else
+    launch_pdl(k_knn_walk<false>, cdiv(n, kWalkWarps), kWalkWarps * kWarp, 0, stream, s, st, b);
 }
 
 void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchDev &b, bool all_items,

@@ -96,6 +96,10 @@ struct SessionDev {
 
 constexpr int kCell = 8;
 
+// Radius of the sorted k-NN offset table: every lattice offset with
+// dx^2 + dy^2 <= kKnnTabRadius^2.
+constexpr int kKnnTabRadius = 36;
+
 struct StageDev {
   uint32_t level;
   int slow_lut;            // LUT holds a non-finite value: exact sequential argmin
@@ -119,6 +123,7 @@ struct BatchDev {
   double *mean;          // [batch] mean of the 4x-duplicated distance list
   Result *res;           // [batch]
   int grid_first;        // sparse step: search the cell grid without walking the offset table first
+  int walk_window;       // small step (latency-bound): the single-session walk lets sparse items walk a shared-memory bitmap window
 };
 
 // One batch step of one session as the multi-session kernels read it.

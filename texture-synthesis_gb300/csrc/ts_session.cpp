@@ -44,9 +44,11 @@ constexpr uint32_t kMaxM = 1024;
 constexpr uint32_t kMaxExamples = 256;
 constexpr uint32_t kMaxSide = 16384;
 constexpr float kTilingBoundary = 0.05f;  // TILING_BOUNDARY_PERCENTAGE, ms.rs:15
-constexpr int kKnnTabRadius = 36;
 constexpr int kDistTabRadius = 64;  // offsets the weight tables cover
 constexpr uint64_t kRcandBudget = 64ull << 20;  // random-candidate entries held at once
+// Walk steps of at most this many items are latency-bound: their sparse items
+// build a bitmap window instead of more rounds of bitmap loads.
+constexpr uint32_t kWalkWindowItems = 4096;
 // Runs whose random candidates for every stage fit this many entries make
 // them all ahead, on a side stream, while the first stages run.
 constexpr uint64_t kRcandWhole = 256ull << 20;
@@ -1688,6 +1690,7 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
         stp.n = bp.i1 - bp.i0;
         stp.exhaustive = bp.exhaustive;
         bd.grid_first = bp.grid_first ? 1 : 0;
+        bd.walk_window = (bp.i1 - bp.i0) <= kWalkWindowItems ? 1 : 0;
         if (stp.n <= p.team_max_batch)
           stp.resolve = (stp.n <= p.team_full_max_batch && team_full_fits(k, m)) ? kPhaseTeamFull : kPhaseTeamPart;
         else
