@@ -255,7 +255,7 @@ int ts_builder_batch_schedule(ts_builder *b, uint32_t batch_divisor, uint32_t ma
  * at most `full_max_batch` items score every candidate of an item with one
  * CTA (lowest latency); up to `team_max_batch` items, one CTA per item with
  * early exit; larger batches, one warp per item (highest throughput).
- * Defaults 8192 and 1024. */
+ * Defaults 2048 and 256. */
 int ts_builder_resolve_team(ts_builder *b, uint32_t team_max_batch, uint32_t full_max_batch);
 /* CUDA device ordinal (default 0). */
 int ts_builder_device(ts_builder *b, int32_t device);
@@ -326,8 +326,8 @@ int ts_batch_profile(ts_batch *b, int32_t on);
 int ts_batch_plan_threads(ts_batch *b, uint32_t n);
 /* Resolve kernel form per batch step from the step's items summed over all
  * sessions: one CTA per item up to team_max_items (every candidate scored
- * in full up to full_max_items), one warp per item above.  Defaults 8192
- * and 1024; the results do not depend on them. */
+ * in full up to full_max_items), one warp per item above.  Defaults 2048
+ * and 256; the results do not depend on them. */
 int ts_batch_resolve_team(ts_batch *b, uint32_t team_max_items, uint32_t full_max_items);
 /* Runs every added session; out[i] receives the result of the i-th added
  * session (free each with ts_generated_free).  The batch is then empty and

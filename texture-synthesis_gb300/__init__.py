@@ -418,7 +418,7 @@ class SessionBuilder:
     def device(self, ordinal):
         return self._check(lib().ts_builder_device(self._h, int(ordinal)))
 
-    def resolve_team(self, max_batch, full_max_batch=1024):
+    def resolve_team(self, max_batch, full_max_batch=256):
         """Resolve kernel forms by batch size (identical results): up to
         full_max_batch items, one CTA scores every candidate of an item; up to
         max_batch, one CTA per item with early exit; above, a warp per item."""
@@ -705,7 +705,7 @@ class CoordinateTransform:
 
 
 def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0, profile=False, team_max_batch=None,
-                      team_full_max_batch=1024):
+                      team_full_max_batch=256):
     """A SessionBuilder for a workload spec dict (see workloads.py)."""
     p = spec["params"]
     b = Session.builder()
@@ -742,7 +742,7 @@ def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0, profile=Fals
     return b
 
 
-def run_spec(spec, batch_divisor=8, max_batch=0, device=0, team_max_batch=None, team_full_max_batch=1024):
+def run_spec(spec, batch_divisor=8, max_batch=0, device=0, team_max_batch=None, team_full_max_batch=256):
     """Build and run a workload spec; returns a dict shaped like the oracle's."""
     g = builder_from_spec(spec, batch_divisor, max_batch, device, team_max_batch=team_max_batch,
                           team_full_max_batch=team_full_max_batch).build().run()

@@ -322,40 +322,44 @@ TS_HD uint64_t ts_add_rn(uint64_t bx, uint64_t by) {
 // RN(RN(RN(RN(s + d) + d) + d) + d).  When all four sums stay in s's binade,
 // s is on that binade's grid u and every step adds d rounded to u: the bit
 // pattern advances by 4 * round(d / u) (exact ties alternate by parity).
-TS_HD uint64_t ts_add4_rn(uint64_t bs, uint64_t bd) {
-  if (bd == 0) return bs;
-  if (bs != 0 && bs > bd) {
-    const uint32_t es = (uint32_t)(bs >> 52), ed = (uint32_t)(bd >> 52);
-    const uint32_t sh = es - ed;
-    uint64_t a, rem, half;
-    if (sh >= 54) {
-      a = 0;
-      rem = 1;  // below half an ulp: rounds down
-      half = 2;
-    } else if (sh >= 1) {
-      const uint64_t md = (bd & kFrac52) | (1ULL << 52);
-      a = md >> sh;
-      rem = md & ((1ULL << sh) - 1);
-      half = 1ULL << (sh - 1);
-    } else {
-      a = 0;
-      rem = 0;
-      half = 0;  // same binade: not this path
-    }
-    if (sh >= 1) {
-      const bool tie = rem == half;
-      const uint64_t step = a + (rem > half ? 1u : 0u);
-      if ((bs & kFrac52) + 4 * (a + 1) < (1ULL << 52)) {
-        if (!tie) return bs + 4 * step;
-        uint64_t b = bs;
-        for (int i = 0; i < 4; ++i) {
-          b += a;
-          b += b & 1u;  // the tie goes to the even neighbour
-        }
-        return b;
-      }
-    }
+// ts_add4_fast handles that case (and d = 0) and returns false otherwise.
+TS_HD bool ts_add4_fast(uint64_t bs, uint64_t bd, uint64_t &out) {
+  if (bd == 0) {
+    out = bs;
+    return true;
   }
+  if (bs == 0 || bs <= bd) return false;
+  const uint32_t es = (uint32_t)(bs >> 52), ed = (uint32_t)(bd >> 52);
+  const uint32_t sh = es - ed;
+  if (sh == 0) return false;  // same binade: a carry is likely
+  uint64_t a, rem, half;
+  if (sh >= 54) {
+    a = 0;
+    rem = 1;  // below half an ulp: rounds down
+    half = 2;
+  } else {
+    const uint64_t md = (bd & kFrac52) | (1ULL << 52);
+    a = md >> sh;
+    rem = md & ((1ULL << sh) - 1);
+    half = 1ULL << (sh - 1);
+  }
+  if ((bs & kFrac52) + 4 * (a + 1) >= (1ULL << 52)) return false;  // may leave the binade
+  if (rem != half) {
+    out = bs + 4 * (a + (rem > half ? 1u : 0u));
+    return true;
+  }
+  uint64_t b = bs;
+  for (int i = 0; i < 4; ++i) {
+    b += a;
+    b += b & 1u;  // the tie goes to the even neighbour
+  }
+  out = b;
+  return true;
+}
+
+TS_HD uint64_t ts_add4_rn(uint64_t bs, uint64_t bd) {
+  uint64_t out;
+  if (ts_add4_fast(bs, bd, out)) return out;
   bs = ts_add_rn(bs, bd);
   bs = ts_add_rn(bs, bd);
   bs = ts_add_rn(bs, bd);

@@ -723,9 +723,23 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
   if (with_mean) {
     __syncthreads();
     if (threadIdx.x == 0 && nout > 0) {  // the mean (ms.rs:417-423), as k_mean computes it
+      // one thread: the four adds of a distance in integer arithmetic while
+      // the sum stays in its binade, else four f64 adds (64 cycles each)
       uint64_t acc = 0;
-      for (uint32_t i = 0; i < nout; ++i) acc = ts_add4_rn(acc, dbl_bits(sh.dist[i]));
-      b.mean[local] = bits_dbl(ts_div_int_rn(acc, nout * 4u));
+      for (uint32_t i = 0; i < nout; ++i) {
+        const double d = sh.dist[i];
+        uint64_t nx;
+        if (!ts_add4_fast(acc, dbl_bits(d), nx)) {
+          double a = bits_dbl(acc);
+          a = __dadd_rn(a, d);
+          a = __dadd_rn(a, d);
+          a = __dadd_rn(a, d);
+          a = __dadd_rn(a, d);
+          nx = dbl_bits(a);
+        }
+        acc = nx;
+      }
+      b.mean[local] = __ddiv_rn(bits_dbl(acc), (double)(nout * 4u));
     }
   }
   if (threadIdx.x == 0) b.ncnt[local] = nout;

@@ -95,8 +95,8 @@ struct Params {
   uint32_t max_batch = 0;
   int device = 0;
   bool profile = false;
-  uint32_t team_max_batch = 8192;
-  uint32_t team_full_max_batch = 1024;
+  uint32_t team_max_batch = 2048;
+  uint32_t team_full_max_batch = 256;
 };
 
 std::string fmt_float(float v) {
@@ -2044,7 +2044,7 @@ struct ts_batch {
   bool graph = false;
   bool profile = false;
   uint32_t plan_threads = 0;
-  uint32_t team_max_items = 8192, team_full_max_items = 1024;
+  uint32_t team_max_items = 2048, team_full_max_items = 256;
   ts_batch_stats stats{};
   std::string err;
 };
@@ -2621,7 +2621,7 @@ struct ts_server {
   int device = 0;
   uint64_t budget = 0;
   uint32_t max_active = 0;
-  uint32_t team_max_items = 8192, team_full_max_items = 1024;
+  uint32_t team_max_items = 2048, team_full_max_items = 256;
   double t0 = 0;
   std::mutex mu;
   std::condition_variable cv_work, cv_done, cv_complete, cv_pick, cv_picked;
