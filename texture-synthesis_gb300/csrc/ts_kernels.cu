@@ -1049,11 +1049,67 @@ __device__ void sequential_best(const SessionDev &s, const StageDev &st, const W
   }
 }
 
+__device__ __forceinline__ void add_cell_point(const SessionDev &s, int x, int y) {
+  atomicAdd(&s.cells[(size_t)((y - s.coy) / kCell) * s.cgw + (x - s.cox) / kCell], 1u);
+}
+
+// update + flush_resolved of one item (ms.rs:296-377): its colour and state,
+// its place in the resolved list, the bitmap, mirrors and cell counts.
+__device__ __forceinline__ void commit_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
+                                            const Result &r) {
+  const uint32_t p = r.pixel;
+  if (r.cmap >= s.n_maps || p >= s.W * s.H) {
+    set_err(s.err, kDevErrIndex);
+    return;
+  }
+  const MapDesc md = s.maps[r.cmap];
+  const uint32_t sx = r.srcxy & 0xffffu, sy = r.srcxy >> 16;
+  if (sx >= md.w || sy >= md.h) {
+    set_err(s.err, kDevErrIndex);
+    return;
+  }
+  s.state[p] = make_uint4(r.srcxy, r.idp, r.idm, r.cmap);
+  s.color[p] = s.levels[md.off + (size_t)st.level * md.w * md.h + (size_t)sy * md.w + sx];
+  if (r.ncand) atomicAdd(s.evals, (unsigned long long)r.ncand);
+  if (r.flags & kResAppend) {
+    const uint32_t item = b.i0 + local;
+    const uint32_t pos = b.n_res + (item - b.append_from);
+    s.resolved[pos] = p;
+    s.rscore[pos] = r.score;
+    const uint32_t x = p % s.W, y = p / s.W;
+    atomicOr(&s.occ[(size_t)y * s.wpr + (x >> 5)], 1u << (x & 31));
+    add_cell_point(s, (int)x, (int)y);
+    if (s.tiling && (r.flags & kResMirrors)) {
+      atomicOr(&s.mir[(size_t)y * s.wpr + (x >> 5)], 1u << (x & 31));
+      // the tree's mirror copies (flush_resolved, ms.rs:306-328)
+      if ((int)x < s.x_l)
+        add_cell_point(s, (int)x + (int)s.W, (int)y);
+      else if ((int)x > s.x_r)
+        add_cell_point(s, (int)x - (int)s.W, (int)y);
+      if ((int)y < s.y_b)
+        add_cell_point(s, (int)x, (int)y + (int)s.H);
+      else if ((int)y > s.y_t)
+        add_cell_point(s, (int)x, (int)y - (int)s.H);
+    }
+  }
+}
+
+// An item's result: committed at once when the batch holds only new items
+// (b.fused_commit: no item of the batch is in the tree, so no other item
+// reads its pixel, state or bit during the batch), else kept for k_commit.
+__device__ __forceinline__ void emit_result(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
+                                            const Result &r) {
+  if (b.fused_commit)
+    commit_item(s, st, b, local, r);
+  else
+    b.res[local] = r;
+}
+
 // The winning candidate as an update (ms.rs:976-1001): source coordinate and
 // map, patch id (the neighbour's for coherence candidates, the example flat
 // index for random ones), score.
-__device__ void write_result(const SessionDev &s, const WarpSmem &w, const BatchDev &b, uint32_t local,
-                             uint32_t pixel, int px, int py, bool is_new, uint32_t nc, float best_s,
+__device__ void write_result(const SessionDev &s, const StageDev &st, const WarpSmem &w, const BatchDev &b,
+                             uint32_t local, uint32_t pixel, int px, int py, bool is_new, uint32_t nc, float best_s,
                              uint32_t best_i) {
   const uint32_t aux = w.caux[best_i];
   const uint32_t map = aux & 0x7fffu;
@@ -1076,7 +1132,7 @@ __device__ void write_result(const SessionDev &s, const WarpSmem &w, const Batch
   r.flags = (is_new ? kResAppend : 0u) | kResMirrors;
   r.score = best_s;
   r.ncand = nc;
-  b.res[local] = r;
+  emit_result(s, st, b, local, r);
 }
 
 // Result for an item with no resolved neighbour: resolve_at_random with the
@@ -1103,12 +1159,13 @@ __device__ void write_random_result(const SessionDev &s, const StageDev &st, con
   r.flags = kResAppend;
   r.score = 0.0f;
   r.ncand = 0;
-  b.res[local] = r;
+  emit_result(s, st, b, local, r);
 }
 
 // A result that commit skips (an invalid map id was met; the reference
 // panics there).
-__device__ void write_bad_result(const SessionDev &s, const BatchDev &b, uint32_t local, uint32_t pixel) {
+__device__ void write_bad_result(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
+                                 uint32_t pixel) {
   set_err(s.err, kDevErrIndex);
   Result r;
   r.pixel = pixel;
@@ -1119,7 +1176,7 @@ __device__ void write_bad_result(const SessionDev &s, const BatchDev &b, uint32_
   r.flags = 0;
   r.score = 0.0f;
   r.ncand = 0;
-  b.res[local] = r;
+  emit_result(s, st, b, local, r);
 }
 
 __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t vb,
@@ -1198,7 +1255,7 @@ __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev
     if (__any_sync(0xffffffffu, bad_map)) {
       // the reference panics on this index; record the error and leave the
       // pixel untouched (commit skips results with an invalid map)
-      if (lane == 0) write_bad_result(s, b, local, pixel);
+      if (lane == 0) write_bad_result(s, st, b, local, pixel);
       continue;
     }
     // random candidates after the coherence ones
@@ -1255,7 +1312,7 @@ __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev
     } else if (lane == 0) {
       sequential_best(s, st, w, lc, lg, nk, nc, best_s, best_i);
     }
-    if (lane == 0) write_result(s, w, b, local, pixel, px, py, is_new, ncoh_all + s.m, best_s, best_i);
+    if (lane == 0) write_result(s, st, w, b, local, pixel, px, py, is_new, ncoh_all + s.m, best_s, best_i);
   }
 }
 
@@ -1350,7 +1407,7 @@ __device__ __forceinline__ void resolve_team_body(const SessionDev &s, const Sta
     }
     __syncthreads();
     if (sh_flags & 2) {
-      if (tid == 0) write_bad_result(s, b, local, pixel);
+      if (tid == 0) write_bad_result(s, st, b, local, pixel);
       __syncthreads();
       continue;
     }
@@ -1551,56 +1608,18 @@ __device__ __forceinline__ void resolve_team_body(const SessionDev &s, const Sta
     } else if (tid == 0) {
       sequential_best(s, st, w, lc, lg, nk, nc, best_s, best_i);
     }
-    if (tid == 0) write_result(s, w, b, local, pixel, px, py, is_new, nc, best_s, best_i);
+    if (tid == 0) write_result(s, st, w, b, local, pixel, px, py, is_new, nc, best_s, best_i);
     __syncthreads();
   }
 }
 
-// update + flush_resolved for a batch (ms.rs:296-377).
-__device__ __forceinline__ void add_cell_point(const SessionDev &s, int x, int y) {
-  atomicAdd(&s.cells[(size_t)((y - s.coy) / kCell) * s.cgw + (x - s.cox) / kCell], 1u);
-}
+// update + flush_resolved for a batch (ms.rs:296-377): one thread per item.
 
 __device__ __forceinline__ void commit_body(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t vb) {
   const uint32_t local = vb * blockDim.x + threadIdx.x;
   const uint32_t nb = b.i1 - b.i0;
   if (local >= nb) return;
-  const Result r = b.res[local];
-  const uint32_t p = r.pixel;
-  if (r.cmap >= s.n_maps || p >= s.W * s.H) {
-    set_err(s.err, kDevErrIndex);
-    return;
-  }
-  const MapDesc md = s.maps[r.cmap];
-  const uint32_t sx = r.srcxy & 0xffffu, sy = r.srcxy >> 16;
-  if (sx >= md.w || sy >= md.h) {
-    set_err(s.err, kDevErrIndex);
-    return;
-  }
-  s.state[p] = make_uint4(r.srcxy, r.idp, r.idm, r.cmap);
-  s.color[p] = s.levels[md.off + (size_t)st.level * md.w * md.h + (size_t)sy * md.w + sx];
-  if (r.ncand) atomicAdd(s.evals, (unsigned long long)r.ncand);
-  if (r.flags & kResAppend) {
-    const uint32_t item = b.i0 + local;
-    const uint32_t pos = b.n_res + (item - b.append_from);
-    s.resolved[pos] = p;
-    s.rscore[pos] = r.score;
-    const uint32_t x = p % s.W, y = p / s.W;
-    atomicOr(&s.occ[(size_t)y * s.wpr + (x >> 5)], 1u << (x & 31));
-    add_cell_point(s, (int)x, (int)y);
-    if (s.tiling && (r.flags & kResMirrors)) {
-      atomicOr(&s.mir[(size_t)y * s.wpr + (x >> 5)], 1u << (x & 31));
-      // the tree's mirror copies (flush_resolved, ms.rs:306-328)
-      if ((int)x < s.x_l)
-        add_cell_point(s, (int)x + (int)s.W, (int)y);
-      else if ((int)x > s.x_r)
-        add_cell_point(s, (int)x - (int)s.W, (int)y);
-      if ((int)y < s.y_b)
-        add_cell_point(s, (int)x, (int)y + (int)s.H);
-      else if ((int)y > s.y_t)
-        add_cell_point(s, (int)x, (int)y - (int)s.H);
-    }
-  }
+  commit_item(s, st, b, local, b.res[local]);
 }
 
 // next_pyramid_level (ms.rs:687-700)

@@ -124,6 +124,7 @@ struct BatchDev {
   Result *res;           // [batch]
   int grid_first;        // sparse step: search the cell grid without walking the offset table first
   int walk_window;       // small step (latency-bound): the single-session walk lets sparse items walk a shared-memory bitmap window
+  int fused_commit;      // only new items: the resolve kernels commit each item themselves (no k_commit)
 };
 
 // One batch step of one session as the multi-session kernels read it.

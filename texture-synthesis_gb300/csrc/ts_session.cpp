@@ -1691,6 +1691,9 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
         stp.exhaustive = bp.exhaustive;
         bd.grid_first = bp.grid_first ? 1 : 0;
         bd.walk_window = (bp.i1 - bp.i0) <= kWalkWindowItems ? 1 : 0;
+        // a batch of new items only: none of them is in the tree, so no item
+        // reads another's pixel, state or bit, and each commits as it resolves
+        bd.fused_commit = bp.i0 >= sp.redo ? 1 : 0;
         if (stp.n <= p.team_max_batch)
           stp.resolve = (stp.n <= p.team_full_max_batch && team_full_fits(k, m)) ? kPhaseTeamFull : kPhaseTeamPart;
         else
@@ -1776,8 +1779,11 @@ void enqueue_step(RunCtx &c, const Step &stp, cudaStream_t st, LaunchTimer &lt) 
       lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve(sd, stp.st, stp.bd, st); });
     else
       lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve_team(sd, stp.st, stp.bd, stp.resolve == kPhaseTeamFull, st); });
-    lt.run(TS_KERNEL_COMMIT, [&] { launch_commit(sd, stp.st, stp.bd, st); });
-    c.launches += 2;
+    c.launches += 1;
+    if (!stp.bd.fused_commit) {
+      lt.run(TS_KERNEL_COMMIT, [&] { launch_commit(sd, stp.st, stp.bd, st); });
+      c.launches += 1;
+    }
   }
 }
 
@@ -2063,7 +2069,7 @@ uint32_t phase_units(const Step &stp, const RunCtx &c, int phase) {
     case kPhaseResolve:
     case kPhaseTeamPart:
     case kPhaseTeamFull: return (stp.batch && stp.resolve == phase) ? stp.n : 0;
-    case kPhaseCommit: return stp.batch ? stp.n : 0;
+    case kPhaseCommit: return (stp.batch && !stp.bd.fused_commit) ? stp.n : 0;
     default: return 0;
   }
 }
