@@ -834,6 +834,8 @@ __device__ __forceinline__ float lut4(const float *lut, uint32_t d, float acc) {
 // abandoned.  The terms are never negative, so partial sums never decrease
 // and testing every fourth one, and the total, decides as the reference's
 // test after every term does.
+// kG = false compiles the guide terms out (sessions without guides).
+template <bool kG = true>
 __device__ __forceinline__ bool candidate_cost(const SessionDev &s, const StageDev &st, const WarpSmem &w,
                                                const float *lc, const float *lg, uint32_t nk, uint32_t cxy,
                                                uint32_t aux, float bound, float &out) {
@@ -844,7 +846,7 @@ __device__ __forceinline__ bool candidate_cost(const SessionDev &s, const StageD
   const int cx = (int)(cxy & 0xffffu), cy = (int)(cxy >> 16);
   const uint32_t *gv = nullptr;
   GuideDesc gd;
-  if (s.guided) {
+  if (kG && s.guided) {
     gd = s.gdesc[map];
     gv = s.guides + gd.off + (size_t)st.level * gd.w * gd.h;
   }
@@ -860,14 +862,14 @@ __device__ __forceinline__ bool candidate_cost(const SessionDev &s, const StageD
         nr[u] = w.nbr[j0 + u];
         const int qx = cx + sg * off_dx((int32_t)nr[u].x), qy = cy + sg * off_dy((int32_t)nr[u].x);
         if ((unsigned)qx < md.w && (unsigned)qy < md.h) t[u] = __ldg(&lv[(size_t)qy * md.w + qx]);
-        if (s.guided && (unsigned)qx < gd.w && (unsigned)qy < gd.h) gt[u] = __ldg(&gv[(size_t)qy * gd.w + qx]);
+        if (kG && s.guided && (unsigned)qx < gd.w && (unsigned)qy < gd.h) gt[u] = __ldg(&gv[(size_t)qy * gd.w + qx]);
       }
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       if (j0 + u >= nk) break;
       float nps = lut4(lc, __vabsdiffu4(nr[u].y, t[u]), 0.0f);
-      if (s.guided) nps = lut4(lg, __vabsdiffu4(nr[u].z, gt[u]), nps);
+      if (kG && s.guided) nps = lut4(lg, __vabsdiffu4(nr[u].z, gt[u]), nps);
       score = __fadd_rn(score, __fmul_rn(nps, __uint_as_float(nr[u].w)));
     }
     if (score >= bound) return false;
@@ -926,6 +928,7 @@ __device__ __forceinline__ bool candidate_cost_padded(const SessionDev &s, const
 // (ms.rs:1151-1181, wrapped when tiling), the record in shared memory, and
 // the neighbour's coherence candidate (ms.rs:497-547): its source plus the
 // shift to the centre, kept if valid.  Returns true for a valid candidate.
+template <bool kG = true>
 __device__ __forceinline__ bool neighbour_setup(const SessionDev &s, const StageDev &st, const BatchDev &b,
                                                 uint32_t local, uint32_t nb, int px, int py, uint32_t j, int32_t off,
                                                 double avg, const double *tab, const float *tab_ff,
@@ -947,7 +950,7 @@ __device__ __forceinline__ bool neighbour_setup(const SessionDev &s, const Stage
   const bool inb = (unsigned)qx < s.W && (unsigned)qy < s.H;
   const uint32_t pat = inb ? s.color[(size_t)qy * s.W + qx] : kOutside;
   uint32_t gpat = 0;
-  if (s.guided) gpat = inb ? __ldg(&s.tguide[(size_t)st.level * s.W * s.H + (size_t)qy * s.W + qx]) : kOutside;
+  if (kG && s.guided) gpat = inb ? __ldg(&s.tguide[(size_t)st.level * s.W * s.H + (size_t)qy * s.W + qx]) : kOutside;
   w.nbr[j] = make_uint4((uint32_t)off, pat, gpat, __float_as_uint(wv));
   w.lin[j] = off_dy(off) * (int)s.ppitch + off_dx(off);
   const int wx = modi(nx, W), wy = modi(ny, H);
@@ -969,7 +972,7 @@ __device__ __forceinline__ bool neighbour_setup(const SessionDev &s, const Stage
 // lane j of a group of G lanes (a warp, or a CTA's warp) computes the terms
 // nps_j * w_j of neighbours j, j + G, ..., lane 0 sums them in order; every
 // lane returns the sum.
-template <int G>
+template <int G, bool kG = true>
 __device__ __forceinline__ float candidate0_score(const SessionDev &s, const StageDev &st, const WarpSmem &w,
                                                   const float *lc, const float *lg, uint32_t nk, int gl,
                                                   uint32_t gmask) {
@@ -988,7 +991,7 @@ __device__ __forceinline__ float candidate0_score(const SessionDev &s, const Sta
     }
     const int qx = cx + dx, qy = cy + dy;
     float nps = lut4(lc, __vabsdiffu4(nr.y, texel(lv, md, qx, qy)), 0.0f);
-    if (s.guided) {
+    if (kG && s.guided) {
       const GuideDesc gd = s.gdesc[map];
       const uint32_t *gv = s.guides + gd.off + (size_t)st.level * gd.w * gd.h;
       uint32_t gt = kOutside;
@@ -1007,6 +1010,7 @@ __device__ __forceinline__ float candidate0_score(const SessionDev &s, const Sta
 // The reference's sequential find_best_match (ms.rs:1184-1221), for stages or
 // items with non-finite costs, where early exit and argmin need its exact
 // comparison sequence.  One thread.
+template <bool kG = true>
 __device__ void sequential_best(const SessionDev &s, const StageDev &st, const WarpSmem &w, const float *lc,
                                 const float *lg, uint32_t nk, uint32_t nc, float &best_s, uint32_t &best_i) {
   best_s = FLT_MAX;
@@ -1029,7 +1033,7 @@ __device__ void sequential_best(const SessionDev &s, const StageDev &st, const W
       }
       const int qx = cx + dx, qy = cy + dy;
       float nps = lut4(lc, __vabsdiffu4(nr.y, texel(lv, md, qx, qy)), 0.0f);
-      if (s.guided) {
+      if (kG && s.guided) {
         const GuideDesc gd = s.gdesc[map];
         const uint32_t *gv = s.guides + gd.off + (size_t)st.level * gd.w * gd.h;
         uint32_t gt = kOutside;
@@ -1179,6 +1183,9 @@ __device__ void write_bad_result(const SessionDev &s, const StageDev &st, const 
   emit_result(s, st, b, local, r);
 }
 
+// kLean: sessions without guides only (the guide terms compiled out, which
+// lets the multi-session kernel run more blocks per SM).
+template <bool kLean>
 __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t vb,
                                              uint32_t vg) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1229,7 +1236,7 @@ __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev
         bool valid = false;
         uint32_t cxy = 0, aux = 0;
         if (j < nk)
-          valid = neighbour_setup(s, st, b, local, nb, px, py, j, nbo[j], avg, tab, tab_ff, w, cxy, aux, nan_w,
+          valid = neighbour_setup<!kLean>(s, st, b, local, nb, px, py, j, nbo[j], avg, tab, tab_ff, w, cxy, aux, nan_w,
                                   maxoff, bad_map);
         bool keep = valid;
         if (dedupe) {
@@ -1278,7 +1285,7 @@ __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev
       // lane 0; it wins ties with every later candidate, so the rest run
       // against min(S_0, f32::MAX) from the start
       {
-        const float s0 = candidate0_score<kWarp>(s, st, w, lc, lg, nk, lane, 0xffffffffu);
+        const float s0 = candidate0_score<kWarp, !kLean>(s, st, w, lc, lg, nk, lane, 0xffffffffu);
         if (s0 < best_s) best_s = s0;
       }
       for (uint32_t base = 1; base < nc; base += kWarp) {
@@ -1287,8 +1294,8 @@ __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev
         bool alive = false;
         if (c < nc) {
           if (!padded)
-            alive = candidate_cost(s, st, w, lc, lg, nk, w.cxy[c], w.caux[c], best_s, sc);
-          else if (s.guided)
+            alive = candidate_cost<!kLean>(s, st, w, lc, lg, nk, w.cxy[c], w.caux[c], best_s, sc);
+          else if (!kLean && s.guided)
             alive = candidate_cost_padded<true>(s, st, w, lc, lg, nk, w.cxy[c], w.caux[c], best_s, sc);
           else
             alive = candidate_cost_padded<false>(s, st, w, lc, lg, nk, w.cxy[c], w.caux[c], best_s, sc);
@@ -1310,7 +1317,7 @@ __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev
         }
       }
     } else if (lane == 0) {
-      sequential_best(s, st, w, lc, lg, nk, nc, best_s, best_i);
+      sequential_best<!kLean>(s, st, w, lc, lg, nk, nc, best_s, best_i);
     }
     if (lane == 0) write_result(s, st, w, b, local, pixel, px, py, is_new, ncoh_all + s.m, best_s, best_i);
   }
@@ -1824,7 +1831,7 @@ struct SegView {
 // The segment owning this block: segments are sorted by first block, so the
 // ones starting at or before blockIdx.x form a prefix; one ballot per 32.
 __device__ __forceinline__ SegView find_segment(const MultiLaunch &ml) {
-  const uint32_t bx = blockIdx.x;
+  const uint32_t bx = blockIdx.x + ml.block_base;
   const int lane = threadIdx.x & 31;
   uint32_t j = 0;
   for (uint32_t c = 0; c < ml.n_segs; c += kWarp) {
@@ -1921,12 +1928,18 @@ __global__ void __launch_bounds__(128) k_mean_multi(MultiLaunch ml) {
 
 __global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve(SessionDev s, StageDev st, BatchDev b) {
   pdl_enter();
-  resolve_body(s, st, b, blockIdx.x, gridDim.x);
+  resolve_body<false>(s, st, b, blockIdx.x, gridDim.x);
 }
 __global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve_multi(MultiLaunch ml) {
   pdl_enter();
   const SegView v = find_segment(ml);
-  resolve_body(*v.s, v.d->st, v.d->b, v.vb, v.vg);
+  resolve_body<false>(*v.s, v.d->st, v.d->b, v.vb, v.vg);
+}
+// Segments of sessions without guides: 56 registers, nine blocks per SM.
+__global__ void __launch_bounds__(kResolveWarps *kWarp, 9) k_resolve_multi_lean(MultiLaunch ml) {
+  pdl_enter();
+  const SegView v = find_segment(ml);
+  resolve_body<true>(*v.s, v.d->st, v.d->b, v.vb, v.vg);
 }
 
 template <int T, bool kFull>
@@ -2022,7 +2035,10 @@ cudaError_t configure_kernels(uint32_t k, uint32_t m) {
 cudaError_t set_multi_smem(int phase, size_t bytes) {
   switch (phase) {
     case kPhaseExhaustive: return raise_smem(k_knn_exhaustive_multi, bytes);
-    case kPhaseResolve: return raise_smem(k_resolve_multi, bytes);
+    case kPhaseResolve: {
+      const cudaError_t e = raise_smem(k_resolve_multi, bytes);
+      return e != cudaSuccess ? e : raise_smem(k_resolve_multi_lean, bytes);
+    }
     case kPhaseTeamPart: return raise_smem(k_resolve_team_multi<kTeamThreads, false>, bytes);
     case kPhaseTeamFull: return raise_smem(k_resolve_team_multi<kTeamFullThreads, true>, bytes);
     default: return cudaSuccess;
@@ -2086,7 +2102,18 @@ void launch_multi(int phase, const MultiLaunch &ml, uint32_t blocks, size_t smem
     case kPhaseWalk: launch_pdl(k_knn_walk_multi, blocks, t, 0, stream, ml); break;
     case kPhaseExhaustive: launch_pdl(k_knn_exhaustive_multi, blocks, t, smem, stream, ml); break;
     case kPhaseMean: launch_pdl(k_mean_multi, blocks, t, 0, stream, ml); break;
-    case kPhaseResolve: launch_pdl(k_resolve_multi, blocks, t, smem, stream, ml); break;
+    case kPhaseResolve: {
+      // segments [0, n_lean) belong to sessions without guides (lean kernel,
+      // blocks [0, lean_blocks)); the rest run the general kernel
+      MultiLaunch a = ml, g = ml;
+      a.n_segs = ml.n_lean;
+      g.segs = ml.segs + ml.n_lean;
+      g.n_segs = ml.n_segs - ml.n_lean;
+      g.block_base = ml.block_base + ml.lean_blocks;
+      if (a.n_segs) launch_pdl(k_resolve_multi_lean, ml.lean_blocks, t, smem, stream, a);
+      if (g.n_segs) launch_pdl(k_resolve_multi, blocks - ml.lean_blocks, t, smem, stream, g);
+      break;
+    }
     case kPhaseTeamPart: launch_pdl(k_resolve_team_multi<kTeamThreads, false>, blocks, t, smem, stream, ml); break;
     case kPhaseTeamFull: launch_pdl(k_resolve_team_multi<kTeamFullThreads, true>, blocks, t, smem, stream, ml); break;
     case kPhaseCommit: launch_pdl(k_commit_multi, blocks, t, 0, stream, ml); break;

@@ -157,6 +157,10 @@ struct MultiLaunch {
   const Segment *fb;
   uint32_t n_fb;
   uint32_t pool_block0;
+  uint32_t block_base = 0;  // block index of this launch's first block in the segment numbering
+  // resolve phase: the first n_lean segments (lean_blocks blocks) belong to
+  // sessions without guides
+  uint32_t n_lean = 0, lean_blocks = 0;
 };
 
 // Phases of a batch step, in launch order.

@@ -2091,6 +2091,7 @@ struct PlannedLaunch {
   uint32_t seg0, n_segs, blocks;
   size_t smem;
   uint32_t fb0 = 0, n_fb = 0, pool_block0 = 0;  // exhaustive k-NN: fallback lists drained by a block pool
+  uint32_t n_lean = 0, lean_blocks = 0;  // resolve: leading segments of sessions without guides
   int wait_rc = -1;  // first wait for the side stream's random candidates up to this launch of them
   int wait_items = -1;  // first wait for the side stream's item uploads up to this part
 };
@@ -2332,22 +2333,30 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
         pl.n_segs = pl.blocks = 0;
         pl.smem = 0;
         pl.fb0 = (uint32_t)h_fb.size();
-        for (size_t j : heavy) {
-          const RunCtx &c = *ctx[j];
-          if (t >= c.steps.size()) continue;
-          const Step &stp = c.steps[t];
-          if (ph == kPhaseExhaustive && stp.batch && c.k > 0 && !stp.exhaustive) {
-            h_fb.push_back(Segment{0, 0, (uint32_t)j, (uint32_t)t});
-            pl.n_fb += 1;
+        // resolve: sessions without guides first (the lean kernel), then the rest
+        for (int pass = 0; pass < (ph == kPhaseResolve ? 2 : 1); ++pass) {
+          for (size_t j : heavy) {
+            const RunCtx &c = *ctx[j];
+            if (t >= c.steps.size()) continue;
+            if (ph == kPhaseResolve && sessions[j]->guided != (pass == 1)) continue;
+            const Step &stp = c.steps[t];
+            if (ph == kPhaseExhaustive && stp.batch && c.k > 0 && !stp.exhaustive) {
+              h_fb.push_back(Segment{0, 0, (uint32_t)j, (uint32_t)t});
+              pl.n_fb += 1;
+              pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
+            }
+            const uint32_t units = phase_units(stp, c, ph);
+            const uint32_t nb = multi_blocks(ph, units, phase_cap(stp, ph));
+            if (nb == 0) continue;
+            h_segs.push_back(Segment{pl.blocks, nb, (uint32_t)j, (uint32_t)t});
+            pl.blocks += nb;
+            pl.n_segs += 1;
             pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
           }
-          const uint32_t units = phase_units(stp, c, ph);
-          const uint32_t nb = multi_blocks(ph, units, phase_cap(stp, ph));
-          if (nb == 0) continue;
-          h_segs.push_back(Segment{pl.blocks, nb, (uint32_t)j, (uint32_t)t});
-          pl.blocks += nb;
-          pl.n_segs += 1;
-          pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
+          if (ph == kPhaseResolve && pass == 0) {
+            pl.n_lean = pl.n_segs;
+            pl.lean_blocks = pl.blocks;
+          }
         }
         pl.pool_block0 = pl.blocks;
         if (pl.n_fb) pl.blocks += kFallbackPool;
@@ -2481,6 +2490,8 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
         ml.fb = d_fb.p + pl.fb0;
         ml.n_fb = pl.n_fb;
         ml.pool_block0 = pl.n_fb ? pl.pool_block0 : pl.blocks;
+        ml.n_lean = pl.n_lean;
+        ml.lean_blocks = pl.lean_blocks;
         if (!pev.empty()) CUDA_TRY(cudaEventRecord(pev[li].a, s));
         launch_multi(pl.phase, ml, pl.blocks, pl.smem, s);
         if (!pev.empty()) CUDA_TRY(cudaEventRecord(pev[li].b, s));
@@ -2528,6 +2539,8 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
     bs.sessions = n;
     bs.steps = max_steps;
     bs.launches = launches.size() + rc_launches.size();
+    for (const PlannedLaunch &pl : launches)
+      if (pl.phase == kPhaseResolve && pl.n_lean && pl.n_lean < pl.n_segs) bs.launches += 1;  // two kernels
     bs.phase_launches[kPhaseRandom] += rc_launches.size();
     bs.plan_ms = plan_ms;
     {
@@ -2829,20 +2842,28 @@ void server_driver(ts_server *S) {
           pl.n_segs = pl.blocks = 0;
           pl.smem = 0;
           pl.fb0 = (uint32_t)fb.size();
-          for (ServerReq *r : ready) {
-            const RunCtx &c = *r->c;
-            const Step &stp = c.steps[r->cursor];
-            if (ph == kPhaseExhaustive && stp.batch && c.k > 0 && !stp.exhaustive) {
-              fb.push_back(Segment{0, 0, r->slot, (uint32_t)r->cursor});
-              pl.n_fb += 1;
+          // resolve: sessions without guides first (the lean kernel), then the rest
+          for (int pass = 0; pass < (ph == kPhaseResolve ? 2 : 1); ++pass) {
+            for (ServerReq *r : ready) {
+              const RunCtx &c = *r->c;
+              if (ph == kPhaseResolve && r->s->guided != (pass == 1)) continue;
+              const Step &stp = c.steps[r->cursor];
+              if (ph == kPhaseExhaustive && stp.batch && c.k > 0 && !stp.exhaustive) {
+                fb.push_back(Segment{0, 0, r->slot, (uint32_t)r->cursor});
+                pl.n_fb += 1;
+                pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
+              }
+              const uint32_t nb = multi_blocks(ph, phase_units(stp, c, ph), phase_cap(stp, ph));
+              if (nb == 0) continue;
+              segs.push_back(Segment{pl.blocks, nb, r->slot, (uint32_t)r->cursor});
+              pl.blocks += nb;
+              pl.n_segs += 1;
               pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
             }
-            const uint32_t nb = multi_blocks(ph, phase_units(stp, c, ph), phase_cap(stp, ph));
-            if (nb == 0) continue;
-            segs.push_back(Segment{pl.blocks, nb, r->slot, (uint32_t)r->cursor});
-            pl.blocks += nb;
-            pl.n_segs += 1;
-            pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
+            if (ph == kPhaseResolve && pass == 0) {
+              pl.n_lean = pl.n_segs;
+              pl.lean_blocks = pl.blocks;
+            }
           }
           pl.pool_block0 = pl.blocks;
           if (pl.n_fb) pl.blocks += kFallbackPool;
@@ -2869,9 +2890,13 @@ void server_driver(ts_server *S) {
           ml.fb = R.h + segs.size() + pl.fb0;
           ml.n_fb = pl.n_fb;
           ml.pool_block0 = pl.n_fb ? pl.pool_block0 : pl.blocks;
+          ml.n_lean = pl.n_lean;
+          ml.lean_blocks = pl.lean_blocks;
           launch_multi(pl.phase, ml, pl.blocks, pl.smem, S->st);
         }
         tick_launches = launches.size();
+        for (const PlannedLaunch &pl : launches)
+          if (pl.phase == kPhaseResolve && pl.n_lean && pl.n_lean < pl.n_segs) tick_launches += 1;
       }
       CUDA_TRY(cudaGetLastError());
       CUDA_TRY(cudaEventRecord(R.ev, S->st));
