@@ -33,6 +33,8 @@
 #include <float.h>
 #include <stdint.h>
 
+#include <cuda_pipeline.h>
+
 #include <algorithm>
 #include <map>
 #include <mutex>
@@ -1918,6 +1920,38 @@ __global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive_multi(MultiLaunc
   }
 }
 
+// The single-session mean: each thread first copies its item's distances
+// into its own column of shared memory with asynchronous copies (all in
+// flight at once), so that only the f64 chain itself stays on the
+// critical path of these mostly latency-bound launches.
+constexpr uint32_t kMeanThreads = 64;
+__device__ __forceinline__ void mean_body_staged(const BatchDev &b, uint32_t vb) {
+  extern __shared__ double md[];  // [k][kMeanThreads]
+  const uint32_t nb = b.i1 - b.i0;
+  const uint32_t local = vb * kMeanThreads + threadIdx.x;
+  if (local >= nb) return;
+  const uint32_t nk = b.ncnt[local];
+  if (nk == 0) return;
+  double *col = md + threadIdx.x;
+  for (uint32_t j = 0; j < nk; ++j) __pipeline_memcpy_async(col + j * kMeanThreads, b.dist + (size_t)j * nb + local, 8);
+  __pipeline_commit();
+  __pipeline_wait_prior(0);
+  double sum = 0.0;
+  for (uint32_t j = 0; j < nk; ++j) {
+    const double d = col[j * kMeanThreads];
+    sum = __dadd_rn(sum, d);
+    sum = __dadd_rn(sum, d);
+    sum = __dadd_rn(sum, d);
+    sum = __dadd_rn(sum, d);
+  }
+  b.mean[local] = __ddiv_rn(sum, (double)(nk * 4u));
+}
+
+__global__ void __launch_bounds__(kMeanThreads) k_mean_staged(SessionDev s, StageDev st, BatchDev b) {
+  pdl_enter();
+  mean_body_staged(b, blockIdx.x);
+}
+
 __global__ void __launch_bounds__(128) k_mean(SessionDev s, StageDev st, BatchDev b) {
   pdl_enter(); mean_body(s, b, blockIdx.x); }
 __global__ void __launch_bounds__(128) k_mean_multi(MultiLaunch ml) {
@@ -2024,6 +2058,8 @@ cudaError_t configure_kernels(uint32_t k, uint32_t m) {
   cudaError_t e = raise_smem(k_resolve, resolve_smem_bytes(k, m, 0));
   if (e != cudaSuccess) return e;
   e = raise_smem(k_knn_exhaustive, kExhAllKeys * 8);
+  if (e != cudaSuccess) return e;
+  e = raise_smem(k_mean_staged, (size_t)k * kMeanThreads * 8);
   if (e != cudaSuccess) return e;
   e = raise_smem(k_resolve_team<kTeamThreads, false>, team_smem_bytes(k, m));
   if (e != cudaSuccess) return e;
@@ -2146,7 +2182,7 @@ void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchD
 void launch_mean(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
   const uint32_t n = b.i1 - b.i0;
   if (n == 0 || s.k == 0) return;
-  launch_pdl(k_mean, cdiv(n, 128), 128, 0, stream, s, st, b);
+  launch_pdl(k_mean_staged, cdiv(n, kMeanThreads), kMeanThreads, (size_t)s.k * kMeanThreads * 8, stream, s, st, b);
 }
 
 void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
