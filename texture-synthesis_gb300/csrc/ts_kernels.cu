@@ -1797,6 +1797,67 @@ __global__ void k_resize_h(const float *tmp, uint32_t w, uint32_t nh, uint8_t *d
   *(uchar4 *)(dst + ((size_t)y * nw + ox) * 4) = o;
 }
 
+// The job owning block b of a pass: jobs sorted by first block, one ballot
+// per 32 (block0 selects the pass's column).
+template <bool kV>
+__device__ __forceinline__ uint32_t find_job(const ResizeJob *jobs, uint32_t n, uint32_t b) {
+  const int lane = threadIdx.x & 31;
+  uint32_t j = 0;
+  for (uint32_t c = 0; c < n; c += 32) {
+    const uint32_t i = c + lane;
+    const bool le = i < n && (kV ? jobs[i].block0_v : jobs[i].block0_h) <= b;
+    const uint32_t bal = __ballot_sync(0xffffffffu, le);
+    j = c + __popc(bal) - 1;
+    if (bal != 0xffffffffu) break;
+  }
+  return j;
+}
+
+// k_resize_v over many jobs: job blocks laid out as cdiv(w, 128) x nh.
+__global__ void k_resize_v_jobs(const ResizeJob *jobs, uint32_t n) {
+  const uint32_t j = find_job<true>(jobs, n, blockIdx.x);
+  const ResizeJob jb = jobs[j];
+  const uint32_t lb = blockIdx.x - jb.block0_v, bx = (jb.w + 127) / 128;
+  const uint32_t x = (lb % bx) * 128 + threadIdx.x, oy = lb / bx;
+  if (x >= jb.w || oy >= jb.nh) return;
+  const uint4 t = jb.tv[oy];
+  float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+  for (uint32_t i = 0; i < t.y; ++i) {
+    const uchar4 p = *(const uchar4 *)(jb.src + ((size_t)(t.x + i) * jb.w + x) * 4);
+    const float wt = jb.wv[t.z + i];
+    a0 = __fadd_rn(a0, __fmul_rn((float)p.x, wt));
+    a1 = __fadd_rn(a1, __fmul_rn((float)p.y, wt));
+    a2 = __fadd_rn(a2, __fmul_rn((float)p.z, wt));
+    a3 = __fadd_rn(a3, __fmul_rn((float)p.w, wt));
+  }
+  *(float4 *)(jb.tmp + ((size_t)oy * jb.w + x) * 4) = make_float4(a0, a1, a2, a3);
+}
+
+// k_resize_h over many jobs: job blocks laid out as cdiv(nw, 128) x nh.
+__global__ void k_resize_h_jobs(const ResizeJob *jobs, uint32_t n) {
+  const uint32_t j = find_job<false>(jobs, n, blockIdx.x);
+  const ResizeJob jb = jobs[j];
+  const uint32_t lb = blockIdx.x - jb.block0_h, bx = (jb.nw + 127) / 128;
+  const uint32_t ox = (lb % bx) * 128 + threadIdx.x, y = lb / bx;
+  if (ox >= jb.nw || y >= jb.nh) return;
+  const uint4 t = jb.th[ox];
+  float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+  for (uint32_t i = 0; i < t.y; ++i) {
+    const float4 p = *(const float4 *)(jb.tmp + ((size_t)y * jb.w + t.x + i) * 4);
+    const float wt = jb.wh[t.z + i];
+    a0 = __fadd_rn(a0, __fmul_rn(p.x, wt));
+    a1 = __fadd_rn(a1, __fmul_rn(p.y, wt));
+    a2 = __fadd_rn(a2, __fmul_rn(p.z, wt));
+    a3 = __fadd_rn(a3, __fmul_rn(p.w, wt));
+  }
+  uchar4 o;
+  o.x = to_u8(a0);
+  o.y = to_u8(a1);
+  o.z = to_u8(a2);
+  o.w = to_u8(a3);
+  *(uchar4 *)(jb.dst + ((size_t)y * jb.nw + ox) * 4) = o;
+}
+
 // Padded copy: dst[l][y + kPad][x + kPad] = src[l][y][x], border = kOutside.
 __global__ void k_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, uint32_t pw, uint32_t *dst) {
   const uint32_t ph = h + 2 * kPad;
@@ -2264,6 +2325,16 @@ void launch_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uin
   if (w == 0 || nh == 0) return;
   dim3 grid(cdiv(w, 128), nh);
   k_resize_v<<<grid, 128, 0, stream>>>(src, w, h, tmp, nh, taps, wts);
+}
+
+void launch_resize_v_jobs(const ResizeJob *jobs, uint32_t n, uint32_t blocks, cudaStream_t stream) {
+  if (n == 0 || blocks == 0) return;
+  k_resize_v_jobs<<<blocks, 128, 0, stream>>>(jobs, n);
+}
+
+void launch_resize_h_jobs(const ResizeJob *jobs, uint32_t n, uint32_t blocks, cudaStream_t stream) {
+  if (n == 0 || blocks == 0) return;
+  k_resize_h_jobs<<<blocks, 128, 0, stream>>>(jobs, n);
 }
 
 void launch_resize_h(const float *tmp, uint32_t w, uint32_t nh, uint8_t *dst, uint32_t nw, const uint4 *taps,

@@ -235,6 +235,23 @@ void launch_resize_v(const uint8_t *src, uint32_t w, uint32_t h, float *tmp, uin
 void launch_resize_h(const float *tmp, uint32_t w, uint32_t nh, uint8_t *dst, uint32_t nw, const uint4 *taps,
                      const float *wts, cudaStream_t stream);
 
+// Many resizes in one launch per pass: job j resizes src (w x h) to dst
+// (nw x nh) through tmp (w x nh floats), the taps as above; block0 is the
+// job's first block of the pass (jobs sorted by it, the last entry the total).
+struct ResizeJob {
+  const uint8_t *src;
+  uint8_t *dst;
+  float *tmp;
+  const uint4 *tv, *th;
+  const float *wv, *wh;
+  uint32_t w, h, nw, nh;
+  uint32_t block0_v, block0_h;
+};
+// Vertical passes of jobs [0, n) (blocks: jobs[n].block0_v in total) and
+// horizontal passes (jobs[n].block0_h); jobs in device memory.
+void launch_resize_v_jobs(const ResizeJob *jobs, uint32_t n, uint32_t blocks, cudaStream_t stream);
+void launch_resize_h_jobs(const ResizeJob *jobs, uint32_t n, uint32_t blocks, cudaStream_t stream);
+
 // Padded copy of `levels` images of w x h texels (see kPad) with row pitch
 // `pitch` >= w + 2 kPad.
 void launch_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, uint32_t pitch, uint32_t *dst,

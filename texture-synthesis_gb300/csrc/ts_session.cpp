@@ -450,28 +450,112 @@ Image load_image(const Image &in, bool has_size, uint32_t w, uint32_t h, cudaStr
   return out;
 }
 
-// ImagePyramid::new(img, Some(levels)) (img_pyramid.rs:7-37) written into
-// dst (device, max(levels,1) images of w*h texels).
-void device_pyramid(const Image &img, uint32_t levels, uint32_t *dst, cudaStream_t st) {
-  const uint32_t nl = levels == 0 ? 1 : levels;
-  const size_t sz = (size_t)img.w * img.h;
-  uint8_t *base = (uint8_t *)dst;
-  CUDA_TRY(cudaMemcpyAsync(base + (size_t)(nl - 1) * sz * 4, img.px.data(), sz * 4, cudaMemcpyHostToDevice, st));
-  const uint8_t *orig = base + (size_t)(nl - 1) * sz * 4;
-  for (uint32_t l = 0; l + 1 < nl; ++l) {
-    const uint32_t i = nl - 1 - l;
-    const uint32_t p = 1u << i;
-    const uint32_t sw = img.w / p, sh = img.h / p;
-    DevBuf<uint8_t> small;
-    CUDA_TRY(small.alloc_on((size_t)sw * sh * 4, st));
-    if (sw == 0 || sh == 0) {
-      // a zero-sized intermediate makes the crate return a zero image
-      CUDA_TRY(cudaMemsetAsync(base + (size_t)l * sz * 4, 0, sz * 4, st));
-      continue;
+
+inline uint32_t cdiv_u32(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
+
+// ImagePyramid::new (img_pyramid.rs:7-37) for many images at once: every
+// level of every image is a Gaussian resize of the original down by 2^i and
+// back up, so all images' levels go through four launches (down vertical,
+// down horizontal, up vertical, up horizontal) instead of four per level.
+// The originals are copied from pageable host memory (staged before the
+// call returns); the scratch is stream-ordered pool memory.
+struct PyramidJob {
+  const Image *img;
+  uint32_t levels;
+  uint32_t *dst;  // max(levels, 1) images of w*h texels
+};
+
+void device_pyramids(const std::vector<PyramidJob> &pj, cudaStream_t st) {
+  std::vector<ResizeJob> down, up;
+  size_t small_bytes = 0, tmp_floats = 0;
+  struct Lvl {
+    size_t job;
+    uint32_t l, sw, sh;
+    size_t small_off, tmp_down, tmp_up;
+  };
+  std::vector<Lvl> lv;
+  for (size_t q = 0; q < pj.size(); ++q) {
+    const Image &img = *pj[q].img;
+    const uint32_t nl = pj[q].levels == 0 ? 1 : pj[q].levels;
+    const size_t sz = (size_t)img.w * img.h;
+    uint8_t *base = (uint8_t *)pj[q].dst;
+    CUDA_TRY(cudaMemcpyAsync(base + (size_t)(nl - 1) * sz * 4, img.px.data(), sz * 4, cudaMemcpyHostToDevice, st));
+    for (uint32_t l = 0; l + 1 < nl; ++l) {
+      const uint32_t i = nl - 1 - l;
+      const uint32_t sw = img.w >> std::min(i, 31u), sh = img.h >> std::min(i, 31u);
+      if (sw == 0 || sh == 0) {
+        // a zero-sized intermediate makes the crate return a zero image
+        CUDA_TRY(cudaMemsetAsync(base + (size_t)l * sz * 4, 0, sz * 4, st));
+        continue;
+      }
+      Lvl v{q, l, sw, sh, small_bytes, tmp_floats, 0};
+      small_bytes += ((size_t)sw * sh * 4 + 255) & ~(size_t)255;
+      tmp_floats += (size_t)img.w * sh * 4;
+      v.tmp_up = tmp_floats;
+      tmp_floats += (size_t)sw * img.h * 4;
+      lv.push_back(v);
     }
-    device_resize(orig, img.w, img.h, small.p, sw, sh, kGaussian, st);
-    device_resize(small.p, sw, sh, base + (size_t)l * sz * 4, img.w, img.h, kGaussian, st);
   }
+  if (lv.empty()) return;
+  DevBuf<uint8_t> d_small;
+  DevBuf<float> d_tmp;
+  DevBuf<ResizeJob> d_jobs;
+  CUDA_TRY(d_small.alloc_on(small_bytes, st));
+  CUDA_TRY(d_tmp.alloc_on(tmp_floats, st));
+  uint32_t bdv = 0, bdh = 0, buv = 0, buh = 0;
+  for (const Lvl &v : lv) {
+    const Image &img = *pj[v.job].img;
+    const uint32_t nl = pj[v.job].levels == 0 ? 1 : pj[v.job].levels;
+    const size_t sz = (size_t)img.w * img.h;
+    uint8_t *base = (uint8_t *)pj[v.job].dst;
+    uint8_t *small = d_small.p + v.small_off;
+    ResizeJob d{};
+    d.src = base + (size_t)(nl - 1) * sz * 4;
+    d.dst = small;
+    d.tmp = d_tmp.p + v.tmp_down;
+    d.w = img.w;
+    d.h = img.h;
+    d.nw = v.sw;
+    d.nh = v.sh;
+    const DevTapsRef dv = cached_taps(kGaussian, 0.0f, img.h, v.sh), dh = cached_taps(kGaussian, 0.0f, img.w, v.sw);
+    d.tv = dv.taps;
+    d.wv = dv.wts;
+    d.th = dh.taps;
+    d.wh = dh.wts;
+    d.block0_v = bdv;
+    d.block0_h = bdh;
+    bdv += cdiv_u32(img.w, 128) * v.sh;
+    bdh += cdiv_u32(v.sw, 128) * v.sh;
+    down.push_back(d);
+    ResizeJob u{};
+    u.src = small;
+    u.dst = base + (size_t)v.l * sz * 4;
+    u.tmp = d_tmp.p + v.tmp_up;
+    u.w = v.sw;
+    u.h = v.sh;
+    u.nw = img.w;
+    u.nh = img.h;
+    const DevTapsRef uv = cached_taps(kGaussian, 0.0f, v.sh, img.h), uh = cached_taps(kGaussian, 0.0f, v.sw, img.w);
+    u.tv = uv.taps;
+    u.wv = uv.wts;
+    u.th = uh.taps;
+    u.wh = uh.wts;
+    u.block0_v = buv;
+    u.block0_h = buh;
+    buv += cdiv_u32(v.sw, 128) * img.h;
+    buh += cdiv_u32(img.w, 128) * img.h;
+    up.push_back(u);
+  }
+  const size_t nj = lv.size();
+  std::vector<ResizeJob> all(down);
+  all.insert(all.end(), up.begin(), up.end());
+  CUDA_TRY(d_jobs.alloc_on(all.size(), st));
+  CUDA_TRY(cudaMemcpyAsync(d_jobs.p, all.data(), all.size() * sizeof(ResizeJob), cudaMemcpyHostToDevice, st));
+  launch_resize_v_jobs(d_jobs.p, (uint32_t)nj, bdv, st);
+  launch_resize_h_jobs(d_jobs.p, (uint32_t)nj, bdh, st);
+  launch_resize_v_jobs(d_jobs.p + nj, (uint32_t)nj, buv, st);
+  launch_resize_h_jobs(d_jobs.p + nj, (uint32_t)nj, buh, st);
+  CUDA_TRY(cudaGetLastError());
 }
 
 inline uint32_t pcg_stage_seed(uint64_t seed) {
@@ -587,7 +671,7 @@ int ts_image_pyramid(const uint8_t *rgba, uint32_t w, uint32_t h, uint32_t level
     Image img = copy_image(rgba, w, h);
     DevBuf<uint32_t> d;
     CUDA_TRY(d.alloc((size_t)w * h * nl));
-    device_pyramid(img, levels, d.p, 0);
+    device_pyramids({PyramidJob{&img, levels, d.p}}, 0);
     CUDA_TRY(cudaMemcpy(out, d.p, (size_t)w * h * nl * 4, cudaMemcpyDeviceToHost));
   } catch (const Failure &f) {
     return f.status;
@@ -982,9 +1066,10 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
     }
     CUDA_TRY(s->levels.alloc(texels));
     CUDA_TRY(s->masks.alloc(mask_bytes));
+    std::vector<PyramidJob> pyr;  // every pyramid of the session, built together below
     for (uint32_t f = 0; f < s->n_maps; ++f) {
       const uint32_t e = s->filtered[f];
-      device_pyramid(imgs[e], p.backtrack_stages, s->levels.p + s->maps[f].off, st);
+      pyr.push_back(PyramidJob{&imgs[e], p.backtrack_stages, s->levels.p + s->maps[f].off});
       if (s->maps[f].mask_off >= 0) {
         std::vector<uint8_t> mb((size_t)s->maps[f].w * s->maps[f].h);
         for (size_t i = 0; i < mb.size(); ++i) mb[i] = masks[e].px[4 * i] != 0 ? 1 : 0;
@@ -992,10 +1077,6 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
       }
     }
     CUDA_TRY(s->plevels.alloc(ptexels));
-    for (uint32_t f = 0; f < s->n_maps; ++f)
-      launch_pad(s->levels.p + s->maps[f].off, s->maps[f].w, s->maps[f].h, s->n_levels, pitch,
-                 s->plevels.p + s->maps[f].poff, st);
-    CUDA_TRY(cudaGetLastError());
     CUDA_TRY(s->d_maps.alloc(s->n_maps));
     CUDA_TRY(cudaMemcpy(s->d_maps.p, s->maps.data(), s->n_maps * sizeof(MapDesc), cudaMemcpyHostToDevice));
     // guides: every example (unfiltered order) plus the target guide
@@ -1014,19 +1095,21 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
         if (f >= s->n_ex || gd[f].w != s->maps[f].w || gd[f].h != s->maps[f].h) s->guide_dims_differ = true;
       CUDA_TRY(s->guides.alloc(gtex));
       for (uint32_t e = 0; e < s->n_ex; ++e)
-        device_pyramid(guides[e], p.backtrack_stages, s->guides.p + gd[e].off, st);
-      // padded guides per map, at the map's own padded offsets (same size:
-      // only then are they read)
-      if (!s->guide_dims_differ) {
-        CUDA_TRY(s->pguides.alloc(ptexels));
-        for (uint32_t f = 0; f < s->n_maps; ++f)
-          launch_pad(s->guides.p + gd[f].off, gd[f].w, gd[f].h, s->n_levels, pitch, s->pguides.p + s->maps[f].poff,
-                     st);
-      }
-      CUDA_TRY(cudaGetLastError());
+        pyr.push_back(PyramidJob{&guides[e], p.backtrack_stages, s->guides.p + gd[e].off});
+      if (!s->guide_dims_differ) CUDA_TRY(s->pguides.alloc(ptexels));
       CUDA_TRY(s->tguide.alloc((size_t)W * H * s->n_levels));
-      device_pyramid(tg, p.backtrack_stages, s->tguide.p, st);
+      pyr.push_back(PyramidJob{&tg, p.backtrack_stages, s->tguide.p});
     }
+    device_pyramids(pyr, st);
+    for (uint32_t f = 0; f < s->n_maps; ++f)
+      launch_pad(s->levels.p + s->maps[f].off, s->maps[f].w, s->maps[f].h, s->n_levels, pitch,
+                 s->plevels.p + s->maps[f].poff, st);
+    // padded guides per map, at the map's own padded offsets (same size:
+    // only then are they read)
+    if (s->guided && !s->guide_dims_differ)
+      for (uint32_t f = 0; f < s->n_maps; ++f)
+        launch_pad(s->guides.p + gd[f].off, gd[f].w, gd[f].h, s->n_levels, pitch, s->pguides.p + s->maps[f].poff, st);
+    CUDA_TRY(cudaGetLastError());
     CUDA_TRY(s->d_gdesc.alloc(gd.size()));
     CUDA_TRY(cudaMemcpy(s->d_gdesc.p, gd.data(), gd.size() * sizeof(GuideDesc), cudaMemcpyHostToDevice));
     // the pyramids are still being built: run() waits for this event on the
