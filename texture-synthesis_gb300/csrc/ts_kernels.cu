@@ -360,20 +360,20 @@ __device__ __forceinline__ void for_points(const SessionDev &s, uint32_t n_res, 
 }
 
 __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
-                                    ExhShared &sh, unsigned long long *all, bool with_mean);
+                                    ExhShared &sh, unsigned long long *all, uint32_t cap, bool with_mean);
 
 // One CTA per item.  `all` (dynamic shared memory, kExhAllKeys entries)
 // receives every point's key in one pass over the resolved list; when they
 // fit, a bitonic sort of them gives the answer directly, otherwise a
 // radix select over further passes finds the cut distance first.
 __device__ __forceinline__ void knn_exhaustive_body(const SessionDev &s, const StageDev &st, const BatchDev &b,
-                                                    int all_items, uint32_t vb, uint32_t vg) {
+                                                    int all_items, uint32_t cap, uint32_t vb, uint32_t vg) {
   __shared__ ExhShared sh;
   extern __shared__ unsigned long long all_keys[];
   const uint32_t n = all_items ? b.i1 - b.i0 : *b.fb_count;
   for (uint32_t e = vb; e < n; e += vg) {
     const uint32_t local = all_items ? e : b.fb_list[e];
-    knn_exhaustive_item(s, st, b, local, sh, all_keys, all_items != 0);
+    knn_exhaustive_item(s, st, b, local, sh, all_keys, cap, all_items != 0);
     __syncthreads();
   }
 }
@@ -411,7 +411,7 @@ __device__ __forceinline__ void block_bitonic(unsigned long long *keys, uint32_t
 __device__ __forceinline__ uint32_t ring_base(uint32_t r) { return r == 0 ? 0u : 4u * r * (r - 1u) + 1u; }
 
 __device__ void grid_collect(const SessionDev &s, int px, int py, uint32_t k, ExhShared &sh,
-                             unsigned long long *all) {
+                             unsigned long long *all, uint32_t cap) {
   if (threadIdx.x == 0) {
     sh.total = 0;
     sh.prefix = 0;
@@ -461,7 +461,7 @@ __device__ void grid_collect(const SessionDev &s, int px, int py, uint32_t k, Ex
             const uint32_t d2 = (uint32_t)(dx * dx + dy * dy);
             dor |= d2;
             const uint32_t slot = atomicAdd(&sh.total, 1u);
-            if (slot < (uint32_t)kExhAllKeys) all[slot] = nb_key(d2, x, y);
+            if (slot < cap) all[slot] = nb_key(d2, x, y);
             ++found;
           }
         }
@@ -470,7 +470,7 @@ __device__ void grid_collect(const SessionDev &s, int px, int py, uint32_t k, Ex
     if (dor) atomicOr(&sh.prefix, dor);
     __syncthreads();
     const uint32_t n = sh.total;
-    if (n > (uint32_t)kExhAllKeys) break;
+    if (n > cap) break;
     // the last ring this round completed
     const uint32_t f_done = min(f0 + blockDim.x, f_end_all);
     uint32_t r_done = 0;
@@ -492,7 +492,7 @@ __device__ void grid_collect(const SessionDev &s, int px, int py, uint32_t k, Ex
 }
 
 __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
-                                    ExhShared &sh, unsigned long long *all, bool with_mean) {
+                                    ExhShared &sh, unsigned long long *all, uint32_t cap, bool with_mean) {
   const uint32_t pixel = st.items[b.i0 + local];
   const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
   const uint32_t k = s.k;
@@ -514,7 +514,7 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
   // instead, which hold the k nearest.
   const int lane = threadIdx.x & 31;
   const bool grid = s.cells != nullptr && n_res > kExhGridFrom;
-  if (grid) grid_collect(s, px, py, k, sh, all);
+  if (grid) grid_collect(s, px, py, k, sh, all, cap);
   for (uint32_t e0 = 0; e0 < (grid ? 0u : n_res); e0 += blockDim.x) {
     const uint32_t e = e0 + threadIdx.x;
     int xs[3], ys[3];
@@ -555,7 +555,7 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
     for (uint32_t i = 0; i < cnt; ++i) {
       const uint32_t d2 = d2of(xs[i], ys[i]);
       dor |= d2;
-      if (base + i < (uint32_t)kExhAllKeys) all[base + i] = nb_key(d2, xs[i], ys[i]);
+      if (base + i < cap) all[base + i] = nb_key(d2, xs[i], ys[i]);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) dor |= __shfl_xor_sync(0xffffffffu, dor, o);
@@ -563,14 +563,14 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
   }
   __syncthreads();
   uint32_t total = sh.total;
-  if (!grid && total > (uint32_t)kExhAllKeys && s.cells != nullptr) {
+  if (!grid && total > cap && s.cells != nullptr) {
     __syncthreads();
-    grid_collect(s, px, py, k, sh, all);
+    grid_collect(s, px, py, k, sh, all, cap);
     total = sh.total;
   }
   const unsigned long long *sorted;
   uint32_t n;
-  if (total <= k || total <= (uint32_t)kExhAllKeys) {
+  if (total <= k || total <= cap) {
     // radix select of the k-th smallest d2 over the shared keys, digits of
     // 8 bits from the highest significant bit down
     const uint32_t dor_all = sh.prefix;
@@ -1932,11 +1932,11 @@ __global__ void __launch_bounds__(kWalkWarps *kWarp, 4) k_knn_walk_multi(MultiLa
   knn_walk_body<false>(*v.s, v.d->st, v.d->b, v.vb, v.vg);
 }
 
-__global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive(SessionDev s, StageDev st, BatchDev b,
+__global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive(SessionDev s, StageDev st, BatchDev b, uint32_t cap,
                                                                  int all_items) {
   pdl_enter();
   pdl_enter();
-  knn_exhaustive_body(s, st, b, all_items, blockIdx.x, gridDim.x);
+  knn_exhaustive_body(s, st, b, all_items, cap, blockIdx.x, gridDim.x);
 }
 __global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive_multi(MultiLaunch ml) {
   pdl_enter();
@@ -1947,7 +1947,7 @@ __global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive_multi(MultiLaunc
     const StepDev &d = *v.d;
     const uint32_t n = d.b.i1 - d.b.i0;
     for (uint32_t e = v.vb; e < n; e += v.vg) {
-      knn_exhaustive_item(*v.s, d.st, d.b, e, sh, all_keys, true);
+      knn_exhaustive_item(*v.s, d.st, d.b, e, sh, all_keys, ml.key_cap, true);
       __syncthreads();
     }
     return;
@@ -1972,7 +1972,8 @@ __global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive_multi(MultiLaunc
         const Segment g = ml.fb[c0 + j];
         const StepDev &d = ml.step_tabs[g.session][g.step];
         for (; v < base + cnt; v += vg) {
-          knn_exhaustive_item(ml.sessions[g.session], d.st, d.b, d.b.fb_list[v - base], sh, all_keys, false);
+          knn_exhaustive_item(ml.sessions[g.session], d.st, d.b, d.b.fb_list[v - base], sh, all_keys, ml.key_cap,
+                              false);
           __syncthreads();
         }
       }
@@ -2101,14 +2102,23 @@ constexpr size_t kTeamFullMaxSmem = 96 * 1024;
 // any order and run later.
 template <typename K>
 static cudaError_t raise_smem(K *kernel, size_t bytes) {
-  if (bytes <= 48 * 1024) return cudaSuccess;
   static std::mutex mu;
   static std::map<std::pair<int, const void *>, size_t> cur;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> lk(mu);
-  size_t &c = cur[{dev, (const void *)kernel}];
+  auto it = cur.find({dev, (const void *)kernel});
+  if (it == cur.end()) {
+    // without the opt-in, static plus dynamic shared memory stays within 48 KB
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    it = cur.emplace(std::make_pair(dev, (const void *)kernel),
+                     fa.sharedSizeBytes < 48 * 1024 ? 48 * 1024 - fa.sharedSizeBytes : 0)
+             .first;
+  }
+  size_t &c = it->second;
   if (bytes <= c) return cudaSuccess;
   e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e == cudaSuccess) c = bytes;
@@ -2232,12 +2242,21 @@ void launch_knn_walk(const SessionDev &s, const StageDev &st, const BatchDev &b,
     launch_pdl(k_knn_walk<false>, cdiv(n, kWalkWarps), kWalkWarps * kWarp, 0, stream, s, st, b);
 }
 
+uint32_t exh_key_cap(const SessionDev &s, const BatchDev &b) {
+  // every point and its (at most two) tiling mirrors while they fit, else
+  // the cell grid's rings (a few times k keys; an overflow falls back to
+  // rescanning the points, exactly)
+  const uint64_t want = b.n_res <= kExhGridFrom ? (uint64_t)b.n_res * (s.tiling ? 3 : 1) + 64 : 2048;
+  return (uint32_t)std::min<uint64_t>(kExhAllKeys, std::max<uint64_t>(want, 4u * std::max<uint32_t>(s.k, 64u)));
+}
+
 void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchDev &b, bool all_items,
                            cudaStream_t stream) {
   const uint32_t n = b.i1 - b.i0;
   if (n == 0) return;
   const uint32_t grid = n < 608u ? n : 608u;  // 152 SMs x 4 CTAs, grid-stride beyond
-  launch_pdl(k_knn_exhaustive, grid, kExhThreads, (size_t)kExhAllKeys * 8, stream, s, st, b, all_items ? 1 : 0);
+  const uint32_t cap = exh_key_cap(s, b);
+  launch_pdl(k_knn_exhaustive, grid, kExhThreads, (size_t)cap * 8, stream, s, st, b, cap, all_items ? 1 : 0);
 }
 
 void launch_mean(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {

@@ -161,6 +161,9 @@ struct MultiLaunch {
   // resolve phase: the first n_lean segments (lean_blocks blocks) belong to
   // sessions without guides
   uint32_t n_lean = 0, lean_blocks = 0;
+  // exhaustive phase: keys held in dynamic shared memory (exh_key_cap, the
+  // largest over the launch's steps)
+  uint32_t key_cap = 8192;
 };
 
 // Phases of a batch step, in launch order.
@@ -187,6 +190,8 @@ void launch_multi(int phase, const MultiLaunch &ml, uint32_t blocks, size_t smem
 // Lets a phase's multi-session kernel use `bytes` of dynamic shared memory
 // (current device).
 cudaError_t set_multi_smem(int phase, size_t bytes);
+// Keys the exhaustive k-NN holds in shared memory for a step (8 bytes each).
+uint32_t exh_key_cap(const SessionDev &s, const BatchDev &b);
 // Whether the full-evaluation team form has room for (k, m).
 bool team_full_fits(uint32_t k, uint32_t m);
 

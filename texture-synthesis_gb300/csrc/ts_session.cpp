@@ -2175,6 +2175,7 @@ struct PlannedLaunch {
   size_t smem;
   uint32_t fb0 = 0, n_fb = 0, pool_block0 = 0;  // exhaustive k-NN: fallback lists drained by a block pool
   uint32_t n_lean = 0, lean_blocks = 0;  // resolve: leading segments of sessions without guides
+  uint32_t key_cap = 0;                  // exhaustive: keys in shared memory (largest over the steps)
   int wait_rc = -1;  // first wait for the side stream's random candidates up to this launch of them
   int wait_items = -1;  // first wait for the side stream's item uploads up to this part
 };
@@ -2426,7 +2427,7 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
             if (ph == kPhaseExhaustive && stp.batch && c.k > 0 && !stp.exhaustive) {
               h_fb.push_back(Segment{0, 0, (uint32_t)j, (uint32_t)t});
               pl.n_fb += 1;
-              pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
+              pl.key_cap = std::max(pl.key_cap, exh_key_cap(c.sd, stp.bd));
             }
             const uint32_t units = phase_units(stp, c, ph);
             const uint32_t nb = multi_blocks(ph, units, phase_cap(stp, ph));
@@ -2434,7 +2435,10 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
             h_segs.push_back(Segment{pl.blocks, nb, (uint32_t)j, (uint32_t)t});
             pl.blocks += nb;
             pl.n_segs += 1;
-            pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
+            if (ph == kPhaseExhaustive)
+              pl.key_cap = std::max(pl.key_cap, exh_key_cap(c.sd, stp.bd));
+            else
+              pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
           }
           if (ph == kPhaseResolve && pass == 0) {
             pl.n_lean = pl.n_segs;
@@ -2443,6 +2447,7 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
         }
         pl.pool_block0 = pl.blocks;
         if (pl.n_fb) pl.blocks += kFallbackPool;
+        if (ph == kPhaseExhaustive) pl.smem = (size_t)pl.key_cap * 8;
         if (pl.n_segs || pl.n_fb) {
           phase_smem[ph] = std::max(phase_smem[ph], pl.smem);
           launches.push_back(pl);
@@ -2575,6 +2580,7 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
         ml.pool_block0 = pl.n_fb ? pl.pool_block0 : pl.blocks;
         ml.n_lean = pl.n_lean;
         ml.lean_blocks = pl.lean_blocks;
+        ml.key_cap = pl.key_cap;
         if (!pev.empty()) CUDA_TRY(cudaEventRecord(pev[li].a, s));
         launch_multi(pl.phase, ml, pl.blocks, pl.smem, s);
         if (!pev.empty()) CUDA_TRY(cudaEventRecord(pev[li].b, s));
@@ -2934,14 +2940,17 @@ void server_driver(ts_server *S) {
               if (ph == kPhaseExhaustive && stp.batch && c.k > 0 && !stp.exhaustive) {
                 fb.push_back(Segment{0, 0, r->slot, (uint32_t)r->cursor});
                 pl.n_fb += 1;
-                pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
+                pl.key_cap = std::max(pl.key_cap, exh_key_cap(c.sd, stp.bd));
               }
               const uint32_t nb = multi_blocks(ph, phase_units(stp, c, ph), phase_cap(stp, ph));
               if (nb == 0) continue;
               segs.push_back(Segment{pl.blocks, nb, r->slot, (uint32_t)r->cursor});
               pl.blocks += nb;
               pl.n_segs += 1;
-              pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
+              if (ph == kPhaseExhaustive)
+                pl.key_cap = std::max(pl.key_cap, exh_key_cap(c.sd, stp.bd));
+              else
+                pl.smem = std::max(pl.smem, multi_smem_bytes(ph, c.k, c.m));
             }
             if (ph == kPhaseResolve && pass == 0) {
               pl.n_lean = pl.n_segs;
@@ -2950,6 +2959,7 @@ void server_driver(ts_server *S) {
           }
           pl.pool_block0 = pl.blocks;
           if (pl.n_fb) pl.blocks += kFallbackPool;
+          if (ph == kPhaseExhaustive) pl.smem = (size_t)pl.key_cap * 8;
           if (pl.n_segs || pl.n_fb) {
             if (pl.smem > phase_smem[ph]) {
               CUDA_TRY(set_multi_smem(ph, pl.smem));
@@ -2975,6 +2985,7 @@ void server_driver(ts_server *S) {
           ml.pool_block0 = pl.n_fb ? pl.pool_block0 : pl.blocks;
           ml.n_lean = pl.n_lean;
           ml.lean_blocks = pl.lean_blocks;
+          ml.key_cap = pl.key_cap;
           launch_multi(pl.phase, ml, pl.blocks, pl.smem, S->st);
         }
         tick_launches = launches.size();
