@@ -2001,6 +2001,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     const double plan_ms = lap();
     run_alloc(c, st);
     CUDA_TRY(pitems.alloc(c.items.size()));
+    run_stage_tables(c);  // its pinned block too, before the device clock starts
     const double alloc_ms = lap();
     EventPair ev, ev_up, ev_rb;
     ev.create();
