@@ -2026,6 +2026,11 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve(SessionDev 
   pdl_enter();
   resolve_body<false>(s, st, b, blockIdx.x, gridDim.x);
 }
+// Sessions without guides (the guide terms compiled out).
+__global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve_lean(SessionDev s, StageDev st, BatchDev b) {
+  pdl_enter();
+  resolve_body<true>(s, st, b, blockIdx.x, gridDim.x);
+}
 __global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve_multi(MultiLaunch ml) {
   pdl_enter();
   const SegView v = find_segment(ml);
@@ -2127,6 +2132,8 @@ static cudaError_t raise_smem(K *kernel, size_t bytes) {
 
 cudaError_t configure_kernels(uint32_t k, uint32_t m) {
   cudaError_t e = raise_smem(k_resolve, resolve_smem_bytes(k, m, 0));
+  if (e != cudaSuccess) return e;
+  e = raise_smem(k_resolve_lean, resolve_smem_bytes(k, m, 0));
   if (e != cudaSuccess) return e;
   e = raise_smem(k_knn_exhaustive, kExhAllKeys * 8);
   if (e != cudaSuccess) return e;
@@ -2269,7 +2276,10 @@ void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, 
   const uint32_t n = b.i1 - b.i0;
   if (n == 0) return;
   const size_t smem = resolve_smem_bytes(s.k, s.m, s.guided);
-  launch_pdl(k_resolve, cdiv(n, kResolveWarps), kResolveWarps * kWarp, smem, stream, s, st, b);
+  if (s.guided)
+    launch_pdl(k_resolve, cdiv(n, kResolveWarps), kResolveWarps * kWarp, smem, stream, s, st, b);
+  else
+    launch_pdl(k_resolve_lean, cdiv(n, kResolveWarps), kResolveWarps * kWarp, smem, stream, s, st, b);
 }
 
 void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev &b, bool full,
