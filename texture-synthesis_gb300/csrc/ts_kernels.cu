@@ -253,14 +253,8 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
       const uint32_t b0 = __ballot_sync(0xffffffffu, h0);
       const uint32_t b1 = __ballot_sync(0xffffffffu, h1);
       const uint32_t r0 = count + __popc(b0 & lt), r1 = count + __popc(b0) + __popc(b1 & lt);
-      if (h0 && r0 < s.k) {
-        nbo[r0] = o0;
-        b.dist[(size_t)r0 * nb + local] = neighbour_dist(s, px, py, off_dx(o0), off_dy(o0), x2, y2);
-      }
-      if (h1 && r1 < s.k) {
-        nbo[r1] = o1;
-        b.dist[(size_t)r1 * nb + local] = neighbour_dist(s, px, py, off_dx(o1), off_dy(o1), x2, y2);
-      }
+      if (h0 && r0 < s.k) nbo[r0] = o0;
+      if (h1 && r1 < s.k) nbo[r1] = o1;
       count += __popc(b0) + __popc(b1);
     };
     // rounds look the bitmap up directly while the hits so far say that
@@ -291,6 +285,16 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
         if (count >= s.k) break;
       }
       __syncwarp();  // the window is rebuilt for the warp's next item
+    }
+    if (count >= s.k) {
+      // the distances once the k offsets are known, 32 per f64 warp
+      // instruction (an f64 instruction costs the same whatever its active
+      // lanes, and GB300's f64 pipe is narrow)
+      __syncwarp();
+      for (uint32_t j = lane; j < s.k; j += kWarp) {
+        const int32_t o = nbo[j];
+        b.dist[(size_t)j * nb + local] = neighbour_dist(s, px, py, off_dx(o), off_dy(o), x2, y2);
+      }
     }
     if (lane == 0) {
       if (count >= s.k) {
