@@ -161,6 +161,15 @@ __device__ __forceinline__ double neighbour_dist(const SessionDev &s, int px, in
   return __fma_rn(ddx, ddx, __dmul_rn(ddy, ddy));
 }
 
+// The same from the per-pixel tables only, for offsets within their radius
+// (every offset the walk's table holds): one f64 instruction, and no
+// predicated far-offset path beside it.
+__device__ __forceinline__ double neighbour_dist_near(const SessionDev &s, int px, int py, int dx, int dy) {
+  const int R = s.dtab_r;
+  const double ddx = __ldg(&s.dxt[(size_t)px * (2 * R + 1) + dx + R]);
+  return __fma_rn(ddx, ddx, __ldg(&s.dy2t[(size_t)py * (2 * R + 1) + dy + R]));
+}
+
 __device__ __forceinline__ unsigned long long nb_key(uint32_t d2, int x, int y) {
   return ((unsigned long long)d2 << 32) | ((uint32_t)(y + 32768) << 16) | (uint32_t)(x + 32768);
 }
@@ -238,7 +247,6 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
   for (uint32_t local = vb * kWalkWarps + (threadIdx.x >> 5); local < nb; local += vg * kWalkWarps) {
     const uint32_t pixel = st.items[b.i0 + local];
     const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
-    const double x2 = s.xdiv[px + s.xdiv_off], y2 = s.ydiv[py + s.ydiv_off];
     int32_t *nbo = b.nbuf + (size_t)local * s.k;
     uint32_t count = 0;
     const uint32_t tab_n = b.grid_first ? 0u : s.knn_tab_n;
@@ -293,7 +301,7 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
       __syncwarp();
       for (uint32_t j = lane; j < s.k; j += kWarp) {
         const int32_t o = nbo[j];
-        b.dist[(size_t)j * nb + local] = neighbour_dist(s, px, py, off_dx(o), off_dy(o), x2, y2);
+        b.dist[(size_t)j * nb + local] = neighbour_dist_near(s, px, py, off_dx(o), off_dy(o));
       }
     }
     if (lane == 0) {

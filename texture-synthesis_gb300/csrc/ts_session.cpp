@@ -45,6 +45,7 @@ constexpr uint32_t kMaxExamples = 256;
 constexpr uint32_t kMaxSide = 16384;
 constexpr float kTilingBoundary = 0.05f;  // TILING_BOUNDARY_PERCENTAGE, ms.rs:15
 constexpr int kDistTabRadius = 64;  // offsets the weight tables cover
+static_assert(kDistTabRadius >= kKnnTabRadius, "the walk's distances come from the tables alone");
 constexpr uint64_t kRcandBudget = 64ull << 20;  // random-candidate entries held at once
 // Walk steps of at most this many items are latency-bound: their sparse items
 // build a bitmap window instead of more rounds of bitmap loads.
