@@ -55,6 +55,7 @@ constexpr int kTeamThreads = 128;
 constexpr int kTeamFullThreads = 256;  // the full-evaluation form: batches of at most ~1000 items
 constexpr int kExhCap = 2048;      // keys kept by the exhaustive k-NN at the cut distance
 constexpr int kExhAllKeys = 8192;  // keys the exhaustive k-NN sorts in shared memory directly
+constexpr int kExhSortAll = 256;   // at most this many keys are sorted without a select
 constexpr uint32_t kMaxDraws = 1u << 22;
 
 __device__ const double g_exp2_64[64] = {TS_EXP2_TABLE_VALUES};
@@ -330,6 +331,7 @@ struct ExhShared {
   uint32_t rank;
   int overflow;
   uint32_t flag, cnt;  // cell-grid search: a ring cell lies in the grid; keys below the bound
+  uint32_t below, le;  // select: keys below the selected digit's range; at or below it
 };
 
 constexpr uint32_t kExhGridFrom = 4096;  // resolved points from which the cell grid is searched
@@ -372,20 +374,22 @@ __device__ __forceinline__ void for_points(const SessionDev &s, uint32_t n_res, 
 }
 
 __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
-                                    ExhShared &sh, unsigned long long *all, uint32_t cap, bool with_mean);
+                                    ExhShared &sh, unsigned long long *all, uint32_t cap, bool with_mean,
+                                    bool use_grid = true);
 
 // One CTA per item.  `all` (dynamic shared memory, kExhAllKeys entries)
 // receives every point's key in one pass over the resolved list; when they
 // fit, a bitonic sort of them gives the answer directly, otherwise a
 // radix select over further passes finds the cut distance first.
 __device__ __forceinline__ void knn_exhaustive_body(const SessionDev &s, const StageDev &st, const BatchDev &b,
-                                                    int all_items, uint32_t cap, uint32_t vb, uint32_t vg) {
+                                                    int all_items, uint32_t cap, uint32_t vb, uint32_t vg,
+                                                    bool use_grid = true) {
   __shared__ ExhShared sh;
   extern __shared__ unsigned long long all_keys[];
   const uint32_t n = all_items ? b.i1 - b.i0 : *b.fb_count;
   for (uint32_t e = vb; e < n; e += vg) {
     const uint32_t local = all_items ? e : b.fb_list[e];
-    knn_exhaustive_item(s, st, b, local, sh, all_keys, cap, all_items != 0);
+    knn_exhaustive_item(s, st, b, local, sh, all_keys, cap, all_items != 0, use_grid);
     __syncthreads();
   }
 }
@@ -504,7 +508,8 @@ __device__ void grid_collect(const SessionDev &s, int px, int py, uint32_t k, Ex
 }
 
 __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
-                                    ExhShared &sh, unsigned long long *all, uint32_t cap, bool with_mean) {
+                                    ExhShared &sh, unsigned long long *all, uint32_t cap, bool with_mean,
+                                    bool use_grid) {
   const uint32_t pixel = st.items[b.i0 + local];
   const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
   const uint32_t k = s.k;
@@ -525,35 +530,37 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
   // shared atomic per warp and round.  Many points: the cell grid's rings
   // instead, which hold the k nearest.
   const int lane = threadIdx.x & 31;
-  const bool grid = s.cells != nullptr && n_res > kExhGridFrom;
+  const bool grid = use_grid && s.cells != nullptr && n_res > kExhGridFrom;
   if (grid) grid_collect(s, px, py, k, sh, all, cap);
-  for (uint32_t e0 = 0; e0 < (grid ? 0u : n_res); e0 += blockDim.x) {
-    const uint32_t e = e0 + threadIdx.x;
-    int xs[3], ys[3];
-    uint32_t cnt = 0;
-    if (e < n_res) {
-      const uint32_t p = s.resolved[e];
-      const int x = (int)(p % s.W), y = (int)(p / s.W);
-      xs[0] = x;
-      ys[0] = y;
-      cnt = 1;
-      if (s.tiling && mir_bit(s, (uint32_t)x, (uint32_t)y)) {
-        if (x < s.x_l) {
-          xs[cnt] = x + (int)s.W;
-          ys[cnt++] = y;
-        } else if (x > s.x_r) {
-          xs[cnt] = x - (int)s.W;
-          ys[cnt++] = y;
-        }
-        if (y < s.y_b) {
-          xs[cnt] = x;
-          ys[cnt++] = y + (int)s.H;
-        } else if (y > s.y_t) {
-          xs[cnt] = x;
-          ys[cnt++] = y - (int)s.H;
-        }
-      }
+  // kPts points per thread and round: their loads (the point, then its
+  // mirror bit) are all in flight together
+  constexpr int kPts = 4;
+  for (uint32_t e0 = 0; e0 < (grid ? 0u : n_res); e0 += kPts * blockDim.x) {
+    uint32_t pt[kPts];
+#pragma unroll
+    for (int u = 0; u < kPts; ++u) {
+      const uint32_t e = e0 + (uint32_t)u * blockDim.x + threadIdx.x;
+      pt[u] = e < n_res ? __ldg(&s.resolved[e]) : 0xffffffffu;
     }
+    // up to three keys per point in fixed slots (the point, its mirror
+    // across x, its mirror across y), compacted through a bit mask
+    int xs[3 * kPts], ys[3 * kPts];
+    uint32_t vm = 0;
+#pragma unroll
+    for (int u = 0; u < kPts; ++u) {
+      const int x = (int)(pt[u] % s.W), y = (int)(pt[u] / s.W);
+      const bool mb = pt[u] != 0xffffffffu && s.tiling && mir_bit(s, (uint32_t)x, (uint32_t)y);
+      xs[3 * u] = x;
+      ys[3 * u] = y;
+      xs[3 * u + 1] = x < s.x_l ? x + (int)s.W : x - (int)s.W;
+      ys[3 * u + 1] = y;
+      xs[3 * u + 2] = x;
+      ys[3 * u + 2] = y < s.y_b ? y + (int)s.H : y - (int)s.H;
+      if (pt[u] != 0xffffffffu) vm |= 1u << (3 * u);
+      if (mb && (x < s.x_l || x > s.x_r)) vm |= 2u << (3 * u);
+      if (mb && (y < s.y_b || y > s.y_t)) vm |= 4u << (3 * u);
+    }
+    const uint32_t cnt = (uint32_t)__popc(vm);
     uint32_t incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -564,10 +571,14 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
     if (lane == 31) base = atomicAdd(&sh.total, incl);
     base = __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
     uint32_t dor = 0;
-    for (uint32_t i = 0; i < cnt; ++i) {
-      const uint32_t d2 = d2of(xs[i], ys[i]);
-      dor |= d2;
-      if (base + i < cap) all[base + i] = nb_key(d2, xs[i], ys[i]);
+#pragma unroll
+    for (int i = 0; i < 3 * kPts; ++i) {
+      if ((vm >> i) & 1u) {
+        const uint32_t d2 = d2of(xs[i], ys[i]);
+        dor |= d2;
+        const uint32_t slot = base + (uint32_t)__popc(vm & ((1u << i) - 1u));
+        if (slot < cap) all[slot] = nb_key(d2, xs[i], ys[i]);
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) dor |= __shfl_xor_sync(0xffffffffu, dor, o);
@@ -575,7 +586,7 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
   }
   __syncthreads();
   uint32_t total = sh.total;
-  if (!grid && total > cap && s.cells != nullptr) {
+  if (use_grid && !grid && total > cap && s.cells != nullptr) {
     __syncthreads();
     grid_collect(s, px, py, k, sh, all, cap);
     total = sh.total;
@@ -583,24 +594,38 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
   const unsigned long long *sorted;
   uint32_t n;
   if (total <= k || total <= cap) {
-    // radix select of the k-th smallest d2 over the shared keys, digits of
-    // 8 bits from the highest significant bit down
+    // radix select over the shared keys, digits of up to 8 bits from the
+    // highest significant bit of any d2 down, until the keys at or below the
+    // selected digit's range fit the sort buffer (for points spread over an
+    // area d2 is near uniform, so the first digit usually suffices); few
+    // keys are sorted whole
     const uint32_t dor_all = sh.prefix;
     const int bits = dor_all ? 32 - __clz(dor_all) : 1;
     uint32_t D = 0xffffffffu;
-    if (total > k) {
+    if (total > k && total > (uint32_t)kExhSortAll) {
       __syncthreads();
       if (threadIdx.x == 0) {
         sh.prefix = 0;
         sh.rank = k;
+        sh.below = 0;
       }
-      for (int shift = ((bits - 1) / 8) * 8; shift >= 0; shift -= 8) {
+      int hi = bits;  // the bits at and above hi are fixed by the prefix
+      for (;;) {
+        const int lo = max(hi - 8, 0);
+        const uint32_t dmask = (1u << (hi - lo)) - 1u;
         for (int i = threadIdx.x; i < 256; i += blockDim.x) sh.hist[i] = 0;
         __syncthreads();
         const uint32_t prefix = sh.prefix;
-        for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) {
-          const uint32_t d2 = (uint32_t)(all[i] >> 32);
-          if (shift == 24 || ((d2 ^ prefix) >> (shift + 8)) == 0) atomicAdd(&sh.hist[(d2 >> shift) & 255u], 1u);
+        for (uint32_t i0 = 0; i0 < total; i0 += blockDim.x) {
+          const uint32_t i = i0 + threadIdx.x;
+          uint32_t bin = 0xffffffffu;
+          if (i < total) {
+            const uint32_t d2 = (uint32_t)(all[i] >> 32);
+            if (hi >= 32 || (d2 >> hi) == (prefix >> hi)) bin = (d2 >> lo) & dmask;
+          }
+          // one shared atomic per distinct digit of the warp
+          const uint32_t peers = __match_any_sync(0xffffffffu, bin);
+          if (bin != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&sh.hist[bin], (uint32_t)__popc(peers));
         }
         __syncthreads();
         if (threadIdx.x < 32) {
@@ -618,19 +643,26 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
             if (lane >= o) off += t;
           }
           off -= acc;  // exclusive prefix of this lane's 8 bins
-          const uint32_t rank = sh.rank;
+          const uint32_t rank = sh.rank, below = sh.below;
+          __syncwarp();
 #pragma unroll
           for (int q = 0; q < 8; ++q) {
-            const uint32_t lo = off + (q ? v[q - 1] : 0u), hi = off + v[q];
-            if (lo < rank && rank <= hi) {
-              sh.prefix = prefix | ((uint32_t)(lane * 8 + q) << shift);
-              sh.rank = rank - lo;
+            const uint32_t lo_c = off + (q ? v[q - 1] : 0u), hi_c = off + v[q];
+            if (lo_c < rank && rank <= hi_c) {
+              sh.prefix = prefix | ((uint32_t)(lane * 8 + q) << lo);
+              sh.rank = rank - lo_c;
+              sh.le = below + hi_c;  // keys at or below the digit's range
+              sh.below = below + lo_c;
             }
           }
         }
         __syncthreads();
+        if (lo == 0 || sh.le <= (uint32_t)kExhCap) {
+          D = sh.prefix | ((1u << lo) - 1u);
+          break;
+        }
+        hi = lo;
       }
-      D = sh.prefix;
       // keys at or below the cut, into the small buffer
       if (threadIdx.x == 0) sh.nkeys = 0;
       __syncthreads();
@@ -736,7 +768,7 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
   }
   if (with_mean) {
     __syncthreads();
-    if (threadIdx.x == 0 && nout > 0) {  // the mean (ms.rs:417-423), as k_mean computes it
+    if (threadIdx.x == 0 && nout > 0) {  // the mean (ms.rs:417-423), as k_mean_staged computes it
       // one thread: the four adds of a distance in integer arithmetic while
       // the sum stays in its binade, else four f64 adds (64 cycles each)
       uint64_t acc = 0;
@@ -1215,7 +1247,6 @@ __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev
   const WarpSmem w = carve(smem + 2048 + (size_t)warp * warp_smem_bytes(s.k, s.m), s.k, s.m);
   __syncthreads();
   const uint32_t nb = b.i1 - b.i0;
-  const int W = (int)s.W, H = (int)s.H;
   for (uint32_t local = vb * kResolveWarps + warp; local < nb; local += vg * kResolveWarps) {
     const uint32_t item = b.i0 + local;
     const uint32_t pixel = st.items[item];
@@ -2026,8 +2057,6 @@ __global__ void __launch_bounds__(kMeanThreads) k_mean_staged(SessionDev s, Stag
   mean_body_staged(b, blockIdx.x);
 }
 
-__global__ void __launch_bounds__(128) k_mean(SessionDev s, StageDev st, BatchDev b) {
-  pdl_enter(); mean_body(s, b, blockIdx.x); }
 __global__ void __launch_bounds__(128) k_mean_multi(MultiLaunch ml) {
   pdl_enter();
   const SegView v = find_segment(ml);
@@ -2065,6 +2094,21 @@ __global__ void __launch_bounds__(T) k_resolve_team_multi(MultiLaunch ml) {
   pdl_enter();
   const SegView v = find_segment(ml);
   resolve_team_body<T, kFull>(*v.s, v.d->st, v.d->b, v.vb, v.vg);
+}
+
+// One step of a batch of new items whose neighbours the exhaustive k-NN
+// finds, one item per CTA at a time: its k-NN and mean, then the
+// full-evaluation team resolve, in one launch.  The other CTAs' commits
+// change only their own pixels, the resolved list beyond n_res and the
+// occupancy, mirror and cell records of those pixels; this k-NN reads the
+// first n_res points and their mirror bits only (the cell grid is not
+// searched here; a key buffer overflow rescans the points).
+__global__ void __launch_bounds__(kTeamFullThreads) k_step_team_full(SessionDev s, StageDev st, BatchDev b,
+                                                                      uint32_t cap) {
+  pdl_enter();
+  knn_exhaustive_body(s, st, b, 1, cap, blockIdx.x, gridDim.x, false);
+  __syncthreads();
+  resolve_team_body<kTeamFullThreads, true>(s, st, b, blockIdx.x, gridDim.x);
 }
 
 __global__ void k_commit(SessionDev s, StageDev st, BatchDev b) {
@@ -2154,7 +2198,11 @@ cudaError_t configure_kernels(uint32_t k, uint32_t m) {
   e = raise_smem(k_resolve_team<kTeamThreads, false>, team_smem_bytes(k, m));
   if (e != cudaSuccess) return e;
   const size_t fsm = team_full_smem_bytes(k, m);
-  if (fsm <= kTeamFullMaxSmem) return raise_smem(k_resolve_team<kTeamFullThreads, true>, fsm);
+  if (fsm <= kTeamFullMaxSmem) {
+    e = raise_smem(k_resolve_team<kTeamFullThreads, true>, fsm);
+    if (e != cudaSuccess) return e;
+    return raise_smem(k_step_team_full, std::max<size_t>(fsm, (size_t)kExhAllKeys * 8));
+  }
   return cudaSuccess;
 }
 
@@ -2304,6 +2352,15 @@ void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev
                st, b);
   else
     launch_pdl(k_resolve_team<kTeamThreads, false>, grid, kTeamThreads, team_smem_bytes(s.k, s.m), stream, s, st, b);
+}
+
+void launch_step_team_full(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
+  const uint32_t n = b.i1 - b.i0;
+  if (n == 0) return;
+  const uint32_t grid = n < 608u ? n : 608u;
+  const uint32_t cap = exh_key_cap(s, b);
+  const size_t smem = std::max<size_t>((size_t)cap * 8, team_full_smem_bytes(s.k, s.m));
+  launch_pdl(k_step_team_full, grid, kTeamFullThreads, smem, stream, s, st, b, cap);
 }
 
 void launch_commit(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {

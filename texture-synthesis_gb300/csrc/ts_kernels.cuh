@@ -208,6 +208,10 @@ void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, 
 // for batches far too small to fill the GPU), otherwise candidate 0 first
 // and the rest with early exit.
 void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev &b, bool full, cudaStream_t stream);
+// One step of a batch whose neighbours the exhaustive k-NN finds, resolved
+// in the full-evaluation team form (when team_full_fits): both in one
+// launch, one CTA per item.
+void launch_step_team_full(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
 void launch_commit(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
 void launch_level_switch(const SessionDev &s, uint32_t level, uint32_t n_res, cudaStream_t stream);
 

@@ -1845,6 +1845,16 @@ void enqueue_step(RunCtx &c, const Step &stp, cudaStream_t st, LaunchTimer &lt) 
   }
   if (stp.batch) {
     lt.items = stp.n;
+    if (c.k > 0 && stp.exhaustive && stp.resolve == kPhaseTeamFull && team_full_fits(sd.k, sd.m)) {
+      // small batch, exhaustive k-NN: neighbours, mean and resolve in one launch
+      lt.run(TS_KERNEL_RESOLVE, [&] { launch_step_team_full(sd, stp.st, stp.bd, st); });
+      c.launches += 1;
+      if (!stp.bd.fused_commit) {
+        lt.run(TS_KERNEL_COMMIT, [&] { launch_commit(sd, stp.st, stp.bd, st); });
+        c.launches += 1;
+      }
+      return;
+    }
     if (c.k > 0) {
       if (stp.exhaustive) {
         lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, stp.st, stp.bd, true, st); });
