@@ -414,6 +414,33 @@ __device__ __forceinline__ void block_bitonic(unsigned long long *keys, uint32_t
   }
 }
 
+// The first `nout` of the n distinct keys in keys[] in ascending order.
+// Up to kExhRankSort keys: each key's rank is the count of smaller keys (all
+// threads read the same key at a time), and the key lands at out[rank] when
+// the rank is below nout; more keys: a bitonic sort in place.  Returns the
+// sorted array.
+constexpr uint32_t kExhRankSort = 512;
+__device__ __forceinline__ const unsigned long long *sort_first(unsigned long long *keys, uint32_t n, uint32_t nout,
+                                                                unsigned long long *out) {
+  if (n <= kExhRankSort) {
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const unsigned long long key = keys[i];
+      uint32_t r = 0;
+#pragma unroll 8
+      for (uint32_t q = 0; q < n; ++q) r += keys[q] < key ? 1u : 0u;
+      if (r < nout) out[r] = key;
+    }
+    __syncthreads();
+    return out;
+  }
+  uint32_t np2 = 1;
+  while (np2 < n) np2 <<= 1;
+  for (uint32_t i = n + threadIdx.x; i < np2; i += blockDim.x) keys[i] = ~0ull;
+  __syncthreads();
+  block_bitonic(keys, np2);
+  return keys;
+}
+
 // The points of the cells in rings around the item's cell, as keys in
 // all[], until k keys lie below the rings' reach: after rings 0..r every
 // point with d2 < (r * kCell + 1)^2 has been seen (the cells beyond are that
@@ -689,12 +716,7 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
       return;
     }
     n = sh.nkeys;
-    uint32_t np2 = 1;
-    while (np2 < n) np2 <<= 1;
-    for (uint32_t i = n + threadIdx.x; i < np2; i += blockDim.x) sh.keys[i] = ~0ull;
-    __syncthreads();
-    block_bitonic(sh.keys, np2);
-    sorted = sh.keys;
+    sorted = sort_first(sh.keys, n, n < k ? n : k, all);
   } else {
     if (threadIdx.x == 0) {
       sh.prefix = 0;
@@ -747,12 +769,7 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
       return;
     }
     n = sh.nkeys;
-    uint32_t np2 = 1;
-    while (np2 < n) np2 <<= 1;
-    for (uint32_t i = n + threadIdx.x; i < np2; i += blockDim.x) sh.keys[i] = ~0ull;
-    __syncthreads();
-    block_bitonic(sh.keys, np2);
-    sorted = sh.keys;
+    sorted = sort_first(sh.keys, n, n < k ? n : k, all);
   }
   const uint32_t nout = n < k ? n : k;
   int32_t *nbo = b.nbuf + (size_t)local * k;
@@ -2068,7 +2085,7 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve(SessionDev 
   resolve_body<false>(s, st, b, blockIdx.x, gridDim.x);
 }
 // Sessions without guides (the guide terms compiled out).
-__global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve_lean(SessionDev s, StageDev st, BatchDev b) {
+__global__ void __launch_bounds__(kResolveWarps *kWarp, 9) k_resolve_lean(SessionDev s, StageDev st, BatchDev b) {
   pdl_enter();
   resolve_body<true>(s, st, b, blockIdx.x, gridDim.x);
 }
