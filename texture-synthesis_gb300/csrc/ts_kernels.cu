@@ -321,8 +321,31 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
 // every resolved point and its mirrors, keep the points at or below it, sort
 // them by (d2, y, x) and emit the first k.
 // ---------------------------------------------------------------------------
+// The mean of a neighbour distance list on one thread (ms.rs:417-423, as
+// k_mean_staged computes it): the four adds of a distance in integer
+// arithmetic while the sum stays in its binade, else four f64 adds (64
+// cycles each), then / (4n).
+__device__ __forceinline__ double mean_chain(const double *d, uint32_t n) {
+  uint64_t acc = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    const double v = d[i];
+    uint64_t nx;
+    if (!ts_add4_fast(acc, dbl_bits(v), nx)) {
+      double a = bits_dbl(acc);
+      a = __dadd_rn(a, v);
+      a = __dadd_rn(a, v);
+      a = __dadd_rn(a, v);
+      a = __dadd_rn(a, v);
+      nx = dbl_bits(a);
+    }
+    acc = nx;
+  }
+  return __ddiv_rn(bits_dbl(acc), (double)(n * 4u));
+}
+
 struct ExhShared {
   double dist[256];  // the item's neighbour distances, when the kernel also computes the mean
+  int32_t nbo[256];  // and their offsets
   uint32_t hist[256];
   unsigned long long keys[kExhCap];
   uint32_t nkeys;
@@ -373,9 +396,9 @@ __device__ __forceinline__ void for_points(const SessionDev &s, uint32_t n_res, 
   }
 }
 
-__device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
-                                    ExhShared &sh, unsigned long long *all, uint32_t cap, bool with_mean,
-                                    bool use_grid = true);
+__device__ uint32_t knn_exhaustive_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
+                                        ExhShared &sh, unsigned long long *all, uint32_t cap, bool with_mean,
+                                        bool use_grid = true, bool mean_here = true);
 
 // One CTA per item.  `all` (dynamic shared memory, kExhAllKeys entries)
 // receives every point's key in one pass over the resolved list; when they
@@ -534,9 +557,9 @@ __device__ void grid_collect(const SessionDev &s, int px, int py, uint32_t k, Ex
   }
 }
 
-__device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
-                                    ExhShared &sh, unsigned long long *all, uint32_t cap, bool with_mean,
-                                    bool use_grid) {
+__device__ uint32_t knn_exhaustive_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
+                                        ExhShared &sh, unsigned long long *all, uint32_t cap, bool with_mean,
+                                        bool use_grid, bool mean_here) {
   const uint32_t pixel = st.items[b.i0 + local];
   const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
   const uint32_t k = s.k;
@@ -713,7 +736,7 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
         set_err(s.err, kDevErrLimit);
         b.ncnt[local] = 0;
       }
-      return;
+      return 0;
     }
     n = sh.nkeys;
     sorted = sort_first(sh.keys, n, n < k ? n : k, all);
@@ -766,7 +789,7 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
         set_err(s.err, kDevErrLimit);
         b.ncnt[local] = 0;
       }
-      return;
+      return 0;
     }
     n = sh.nkeys;
     sorted = sort_first(sh.keys, n, n < k ? n : k, all);
@@ -781,31 +804,17 @@ __device__ void knn_exhaustive_item(const SessionDev &s, const StageDev &st, con
     nbo[i] = pack_off(x - px, y - py);
     const double d = neighbour_dist(s, px, py, x - px, y - py, x2, y2);
     b.dist[(size_t)i * nb + local] = d;
-    if (with_mean) sh.dist[i] = d;
-  }
-  if (with_mean) {
-    __syncthreads();
-    if (threadIdx.x == 0 && nout > 0) {  // the mean (ms.rs:417-423), as k_mean_staged computes it
-      // one thread: the four adds of a distance in integer arithmetic while
-      // the sum stays in its binade, else four f64 adds (64 cycles each)
-      uint64_t acc = 0;
-      for (uint32_t i = 0; i < nout; ++i) {
-        const double d = sh.dist[i];
-        uint64_t nx;
-        if (!ts_add4_fast(acc, dbl_bits(d), nx)) {
-          double a = bits_dbl(acc);
-          a = __dadd_rn(a, d);
-          a = __dadd_rn(a, d);
-          a = __dadd_rn(a, d);
-          a = __dadd_rn(a, d);
-          nx = dbl_bits(a);
-        }
-        acc = nx;
-      }
-      b.mean[local] = __ddiv_rn(bits_dbl(acc), (double)(nout * 4u));
+    if (with_mean) {
+      sh.dist[i] = d;
+      sh.nbo[i] = pack_off(x - px, y - py);
     }
   }
+  if (with_mean && mean_here) {
+    __syncthreads();
+    if (threadIdx.x == 0 && nout > 0) b.mean[local] = mean_chain(sh.dist, nout);
+  }
   if (threadIdx.x == 0) b.ncnt[local] = nout;
+  return nout;
 }
 
 // ---------------------------------------------------------------------------
@@ -991,18 +1000,22 @@ __device__ __forceinline__ bool candidate_cost_padded(const SessionDev &s, const
 // (ms.rs:1151-1181, wrapped when tiling), the record in shared memory, and
 // the neighbour's coherence candidate (ms.rs:497-547): its source plus the
 // shift to the centre, kept if valid.  Returns true for a valid candidate.
-template <bool kG = true>
-__device__ __forceinline__ bool neighbour_setup(const SessionDev &s, const StageDev &st, const BatchDev &b,
-                                                uint32_t local, uint32_t nb, int px, int py, uint32_t j, int32_t off,
-                                                double avg, const double *tab, const float *tab_ff,
-                                                const WarpSmem &w, uint32_t &cxy, uint32_t &aux, bool &nan_w,
-                                                int &maxoff, bool &bad_map) {
-  const int W = (int)s.W, H = (int)s.H;
-  const double dj = b.dist[(size_t)j * nb + local];
+// The weight alone, w = (f32) exp(-(d / mean)) (find_best_match,
+// ms.rs:1198-1203): the double-f32 path when it decides, else the exact f64
+// one.
+__device__ __forceinline__ float neighbour_weight(double dj, double avg, const double *tab, const float *tab_ff) {
   float wv;
   if (!ts_weight_ff(dj, avg, tab_ff, wv))
     wv = __double2float_rn(ts_exp64(-1.0 * ts_div_markstein(dj, avg, __drcp_rn(avg)), tab));
-  nan_w |= (wv != wv);
+  return wv;
+}
+
+// Everything of neighbour_setup but the weight, which the record gets as wv.
+template <bool kG = true>
+__device__ __forceinline__ bool neighbour_records(const SessionDev &s, const StageDev &st, int px, int py, uint32_t j,
+                                                  int32_t off, float wv, const WarpSmem &w, uint32_t &cxy,
+                                                  uint32_t &aux, int &maxoff, bool &bad_map) {
+  const int W = (int)s.W, H = (int)s.H;
   maxoff = max(maxoff, max(abs(off_dx(off)), abs(off_dy(off))));
   const int nx = px + off_dx(off), ny = py + off_dy(off);
   int qx = nx, qy = ny;
@@ -1029,6 +1042,17 @@ __device__ __forceinline__ bool neighbour_setup(const SessionDev &s, const Stage
   cxy = (uint32_t)ccx | ((uint32_t)ccy << 16);
   aux = map | (j << 16);
   return true;
+}
+
+template <bool kG = true>
+__device__ __forceinline__ bool neighbour_setup(const SessionDev &s, const StageDev &st, const BatchDev &b,
+                                                uint32_t local, uint32_t nb, int px, int py, uint32_t j, int32_t off,
+                                                double avg, const double *tab, const float *tab_ff,
+                                                const WarpSmem &w, uint32_t &cxy, uint32_t &aux, bool &nan_w,
+                                                int &maxoff, bool &bad_map) {
+  const float wv = neighbour_weight(b.dist[(size_t)j * nb + local], avg, tab, tab_ff);
+  nan_w |= (wv != wv);
+  return neighbour_records<kG>(s, st, px, py, j, off, wv, w, cxy, aux, maxoff, bad_map);
 }
 
 // Candidate 0's exact score (better_match, ms.rs:1225-1288, with no bound):
@@ -1488,7 +1512,7 @@ __device__ __forceinline__ void resolve_team_body(const SessionDev &s, const Sta
     if (!slow && kFull && padded) {
       // every term nps(c, j) * w_j in parallel, then each candidate's
       // in-order sum on one thread: the reference's scores, all of them.
-      // Padded planes: each candidate's plane offset once, then four texel
+      // Padded planes: each candidate's plane offset once, then eight texel
       // loads in flight per thread before their terms are formed.
       unsigned long long *cb = (unsigned long long *)(term + (((size_t)nk * nc + 1) & ~(size_t)1));
       for (uint32_t c = tid; c < nc; c += T) {
@@ -1500,10 +1524,10 @@ __device__ __forceinline__ void resolve_team_body(const SessionDev &s, const Sta
       }
       __syncthreads();
       const uint32_t total = nc * nk;
-      for (uint32_t i0 = tid; i0 < total; i0 += 4 * T) {
-        uint32_t tx[4], gx[4], ii[4], jj[4];
+      for (uint32_t i0 = tid; i0 < total; i0 += 8 * T) {
+        uint32_t tx[8], gx[8], ii[8], jj[8];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < 8; ++u) {
           const uint32_t i = i0 + (uint32_t)u * T;
           ii[u] = i;
           if (i < total) {
@@ -1517,7 +1541,7 @@ __device__ __forceinline__ void resolve_team_body(const SessionDev &s, const Sta
           }
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < 8; ++u) {
           if (ii[u] < total) {
             const uint4 nr = w.nbr[jj[u]];
             float nps = lut4(lc, __vabsdiffu4(nr.y, tx[u]), 0.0f);
@@ -2114,18 +2138,248 @@ __global__ void __launch_bounds__(T) k_resolve_team_multi(MultiLaunch ml) {
 }
 
 // One step of a batch of new items whose neighbours the exhaustive k-NN
-// finds, one item per CTA at a time: its k-NN and mean, then the
-// full-evaluation team resolve, in one launch.  The other CTAs' commits
+// finds, one item per CTA at a time (256 threads): the item's k-NN, then its
+// full-evaluation resolve (every candidate scored completely, as the team
+// form does), in one launch.  The mean's chain of 4k dependent f64 adds
+// (ms.rs:417-423) runs on warp 0's first lane while warps 1-7 set up the
+// neighbour records and candidates and gather every (candidate, neighbour)
+// LUT sum, none of which needs the mean; the weights and each candidate's
+// in-order sum of nps_j * w_j follow on all warps.  The other CTAs' commits
 // change only their own pixels, the resolved list beyond n_res and the
 // occupancy, mirror and cell records of those pixels; this k-NN reads the
 // first n_res points and their mirror bits only (the cell grid is not
 // searched here; a key buffer overflow rescans the points).
+constexpr int kStepSetupThreads = kTeamFullThreads - kWarp;  // warps 1..7
+
+__device__ __forceinline__ void setup_bar() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kStepSetupThreads) : "memory");
+}
+
 __global__ void __launch_bounds__(kTeamFullThreads) k_step_team_full(SessionDev s, StageDev st, BatchDev b,
                                                                       uint32_t cap) {
+  constexpr int T = kTeamFullThreads, NW = T / kWarp, TS = kStepSetupThreads;
+  __shared__ ExhShared sh;
+  __shared__ double tab[64];
+  __shared__ float tab_ff[128];
+  __shared__ uint32_t wcnt[NW];
+  __shared__ float red_s[NW];
+  __shared__ uint32_t red_i[NW];
+  __shared__ int sh_flags, sh_maxoff;
+  __shared__ uint32_t sh_ncoh;
+  __shared__ double sh_mean;
+  extern __shared__ __align__(16) unsigned char smem[];
   pdl_enter();
-  knn_exhaustive_body(s, st, b, 1, cap, blockIdx.x, gridDim.x, false);
-  __syncthreads();
-  resolve_team_body<kTeamFullThreads, true>(s, st, b, blockIdx.x, gridDim.x);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t nb = b.i1 - b.i0;
+  float *lc = (float *)smem;
+  float *lg = lc + 256;
+  const WarpSmem w = carve(smem + 2048, s.k, s.m);
+  float *term = (float *)(smem + 2048 + warp_smem_bytes(s.k, s.m));
+  for (uint32_t local = blockIdx.x; local < nb; local += gridDim.x) {
+    const uint32_t nk = knn_exhaustive_item(s, st, b, local, sh, (unsigned long long *)smem, cap, true, false, false);
+    __syncthreads();  // sh.dist, sh.nbo; the key buffer is free again
+    const uint32_t item = b.i0 + local;
+    const uint32_t pixel = st.items[item];
+    const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
+    const bool is_new = item >= st.redo;
+    if (nk == 0) {
+      if (tid == 0) write_random_result(s, st, b, local, pixel);
+      __syncthreads();
+      continue;
+    }
+    if (warp == 0) {
+      if (lane == 0) {
+        const double mean = mean_chain(sh.dist, nk);
+        sh_mean = mean;
+        b.mean[local] = mean;
+      }
+    } else {
+      const int t = tid - kWarp;
+      for (int i = t; i < 512; i += TS) lc[i] = st.lut[i];
+      for (int i = t; i < 64; i += TS) tab[i] = g_exp2_64[i];
+      for (int i = t; i < 128; i += TS) tab_ff[i] = g_exp2_ff[i];
+      if (t == 0) {
+        sh_flags = 0;
+        sh_maxoff = 0;
+      }
+      setup_bar();
+      // neighbour records and coherence candidates, compacted in order
+      bool bad_map = false;
+      int maxoff = 0;
+      uint32_t ncoh = 0;
+      for (uint32_t j0 = 0; j0 < nk; j0 += TS) {
+        const uint32_t j = j0 + t;
+        bool valid = false;
+        uint32_t cxy = 0, aux = 0;
+        if (j < nk) valid = neighbour_records(s, st, px, py, j, sh.nbo[j], 0.0f, w, cxy, aux, maxoff, bad_map);
+        const uint32_t bal = __ballot_sync(0xffffffffu, valid);
+        if (lane == 0) wcnt[warp] = __popc(bal);
+        setup_bar();
+        uint32_t base = ncoh, total = 0;
+#pragma unroll
+        for (int i = 1; i < NW; ++i) {
+          if (i < warp) base += wcnt[i];
+          total += wcnt[i];
+        }
+        if (valid) {
+          const uint32_t slot = base + __popc(bal & lt);
+          w.cxy[slot] = cxy;
+          w.caux[slot] = aux;
+        }
+        ncoh += total;
+        setup_bar();
+      }
+      if (bad_map) atomicOr(&sh_flags, 2);
+      if (maxoff) atomicMax(&sh_maxoff, maxoff);
+      const uint2 *rc = st.rcand + (size_t)item * s.m;
+      for (uint32_t q = t; q < s.m; q += TS) {
+        const uint2 v = rc[q];
+        w.cxy[ncoh + q] = v.x;
+        w.caux[ncoh + q] = v.y | kAuxNeg | (q << 16);
+      }
+      if (t == 0) sh_ncoh = ncoh;
+      setup_bar();
+      if (!(sh_flags & 2) && !st.slow_lut) {
+        // every candidate's LUT sums nps(c, j), before the weights exist
+        const uint32_t nc = ncoh + s.m, total = nc * nk;
+        if (sh_maxoff <= kPad && !s.guide_dims_differ) {
+          unsigned long long *cb = (unsigned long long *)(term + (((size_t)nk * nc + 1) & ~(size_t)1));
+          for (uint32_t c = t; c < nc; c += TS) {
+            const uint32_t cxy = w.cxy[c], aux = w.caux[c];
+            const MapDesc md = s.maps[aux & 0x7fffu];
+            const unsigned long long off = md.poff + (unsigned long long)st.level * md.pw * md.ph +
+                                           (unsigned long long)((cxy >> 16) + kPad) * md.pw + ((cxy & 0xffffu) + kPad);
+            cb[c] = off | ((aux & kAuxNeg) ? (1ull << 63) : 0ull);
+          }
+          setup_bar();
+          for (uint32_t i0 = t; i0 < total; i0 += 8 * TS) {
+            uint32_t tx[8], gx[8], ii[8], jj[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const uint32_t i = i0 + (uint32_t)u * TS;
+              ii[u] = i;
+              if (i < total) {
+                const uint32_t c = i / nk;
+                jj[u] = i - c * nk;
+                const unsigned long long v = cb[c];
+                const int lin = (v >> 63) ? -w.lin[jj[u]] : w.lin[jj[u]];
+                const size_t off = (size_t)(v & 0x7fffffffffffffffull) + lin;
+                tx[u] = __ldg(s.plevels + off);
+                if (s.guided) gx[u] = __ldg(s.pguides + off);
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              if (ii[u] < total) {
+                const uint4 nr = w.nbr[jj[u]];
+                float nps = lut4(lc, __vabsdiffu4(nr.y, tx[u]), 0.0f);
+                if (s.guided) nps = lut4(lg, __vabsdiffu4(nr.z, gx[u]), nps);
+                term[ii[u]] = nps;
+              }
+            }
+          }
+        } else {
+          // bounds-checked gathers (far neighbours or guides of other sizes)
+          uint32_t c = (uint32_t)t / nk, j = (uint32_t)t - c * nk;
+          const uint32_t dc = (uint32_t)TS / nk, dj = (uint32_t)TS - dc * nk;
+          for (uint32_t i = t; i < total; i += TS) {
+            const uint32_t cxy = w.cxy[c], aux = w.caux[c];
+            const uint32_t map = aux & 0x7fffu;
+            const int sg = (aux & kAuxNeg) ? -1 : 1;
+            const MapDesc md = s.maps[map];
+            const uint4 nr = w.nbr[j];
+            const int qx = (int)(cxy & 0xffffu) + sg * off_dx((int32_t)nr.x);
+            const int qy = (int)(cxy >> 16) + sg * off_dy((int32_t)nr.x);
+            uint32_t tt = kOutside;
+            if ((unsigned)qx < md.w && (unsigned)qy < md.h)
+              tt = __ldg(&s.levels[md.off + (size_t)st.level * md.w * md.h + (size_t)qy * md.w + qx]);
+            float nps = lut4(lc, __vabsdiffu4(nr.y, tt), 0.0f);
+            if (s.guided) {
+              const GuideDesc gd = s.gdesc[map];
+              uint32_t gt = kOutside;
+              if ((unsigned)qx < gd.w && (unsigned)qy < gd.h)
+                gt = __ldg(&s.guides[gd.off + (size_t)st.level * gd.w * gd.h + (size_t)qy * gd.w + qx]);
+              nps = lut4(lg, __vabsdiffu4(nr.z, gt), nps);
+            }
+            term[i] = nps;
+            c += dc;
+            j += dj;
+            if (j >= nk) {
+              j -= nk;
+              ++c;
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();  // the mean, the records, the candidates and the LUT sums
+    const uint32_t ncoh = sh_ncoh, nc = ncoh + s.m;
+    if (sh_flags & 2) {
+      if (tid == 0) write_bad_result(s, st, b, local, pixel);
+      __syncthreads();
+      continue;
+    }
+    // the weights: into the records (for the sequential form) and, as
+    // floats, into w.term
+    {
+      const double avg = sh_mean;
+      bool nan_w = false;
+      for (uint32_t j = tid; j < nk; j += T) {
+        const float wv = neighbour_weight(sh.dist[j], avg, tab, tab_ff);
+        nan_w |= (wv != wv);
+        w.nbr[j].w = __float_as_uint(wv);
+        w.term[j] = wv;
+      }
+      if (nan_w) atomicOr(&sh_flags, 1);
+    }
+    __syncthreads();
+    float best_s = FLT_MAX;
+    uint32_t best_i = 0;
+    if (!st.slow_lut && !(sh_flags & 1)) {
+      float my_s = FLT_MAX;
+      uint32_t my_i = 0xffffffffu;
+      for (uint32_t cc = tid; cc < nc; cc += T) {
+        float sc = 0.0f;
+        const float *tc = term + (size_t)cc * nk;
+        for (uint32_t jj = 0; jj < nk; ++jj) sc = __fadd_rn(sc, __fmul_rn(tc[jj], w.term[jj]));
+        if (sc < my_s) {  // first strict minimum among this thread's candidates
+          my_s = sc;
+          my_i = cc;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, my_s, o);
+        const uint32_t oi = __shfl_xor_sync(0xffffffffu, my_i, o);
+        if (ov < my_s || (ov == my_s && oi < my_i)) {
+          my_s = ov;
+          my_i = oi;
+        }
+      }
+      if (lane == 0) {
+        red_s[warp] = my_s;
+        red_i[warp] = my_i;
+      }
+      __syncthreads();
+      best_s = red_s[0];
+      best_i = red_i[0];
+      for (int i = 1; i < NW; ++i) {
+        if (red_s[i] < best_s || (red_s[i] == best_s && red_i[i] < best_i)) {
+          best_s = red_s[i];
+          best_i = red_i[i];
+        }
+      }
+      if (best_i == 0xffffffffu) {  // no score below f32::MAX: the reference keeps candidate 0
+        best_s = FLT_MAX;
+        best_i = 0;
+      }
+    } else if (tid == 0) {
+      sequential_best(s, st, w, lc, lg, nk, nc, best_s, best_i);
+    }
+    if (tid == 0) write_result(s, st, w, b, local, pixel, px, py, is_new, nc, best_s, best_i);
+    __syncthreads();
+  }
 }
 
 __global__ void k_commit(SessionDev s, StageDev st, BatchDev b) {
