@@ -18,6 +18,9 @@ Session::run() over one session.
   batched  64 sessions of the batched mix (uneven sizes, k and m from
          {8, 20, 50}, a quarter guided), one after another on the plain
          path and together through the batched form: aggregate Mpx/s
+  tuning   the launch-shape thresholds the autotuner picked on the workload
+         before any timing (ts_autotune_session); the batched and served
+         forms use those ts_autotune_batch picked on the batched mix
   served   a Poisson request stream from the batched mix (70%) and 512^2
          inpainting requests (30%) through the served form and, for
          comparison, through the plain path one request at a time:
@@ -131,6 +134,12 @@ class L2Flush:
             self.torch.cuda.synchronize()
 
 
+def _tuning_dict(t):
+    return {"team_max_items": t.team_max_items, "team_full_max_items": t.team_full_max_items,
+            "walk_window_max_items": t.walk_window_max_items, "trials": t.trials,
+            "tuned_ms": t.gpu_ms, "default_ms": t.default_gpu_ms}
+
+
 def _pct(v, q):
     import numpy as np
 
@@ -150,9 +159,13 @@ def measure_batched(ts, wl, n=64):
     for s in sess:
         gpu += s.run().stats()["gpu_ms"]
     plain_wall = time.perf_counter() - t0
+    del sess
+    # the batched form's team thresholds, tuned on this mix after the plain
+    # runs (which keep the defaults) and before the timed batched runs
+    tuning = ts.autotune_batch(lambda: [ts.builder_from_spec(s).build() for s in specs], repeats=2)
     best = None
     for _ in range(2):
-        b = ts.Batch()
+        b = ts.Batch(tuning=tuning)
         for s in specs:
             b.add(ts.builder_from_spec(s).build())
         t1 = time.perf_counter()
@@ -167,10 +180,10 @@ def measure_batched(ts, wl, n=64):
             "batched": {"mpx_s": px / (st["gpu_ms"] / 1e3) / 1e6, "wall_mpx_s": px / wall / 1e6,
                         "gpu_ms": st["gpu_ms"], "steps": st["steps"], "launches": st["launches"],
                         "plan_ms": st["plan_ms"]},
-            "cost_evals_per_s": st["cost_evals"] / (st["gpu_ms"] / 1e3)}
+            "cost_evals_per_s": st["cost_evals"] / (st["gpu_ms"] / 1e3), "tuning": _tuning_dict(tuning)}, tuning
 
 
-def serve_stream(ts, reqs, served=True, max_active=64):
+def serve_stream(ts, reqs, served=True, max_active=64, tuning=None):
     """A request stream [(arrival_s, spec)]: sessions are built at arrival on
     a client thread; latency runs from the arrival to the result on the
     host.  served=False: the plain path, one request at a time, FIFO."""
@@ -179,7 +192,7 @@ def serve_stream(ts, reqs, served=True, max_active=64):
     px = [0] * n
     t_start = time.perf_counter() + 0.05
     if served:
-        srv = ts.Server(max_active=max_active)
+        srv = ts.Server(max_active=max_active, tuning=tuning)
         tickets = [None] * n
         ready = [threading.Event() for _ in range(n)]
         sub_py = [0.0] * n
@@ -223,15 +236,15 @@ def serve_stream(ts, reqs, served=True, max_active=64):
     return out
 
 
-def measure_served(ts, wl, lams=(50, 200), n=64):
+def measure_served(ts, wl, lams=(50, 200), n=64, tuning=None):
     """Config 4: the Poisson stream through the served form and through the
     plain path, at each arrival rate."""
     warm = wl.config4_requests(6, 1000.0, seed=99)
-    serve_stream(ts, warm, True)
+    serve_stream(ts, warm, True, tuning=tuning)
     rows = []
     for lam in lams:
         reqs = wl.config4_requests(n, float(lam))
-        rows.append({"lambda_req_s": lam, "served": serve_stream(ts, reqs, True),
+        rows.append({"lambda_req_s": lam, "served": serve_stream(ts, reqs, True, tuning=tuning),
                      "plain": serve_stream(ts, reqs, False)})
     return {"workload": "served_mix", "mix": "70% batched mix, 30% 512^2 inpainting", "rates": rows}
 
@@ -297,7 +310,7 @@ def main():
             b.run()
             print(json.dumps(b.stats()))
             return
-        print(json.dumps({"metric": "aggregate output Mpx/s (batched form)", **measure_batched(ts, wl)}))
+        print(json.dumps({"metric": "aggregate output Mpx/s (batched form)", **measure_batched(ts, wl)[0]}))
         return
     if args.workload == "served":
         print(json.dumps({"metric": "request latency p50/p99 and aggregate Mpx/s (served form)",
@@ -309,10 +322,12 @@ def main():
         g = ts.builder_from_spec(spec).build().run()
         print(json.dumps(g.stats()))
         return
+    # --- launch-shape thresholds tuned on this workload (before any timing)
+    tuning = ts.autotune_session(lambda: ts.builder_from_spec(spec), repeats=3)
     # --- device-resident throughput: sessions built before the timed region
     for _ in range(args.warmup):
-        ts.builder_from_spec(spec).build().run()
-    sessions = [ts.builder_from_spec(spec).build() for _ in range(args.steps)]
+        ts.builder_from_spec(spec, tuning=tuning).build().run()
+    sessions = [ts.builder_from_spec(spec, tuning=tuning).build() for _ in range(args.steps)]
     flush = L2Flush()
     gpu_ms, evals, launches, walls = [], [], [], []
     with ClockSampler(0) as clk:
@@ -332,16 +347,16 @@ def main():
     e2e_t = []
     h2d = sum(e["image"].nbytes for e in spec["examples"])
     d2h = px * 4
-    for _ in range(max(1, min(args.steps, 5))):
+    for _ in range(max(1, min(args.steps, 10))):
         t1 = time.perf_counter()
-        g = ts.builder_from_spec(spec).build().run()
+        g = ts.builder_from_spec(spec, tuning=tuning).build().run()
         img = g.into_image()
         e2e_t.append(time.perf_counter() - t1)
     e2e = px / (sum(e2e_t) / len(e2e_t)) / 1e6
     peak, peak_kind = _peaks()
     # --- roofline of the dominant kernel: a separate pass with CUDA events
     # around every launch on the launching stream
-    prof = ts.builder_from_spec(spec, profile=True).build().run().stats()
+    prof = ts.builder_from_spec(spec, profile=True, tuning=tuning).build().run().stats()
     kern = prof["kernels"]
     top = max(kern, key=lambda n: kern[n]["ms"])
     res = kern["resolve"]
@@ -369,11 +384,12 @@ def main():
         "clocks": clk.summary(),
         "e2e": {"value": e2e, "unit": "Mpx/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": roofline,
+        "tuning": _tuning_dict(tuning),
         "cpu_baseline": None,
     }
     if not args.no_extra:
-        line["batched"] = measure_batched(ts, wl)
-        line["served"] = measure_served(ts, wl)
+        line["batched"], btun = measure_batched(ts, wl)
+        line["served"] = measure_served(ts, wl, tuning=btun)
     if not args.no_cpu_baseline and rank == 0:
         from oracle import oracle
 

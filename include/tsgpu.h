@@ -379,6 +379,45 @@ int ts_server_wait(ts_server *s, uint64_t ticket, ts_generated **out, ts_request
 int ts_server_done(ts_server *s, uint64_t ticket);
 void ts_server_stats_get(ts_server *s, ts_server_stats *out);
 
+/* ---- Autotuner (no counterpart in the reference) ------------------------
+ * Each batch step's launch shape follows its item count: one warp per item
+ * for large steps (throughput), one CTA of 128 threads per item with early
+ * exit, or of 256 threads scoring every candidate, for small ones
+ * (latency); on the plain path, the k-NN walk of a small step may also
+ * build a bitmap window in shared memory.  The thresholds between these
+ * never change a result, only the speed, which depends on the GPU, the
+ * sizes, k and m.  The tuner runs the caller's own workload under candidate
+ * thresholds, one threshold at a time starting from the defaults, and keeps
+ * a candidate only when its median device time over `repeats` runs beats
+ * the best so far by more than 1%. */
+typedef struct ts_tuning {
+  uint32_t team_max_items;         /* a CTA per item in steps of at most this many items */
+  uint32_t team_full_max_items;    /* ... scoring every candidate up to this many */
+  uint32_t walk_window_max_items;  /* plain path: walk steps up to this many items may build a window */
+  uint32_t trials;                 /* runs the tuner made (0 for ts_tuning_default) */
+  double gpu_ms;                   /* median device time of the workload with this setting */
+  double default_gpu_ms;           /* the same with the defaults */
+} ts_tuning;
+/* The defaults: 2048, 256 and 4096 items. */
+void ts_tuning_default(ts_tuning *out);
+/* A fresh, configured builder for one run of the workload on each call; the
+ * tuner builds it, runs it and frees it.  NULL ends the tuning with
+ * TS_ERR_STATE. */
+typedef ts_builder *(*ts_builder_factory)(void *user);
+/* Tunes the plain path on the workload `make` describes. */
+int ts_autotune_session(ts_builder_factory make, void *user, uint32_t repeats, ts_tuning *out);
+/* Adds the sessions of one run of the workload to the (empty) batch; a
+ * nonzero return ends the tuning with that status. */
+typedef int (*ts_batch_filler)(ts_batch *b, void *user);
+/* Tunes the batched form (the two team thresholds) on batches of `device`
+ * filled by `fill`. */
+int ts_autotune_batch(int32_t device, ts_batch_filler fill, void *user, uint32_t repeats, ts_tuning *out);
+/* Apply a setting: to a builder's session (all three thresholds), to a
+ * batch or a server (the team thresholds over a step's summed items). */
+int ts_builder_tuning(ts_builder *b, const ts_tuning *t);
+int ts_batch_tuning(ts_batch *b, const ts_tuning *t);
+int ts_server_tuning(ts_server *s, const ts_tuning *t);
+
 /* ---- GeneratedImage (lib.rs:378-455) ------------------------------------- */
 
 void ts_generated_dims(const ts_generated *g, uint32_t *width, uint32_t *height);

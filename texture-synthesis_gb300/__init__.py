@@ -114,7 +114,29 @@ class _LaunchRecord(C.Structure):
     _fields_ = [("kind", C.c_int32), ("stage", C.c_int32), ("batch_items", C.c_uint32), ("ms", C.c_float)]
 
 
+class Tuning(C.Structure):
+    """Launch-shape thresholds (ts_tuning): a CTA per item in steps of at
+    most team_max_items items (every candidate scored up to
+    team_full_max_items), and, on the plain path, a walk bitmap window in
+    steps of at most walk_window_max_items.  Results never depend on them."""
+
+    _fields_ = [("team_max_items", C.c_uint32), ("team_full_max_items", C.c_uint32),
+                ("walk_window_max_items", C.c_uint32), ("trials", C.c_uint32), ("gpu_ms", C.c_double),
+                ("default_gpu_ms", C.c_double)]
+
+    @staticmethod
+    def default():
+        t = Tuning()
+        lib().ts_tuning_default(C.byref(t))
+        return t
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 _PROGRESS_FN = C.CFUNCTYPE(None, C.POINTER(_Progress), C.c_void_p)
+_BUILDER_FACTORY = C.CFUNCTYPE(C.c_void_p, C.c_void_p)
+_BATCH_FILLER = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p)
 
 # every function tsgpu.h declares: name -> (restype, argtypes)
 SIGNATURES = {
@@ -191,6 +213,12 @@ SIGNATURES = {
     "ts_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p), C.POINTER(_RequestTimes)]),
     "ts_server_done": (C.c_int, [C.c_void_p, C.c_uint64]),
     "ts_server_stats_get": (None, [C.c_void_p, C.POINTER(_ServerStats)]),
+    "ts_tuning_default": (None, [C.POINTER(Tuning)]),
+    "ts_autotune_session": (C.c_int, [_BUILDER_FACTORY, C.c_void_p, C.c_uint32, C.POINTER(Tuning)]),
+    "ts_autotune_batch": (C.c_int, [C.c_int32, _BATCH_FILLER, C.c_void_p, C.c_uint32, C.POINTER(Tuning)]),
+    "ts_builder_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    "ts_batch_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    "ts_server_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
 }
 
 
@@ -424,6 +452,11 @@ class SessionBuilder:
         max_batch, one CTA per item with early exit; above, a warp per item."""
         return self._check(lib().ts_builder_resolve_team(self._h, int(max_batch), int(full_max_batch)))
 
+    def tuning(self, tuning):
+        """Launch-shape thresholds (a Tuning from autotune_session, or
+        Tuning.default()); the results do not depend on them."""
+        return self._check(lib().ts_builder_tuning(self._h, C.byref(tuning)))
+
     def profile_kernels(self, on=True):
         """Time every kernel launch with CUDA events (measurement runs)."""
         return self._check(lib().ts_builder_profile_kernels(self._h, 1 if on else 0))
@@ -543,12 +576,14 @@ class Batch:
     phase of each batch step carrying every session's step.  Each result is
     identical to Session.run on the same session."""
 
-    def __init__(self, device=0, graph=False, profile=False, plan_threads=0, team=None):
+    def __init__(self, device=0, graph=False, profile=False, plan_threads=0, team=None, tuning=None):
         self._h = lib().ts_batch_new(device)
         if not self._h:
             raise Error(13, "ts_batch_new")
         if team is not None:
             lib().ts_batch_resolve_team(self._h, team[0], team[1])
+        if tuning is not None:
+            lib().ts_batch_tuning(self._h, C.byref(tuning))
         if graph:
             lib().ts_batch_use_graph(self._h, 1)
         if profile:
@@ -596,12 +631,14 @@ class Server:
     (GeneratedImage, times) with host timestamps in ms (submit, admit,
     done).  Results equal Session.run on the same session."""
 
-    def __init__(self, device=0, hbm_budget=0, max_active=64, team=None):
+    def __init__(self, device=0, hbm_budget=0, max_active=64, team=None, tuning=None):
         self._h = lib().ts_server_new(device, int(hbm_budget), int(max_active))
         if not self._h:
             raise Error(10, "ts_server_new: the device cannot be used")
         if team is not None:
             lib().ts_server_resolve_team(self._h, team[0], team[1])
+        if tuning is not None:
+            lib().ts_server_tuning(self._h, C.byref(tuning))
 
     def close(self):
         """Waits for every submitted request, then stops the server."""
@@ -705,7 +742,7 @@ class CoordinateTransform:
 
 
 def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0, profile=False, team_max_batch=None,
-                      team_full_max_batch=256):
+                      team_full_max_batch=256, tuning=None):
     """A SessionBuilder for a workload spec dict (see workloads.py)."""
     p = spec["params"]
     b = Session.builder()
@@ -739,7 +776,61 @@ def builder_from_spec(spec, batch_divisor=8, max_batch=0, device=0, profile=Fals
         b.profile_kernels(True)
     if team_max_batch is not None:
         b.resolve_team(team_max_batch, team_full_max_batch)
+    if tuning is not None:
+        b.tuning(tuning)
     return b
+
+
+def autotune_session(make_builder, repeats=3):
+    """The autotuner on the plain path (ts_autotune_session).  make_builder()
+    returns a configured SessionBuilder for one run of the workload; it is
+    called once per trial run.  Returns the fastest Tuning found."""
+    errors = []
+
+    @_BUILDER_FACTORY
+    def factory(_user):
+        try:
+            sb = make_builder()
+            h, sb._h = sb._h, None  # the tuner builds and frees it
+            return h
+        except Exception as e:  # reported after the tuner returns
+            errors.append(e)
+            return None
+
+    t = Tuning()
+    rc = lib().ts_autotune_session(factory, None, int(repeats), C.byref(t))
+    if errors:
+        raise errors[0]
+    if rc:
+        raise Error(rc, "ts_autotune_session")
+    return t
+
+
+def autotune_batch(make_sessions, device=0, repeats=2):
+    """The autotuner on the batched form (ts_autotune_batch): make_sessions()
+    returns the built Sessions of one batched run; it is called once per
+    trial run.  Returns the fastest Tuning found (its team thresholds)."""
+    errors = []
+
+    @_BATCH_FILLER
+    def fill(bh, _user):
+        try:
+            for s in make_sessions():
+                rc = lib().ts_batch_add(bh, s._h)
+                if rc:
+                    return rc
+            return 0
+        except Exception as e:
+            errors.append(e)
+            return 11
+
+    t = Tuning()
+    rc = lib().ts_autotune_batch(int(device), fill, None, int(repeats), C.byref(t))
+    if errors:
+        raise errors[0]
+    if rc:
+        raise Error(rc, "ts_autotune_batch")
+    return t
 
 
 def run_spec(spec, batch_divisor=8, max_batch=0, device=0, team_max_batch=None, team_full_max_batch=256):

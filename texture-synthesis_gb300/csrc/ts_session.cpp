@@ -48,7 +48,8 @@ constexpr int kDistTabRadius = 64;  // offsets the weight tables cover
 static_assert(kDistTabRadius >= kKnnTabRadius, "the walk's distances come from the tables alone");
 constexpr uint64_t kRcandBudget = 64ull << 20;  // random-candidate entries held at once
 // Walk steps of at most this many items are latency-bound: their sparse items
-// build a bitmap window instead of more rounds of bitmap loads.
+// build a bitmap window instead of more rounds of bitmap loads (the default;
+// ts_builder_tuning sets it per session).
 constexpr uint32_t kWalkWindowItems = 4096;
 // Runs whose random candidates for every stage fit this many entries make
 // them all ahead, on a side stream, while the first stages run.
@@ -98,6 +99,7 @@ struct Params {
   bool profile = false;
   uint32_t team_max_batch = 2048;
   uint32_t team_full_max_batch = 256;
+  uint32_t walk_window_max = kWalkWindowItems;
 };
 
 std::string fmt_float(float v) {
@@ -878,6 +880,14 @@ int ts_builder_resolve_team(ts_builder *b, uint32_t team_max_batch, uint32_t ful
   BUILDER_GUARD(b);
   b->prm.team_max_batch = team_max_batch;
   b->prm.team_full_max_batch = full_max_batch;
+  return TS_OK;
+}
+int ts_builder_tuning(ts_builder *b, const ts_tuning *t) {
+  BUILDER_GUARD(b);
+  if (!t) return TS_ERR_NULL;
+  b->prm.team_max_batch = t->team_max_items;
+  b->prm.team_full_max_batch = t->team_full_max_items;
+  b->prm.walk_window_max = t->walk_window_max_items;
   return TS_OK;
 }
 int ts_builder_profile_kernels(ts_builder *b, int32_t on) {
@@ -1774,7 +1784,7 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
         stp.n = bp.i1 - bp.i0;
         stp.exhaustive = bp.exhaustive;
         bd.grid_first = bp.grid_first ? 1 : 0;
-        bd.walk_window = (bp.i1 - bp.i0) <= kWalkWindowItems ? 1 : 0;
+        bd.walk_window = (bp.i1 - bp.i0) <= p.walk_window_max ? 1 : 0;
         // a batch of new items only: none of them is in the tree, so no item
         // reads another's pixel, state or bit, and each commits as it resolves
         bd.fused_commit = bp.i0 >= sp.redo ? 1 : 0;
@@ -2225,6 +2235,12 @@ int ts_batch_resolve_team(ts_batch *b, uint32_t team_max_items, uint32_t full_ma
   if (!b) return TS_ERR_NULL;
   b->team_max_items = team_max_items;
   b->team_full_max_items = full_max_items;
+  return TS_OK;
+}
+int ts_batch_tuning(ts_batch *b, const ts_tuning *t) {
+  if (!b || !t) return TS_ERR_NULL;
+  b->team_max_items = t->team_max_items;
+  b->team_full_max_items = t->team_full_max_items;
   return TS_OK;
 }
 int ts_batch_plan_threads(ts_batch *b, uint32_t n) {
@@ -3194,6 +3210,10 @@ int ts_server_resolve_team(ts_server *S, uint32_t team_max_items, uint32_t full_
   S->team_max_items = team_max_items;
   S->team_full_max_items = full_max_items;
   return TS_OK;
+}
+int ts_server_tuning(ts_server *S, const ts_tuning *t) {
+  if (!t) return TS_ERR_NULL;
+  return ts_server_resolve_team(S, t->team_max_items, t->team_full_max_items);
 }
 
 int ts_server_submit(ts_server *S, ts_session *s, uint64_t *ticket) {
