@@ -44,6 +44,14 @@ sys.path.insert(0, ROOT)
 PKG = "texture-synthesis_gb300"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
+# resolve family (k_resolve_lean, k_resolve_team, k_step_team_full) on this
+# workload: 1038.7 MB over the 131 resolve launches of one run, from
+#   ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum
+#       --clock-control none -k regex:"k_resolve|k_step_team" --csv python bench.py --once
+# (one pass; ncu flushes the caches before each launch, so this is a
+# cold-cache upper bound of the live traffic).
+RESOLVE_DRAM_BYTES_PER_LAUNCH = 1038.67e6 / 131
 
 
 def _peaks():
@@ -365,7 +373,8 @@ def main():
     alg_bytes = prof["cost_evals"] * per_eval  # example texels every candidate-cost evaluation reads
     achieved = alg_bytes / (res["ms"] / 1e3) / 1e9
     roofline = {"kernel": "k_resolve", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": RESOLVE_DRAM_BYTES_PER_LAUNCH,
+                "traffic_source": "ncu capture of this workload, cold caches, bytes per resolve launch",
                 "alg_bytes_per_launch": alg_bytes / max(1, res["launches"]),
                 "avg_launch_ms": res["ms"] / max(1, res["launches"]), "launches": res["launches"],
                 "kernel_share": {n: kern[n]["ms"] / max(1e-9, sum(v["ms"] for v in kern.values())) for n in kern},
