@@ -322,25 +322,20 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
 // them by (d2, y, x) and emit the first k.
 // ---------------------------------------------------------------------------
 // The mean of a neighbour distance list on one thread (ms.rs:417-423, as
-// k_mean_staged computes it): the four adds of a distance in integer
-// arithmetic while the sum stays in its binade, else four f64 adds (64
-// cycles each), then / (4n).
+// k_mean_staged computes it): the 4n-long chain of f64 adds in order, then
+// / (4n).  Where one thread runs it alone this is shorter than the integer
+// form of the four adds (ts_add4_fast): 14.1k against 16.8k cycles for
+// n = 50 on GB300.
 __device__ __forceinline__ double mean_chain(const double *d, uint32_t n) {
-  uint64_t acc = 0;
+  double sum = 0.0;
   for (uint32_t i = 0; i < n; ++i) {
     const double v = d[i];
-    uint64_t nx;
-    if (!ts_add4_fast(acc, dbl_bits(v), nx)) {
-      double a = bits_dbl(acc);
-      a = __dadd_rn(a, v);
-      a = __dadd_rn(a, v);
-      a = __dadd_rn(a, v);
-      a = __dadd_rn(a, v);
-      nx = dbl_bits(a);
-    }
-    acc = nx;
+    sum = __dadd_rn(sum, v);
+    sum = __dadd_rn(sum, v);
+    sum = __dadd_rn(sum, v);
+    sum = __dadd_rn(sum, v);
   }
-  return __ddiv_rn(bits_dbl(acc), (double)(n * 4u));
+  return __ddiv_rn(sum, (double)(n * 4u));
 }
 
 struct ExhShared {
@@ -2196,14 +2191,26 @@ __global__ void __launch_bounds__(kTeamFullThreads) k_step_team_full(SessionDev 
       }
     } else {
       const int t = tid - kWarp;
-      for (int i = t; i < 512; i += TS) lc[i] = st.lut[i];
-      for (int i = t; i < 64; i += TS) tab[i] = g_exp2_64[i];
-      for (int i = t; i < 128; i += TS) tab_ff[i] = g_exp2_ff[i];
+      // the LUTs, the exp tables and the first random candidates go into
+      // registers first, so that their loads are in flight together with
+      // the neighbour records' loads; they reach shared memory after the
+      // records (the records loop's barriers order the flags' reset before
+      // their first update)
+      constexpr int kLutPer = (512 + TS - 1) / TS;
+      float lreg[kLutPer];
+#pragma unroll
+      for (int u = 0; u < kLutPer; ++u) {
+        const int i = t + u * TS;
+        lreg[u] = i < 512 ? st.lut[i] : 0.0f;
+      }
+      const double treg = t < 64 ? g_exp2_64[t] : 0.0;
+      const float freg = t < 128 ? g_exp2_ff[t] : 0.0f;
+      const uint2 *rc = st.rcand + (size_t)item * s.m;
+      const uint2 rv0 = (uint32_t)t < s.m ? rc[t] : make_uint2(0u, 0u);
       if (t == 0) {
         sh_flags = 0;
         sh_maxoff = 0;
       }
-      setup_bar();
       // neighbour records and coherence candidates, compacted in order
       bool bad_map = false;
       int maxoff = 0;
@@ -2230,11 +2237,17 @@ __global__ void __launch_bounds__(kTeamFullThreads) k_step_team_full(SessionDev 
         ncoh += total;
         setup_bar();
       }
+#pragma unroll
+      for (int u = 0; u < kLutPer; ++u) {
+        const int i = t + u * TS;
+        if (i < 512) lc[i] = lreg[u];
+      }
+      if (t < 64) tab[t] = treg;
+      if (t < 128) tab_ff[t] = freg;
       if (bad_map) atomicOr(&sh_flags, 2);
       if (maxoff) atomicMax(&sh_maxoff, maxoff);
-      const uint2 *rc = st.rcand + (size_t)item * s.m;
       for (uint32_t q = t; q < s.m; q += TS) {
-        const uint2 v = rc[q];
+        const uint2 v = q == (uint32_t)t ? rv0 : rc[q];
         w.cxy[ncoh + q] = v.x;
         w.caux[ncoh + q] = v.y | kAuxNeg | (q << 16);
       }
@@ -2253,10 +2266,11 @@ __global__ void __launch_bounds__(kTeamFullThreads) k_step_team_full(SessionDev 
             cb[c] = off | ((aux & kAuxNeg) ? (1ull << 63) : 0ull);
           }
           setup_bar();
-          for (uint32_t i0 = t; i0 < total; i0 += 8 * TS) {
-            uint32_t tx[8], gx[8], ii[8], jj[8];
+          constexpr int kRound = 16;  // gathers in flight per thread
+          for (uint32_t i0 = t; i0 < total; i0 += kRound * TS) {
+            uint32_t tx[kRound], gx[kRound], ii[kRound], jj[kRound];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
+            for (int u = 0; u < kRound; ++u) {
               const uint32_t i = i0 + (uint32_t)u * TS;
               ii[u] = i;
               if (i < total) {
@@ -2270,7 +2284,7 @@ __global__ void __launch_bounds__(kTeamFullThreads) k_step_team_full(SessionDev 
               }
             }
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
+            for (int u = 0; u < kRound; ++u) {
               if (ii[u] < total) {
                 const uint4 nr = w.nbr[jj[u]];
                 float nps = lut4(lc, __vabsdiffu4(nr.y, tx[u]), 0.0f);
