@@ -71,3 +71,26 @@ def test_setting_applies_to_a_builder(ts):
     t.team_max_items, t.team_full_max_items, t.walk_window_max_items = 0, 0, 0
     b = ts.Session.builder().add_example(ts.Example(np.zeros((8, 8, 4), np.uint8)))
     assert b.tuning(t) is b
+
+
+def test_build_failure_stops_the_tuner(ts, wl):
+    """Without a usable device the first trial's build fails; the tuner
+    returns that status after one factory call."""
+    import os
+
+    pytest.importorskip("torch")
+    import torch
+
+    if torch.cuda.is_available() or os.path.exists("/dev/nvidia0"):
+        pytest.skip("a device is present")
+    calls = []
+    spec = wl.config0(out=16, ex=8)
+
+    def make():
+        calls.append(1)
+        return ts.builder_from_spec(spec)
+
+    with pytest.raises(ts.Error) as e:
+        ts.autotune_session(make, repeats=1)
+    assert e.value.status == 10  # TS_ERR_CUDA
+    assert len(calls) == 1
