@@ -277,9 +277,13 @@ TS_HD float bits_flt(uint32_t u) {
 // ---------------------------------------------------------------------------
 // IEEE round-to-nearest-even addition of non-negative doubles in integer
 // arithmetic, for the in-order sum of the 4x-duplicated distance list
-// (ms.rs:417-421).  GB300's f64 adds have long latency; this dependent chain
-// of 4k additions runs on the integer pipes instead.  Operands are the bit
-// patterns of finite doubles >= 0 (zero or normal).
+// (ms.rs:417-421), and integer division of that sum.  The kernels sum with
+// hardware f64 adds: as one thread's dependent chain these integer steps
+// measured slower on GB300 (16.8k against 14.1k cycles at k = 50).  They
+// stay as the bit-exact statement of the binade rule (within one binade
+// every add rounds the addend to the sum's ulp) that an exact parallel sum
+// builds on, and the CPU and GPU tests hold them to hardware f64.
+// Operands are the bit patterns of finite doubles >= 0 (zero or normal).
 // ---------------------------------------------------------------------------
 constexpr uint64_t kFrac52 = (1ULL << 52) - 1;
 
