@@ -27,3 +27,23 @@ def test_tuning_dict_keys():
     d = bench._tuning_dict(T())
     assert d == {"team_max_items": 1, "team_full_max_items": 2, "walk_window_max_items": 3, "trials": 4,
                  "tuned_ms": 5.0, "default_ms": 6.0}
+
+
+def test_reference_arm_line():
+    """bench.py --impl reference prints one JSON line with the contract's
+    keys (the oracle port on the host cores; no GPU needed)."""
+    import json
+    import subprocess
+
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "1"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip().startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    for key in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["impl"] == "reference" and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
