@@ -39,6 +39,13 @@ extern "C" {
  * TS_ERR_MAPS_COUNT_MISMATCH mirror texture_synthesis::Error
  * (lib/src/errors.rs:37-57); TS_ERR_IMAGE stands for Error::Image (a buffer
  * whose size does not match its dimensions). */
+/* A random candidate (ms.rs:549-599) draws (x, y) pairs until one lies in
+ * its example's sample mask.  The reference draws without end; here the
+ * GPU path and the CPU oracle both give up after this many pairs and report
+ * TS_ERR_NO_VALID_SAMPLE.  A mask whose valid fraction is f runs out with
+ * probability (1 - f)^TS_MAX_SAMPLE_DRAWS per candidate. */
+#define TS_MAX_SAMPLE_DRAWS (1u << 22)
+
 typedef enum ts_status {
   TS_OK = 0,
   TS_ERR_INVALID_RANGE = 1,
@@ -49,8 +56,10 @@ typedef enum ts_status {
   TS_ERR_IMAGE = 6,
   /* A feature of the reference that this library does not provide. */
   TS_ERR_UNSUPPORTED = 7,
-  /* A sample mask with no usable texel: the reference loops forever
-   * (ms.rs:562-574); this library refuses it. */
+  /* A sample mask with no usable texel, or one so sparse that
+   * TS_MAX_SAMPLE_DRAWS draws of a random candidate all miss it: the
+   * reference keeps drawing (ms.rs:562-574), forever when nothing is valid;
+   * this library refuses it. */
   TS_ERR_NO_VALID_SAMPLE = 8,
   /* A map id beyond the non-ignored example list, where the reference
    * panics on an out-of-bounds index. */
@@ -178,8 +187,11 @@ int ts_guide_map(const uint8_t *rgba, uint32_t width, uint32_t height, const uin
  * bytes) are device buffers of the current device, owned by the caller;
  * they must not overlap.  The work is enqueued on `stream` (a cudaStream_t;
  * NULL is the legacy default stream) and the call returns without waiting
- * for it, so d_out is ready once the stream reaches that point.  No buffer
- * needs to start at zero.
+ * for it, so d_out is ready once the stream reaches that point.  It
+ * enqueues only kernels, device-to-device copies and memsets: the filter
+ * taps travel inside kernel parameters, so no copy from host memory makes
+ * the call wait for earlier work on the stream.  No buffer needs to start
+ * at zero.
  *
  * Intermediate images and filter taps live in one fixed device array of
  * the library (9.4 MiB, held on every device the library runs on until
@@ -190,7 +202,11 @@ int ts_guide_map(const uint8_t *rgba, uint32_t width, uint32_t height, const uin
  * device must not overlap on the device: issue them on one stream or order
  * them with events, or they race on the array and give wrong images.
  * The first call on a device looks up the array's device address (a
- * one-time set-up per device); make it before any stream capture.
+ * one-time set-up per device); make it before any stream capture.  That
+ * address is kept for the life of the process, so resetting the device
+ * (cudaDeviceReset) between calls is not supported.  If a CUDA error is
+ * already pending in the calling thread when the call begins, the call
+ * enqueues nothing, returns TS_ERR_CUDA and leaves that error in place.
  * Returns TS_OK, TS_ERR_NULL, TS_ERR_IMAGE (zero side), TS_ERR_LIMIT or
  * TS_ERR_CUDA. */
 #define TS_NOALLOC_MAX_PIXELS (1024u * 1024u)
@@ -198,6 +214,27 @@ int ts_guide_map(const uint8_t *rgba, uint32_t width, uint32_t height, const uin
 #define TS_NOALLOC_MAX_LEVELS 16u
 int ts_image_pyramid_noalloc(const uint8_t *d_rgba, uint32_t width, uint32_t height, uint32_t levels, uint8_t *d_out,
                              void *stream);
+
+/* ts_measure_gather_peak: no counterpart in the reference; measurement only.
+ * The rate at which the GPU serves the cost loop's loads (better_match,
+ * ms.rs:1225-1288 reads k example texels per candidate), measured with
+ * kernels that do nothing else, at full occupancy, on a table of
+ * width x height 32-bit texels (plus a 12-texel border) that the call
+ * allocates, fills and frees:
+ *   patch_gbs   a pseudo-random centre per thread and the k offsets nearest
+ *               the origin around it, four loads in flight (the cost loop's
+ *               access shape);
+ *   random_gbs  independent pseudo-random texels, four in flight.
+ * Both count 4 bytes per load; the best of `reps` timed launches (CUDA
+ * events) after one warm-up.  k <= 256, sides <= 16384. */
+typedef struct ts_gather_peak {
+  double patch_gbs, random_gbs;
+  double table_bytes;
+  uint32_t threads;
+  float patch_ms, random_ms;
+} ts_gather_peak;
+int ts_measure_gather_peak(int32_t device, uint32_t width, uint32_t height, uint32_t k, int32_t reps,
+                           ts_gather_peak *out);
 
 /* ---- SessionBuilder (session.rs:69-448) ---------------------------------- */
 

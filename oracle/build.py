@@ -15,13 +15,15 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libtsoracle.so")
 SRC = os.path.join(HERE, "ms_oracle.c")
+HDR = os.path.join(os.path.dirname(HERE), "include", "tsgpu.h")  # TS_MAX_SAMPLE_DRAWS
 
 CFLAGS = ["-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-pthread"]
 
 
 def build(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    newest = max(os.path.getmtime(SRC), os.path.getmtime(HDR))
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
         return LIB
     tmp = LIB + ".tmp%d" % os.getpid()
     cmd = ["gcc", *CFLAGS, "-o", tmp, SRC, "-lm"]

@@ -54,6 +54,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "../include/tsgpu.h" /* TS_MAX_SAMPLE_DRAWS, the one bound shared with the GPU path */
+
 #define TSO_OK 0
 #define TSO_ERR_ARG 1
 #define TSO_ERR_NO_VALID_SAMPLE 2
@@ -213,6 +215,22 @@ static double tso_exp(double x) {
   return ldexp(exp2_64[ki & 63] * p, ki >> 6);
 }
 double tso_exp_export(double x) { return tso_exp(x); }
+
+/* Audit of tso_exp against the C library's exp, which the reference calls
+ * (f64::exp, ms.rs:1198-1203): while on, every weight a run computes is
+ * also computed with exp(), and the inputs whose f32 weights differ are
+ * counted.  Test instrumentation; off by default. */
+static int g_exp_audit;
+static uint64_t g_exp_audit_n, g_exp_audit_diff;
+void tso_exp_audit(int on) {
+  g_exp_audit = on;
+  __atomic_store_n(&g_exp_audit_n, 0, __ATOMIC_SEQ_CST);
+  __atomic_store_n(&g_exp_audit_diff, 0, __ATOMIC_SEQ_CST);
+}
+void tso_exp_audit_counts(uint64_t *n, uint64_t *diff) {
+  *n = __atomic_load_n(&g_exp_audit_n, __ATOMIC_SEQ_CST);
+  *diff = __atomic_load_n(&g_exp_audit_diff, __ATOMIC_SEQ_CST);
+}
 
 /* ------------------------------------------------------------------------ */
 /* image 0.23.12 imageops::resize restated (img_pyramid.rs:27-32 calls it     */
@@ -750,6 +768,10 @@ static void resolve_item(const gen_t *g, uint32_t pixel, int is_new, uint64_t lo
   for (size_t j = 0; j < nk; j++) {
     double d = s->dist[j] / avg;
     s->wt[j] = (float)tso_exp(-1.0 * d);
+    if (g_exp_audit) {
+      __atomic_fetch_add(&g_exp_audit_n, 1, __ATOMIC_RELAXED);
+      if ((float)exp(-1.0 * d) != s->wt[j]) __atomic_fetch_add(&g_exp_audit_diff, 1, __ATOMIC_RELAXED);
+    }
   }
   /* find_candidates (ms.rs:478-602) */
   size_t nc = 0;
@@ -784,7 +806,9 @@ static void resolve_item(const gen_t *g, uint32_t pixel, int is_new, uint64_t lo
       rx = (int32_t)gen_range_u32(&rng, w);
       ry = (int32_t)gen_range_u32(&rng, h);
       if (coord_valid(g, rx, ry, map)) break;
-      if (++tries > (1ULL << 26)) {
+      /* the reference draws without end; both sides stop after the same
+       * number of pairs (TS_MAX_SAMPLE_DRAWS, include/tsgpu.h) */
+      if (++tries >= TS_MAX_SAMPLE_DRAWS) {
         res->err = TSO_ERR_NO_VALID_SAMPLE;
         return;
       }

@@ -92,8 +92,39 @@ def lib():
         L.tso_knn.restype = C.c_size_t
         L.tso_knn.argtypes = [C.c_uint32, C.c_uint32, C.c_int, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
                               C.c_uint32, C.c_void_p]
+        L.tso_exp_audit.restype = None
+        L.tso_exp_audit.argtypes = [C.c_int]
+        L.tso_exp_audit_counts.restype = None
+        L.tso_exp_audit_counts.argtypes = [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         _lib = L
     return _lib
+
+
+def exp_audit(spec, **kw):
+    """Runs spec with the exp audit on: (weights computed, weights whose f32
+    value from the project exp differs from the C library's exp's)."""
+    L = lib()
+    L.tso_exp_audit(1)
+    try:
+        run(spec, **kw)
+        n, d = C.c_uint64(), C.c_uint64()
+        L.tso_exp_audit_counts(C.byref(n), C.byref(d))
+    finally:
+        L.tso_exp_audit(0)
+    return n.value, d.value
+
+
+class OracleError(RuntimeError):
+    """A run the oracle refused; status is its TSO_ERR_* code (2 = no valid
+    sample, 3 = index), numbered like the library's TS_ERR_NO_VALID_SAMPLE
+    and TS_ERR_INDEX through NO_VALID_SAMPLE and INDEX below."""
+
+    NO_VALID_SAMPLE = 2
+    INDEX = 3
+
+    def __init__(self, status):
+        super().__init__("oracle run failed with status %d" % status)
+        self.status = status
 
 
 FILTERS = {"nearest": 0, "triangle": 1, "catmullrom": 2, "gaussian": 3}
@@ -182,7 +213,7 @@ def run(spec, batch_divisor=8, max_batch=0, nthreads=1):
     rc = lib().tso_run(C.byref(prm), len(exs), arr, _ptr(tg), _ptr(ip), spec.get("inpaint_index", -1),
                        _ptr(out), _ptr(coord), _ptr(ids), _ptr(resolved), _ptr(rscore), C.byref(st))
     if rc:
-        raise RuntimeError("oracle run failed with status %d" % rc)
+        raise OracleError(rc)
     n = st.n_resolved
     return {
         "image": out, "coord": coord, "id": ids,

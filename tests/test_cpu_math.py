@@ -148,3 +148,68 @@ def test_fast_weight_matches_exact(host):
     # all distances zero: 0 / 0 is NaN in the reference; the fast path defers
     assert host.host_weight_ff(0.0, 0.0, C.byref(w)) == 0
     assert math.isnan(host.host_weight_exact(0.0, 0.0))
+
+
+def _chain_mean(ds):
+    """get_distances_to_k_neighs (ms.rs:405-425): the 4x-duplicated list
+    summed in order with f64 adds, divided by its length."""
+    s = 0.0
+    for d in ds:
+        s += d
+        s += d
+        s += d
+        s += d
+    return s / (4 * len(ds))
+
+
+def _dists(W, H, px, py, pts):
+    x2, y2 = px / W, py / H
+    out = []
+    for x, y in pts:
+        dx, dy = x / W - x2, y / H - y2
+        out.append(dx * dx + dy * dy)  # fma(dx, dx, dy*dy): both products are exact here
+    return out
+
+
+@pytest.mark.parametrize("W,H", [(512, 512), (256, 256), (1024, 64), (16384, 16384)])
+def test_power_of_two_distance_sums_are_exact(W, H):
+    """For power-of-two output sides the walk and the exhaustive k-NN sum a
+    distance list in warp order instead of the reference's in-order chain
+    (SessionDev::exact_sum): every distance is an integer multiple of
+    1/max(W,H)^2 and no partial sum needs more than 53 bits, so both orders
+    give the same double, and so the same mean."""
+    import random
+
+    rng = random.Random(W * 7 + H)
+    for _ in range(300):
+        k = rng.choice([1, 8, 20, 50, 256])
+        px, py = rng.randrange(W), rng.randrange(H)
+        # points anywhere in the plane the tree spans (tiling mirrors lie in [-W, 2W) x [-H, 2H))
+        pts = [(rng.randrange(-W, 2 * W), rng.randrange(-H, 2 * H)) for _ in range(k)]
+        ds = _dists(W, H, px, py, pts)
+        order = list(range(k))
+        rng.shuffle(order)
+        tree = 0.0
+        for i in order:
+            tree += ds[i]
+        assert 4.0 * tree / (4 * k) == _chain_mean(ds)
+
+
+def test_non_power_of_two_sums_can_round():
+    """The same shortcut would be wrong for other sizes: the distances are
+    then inexact doubles and the order of the adds changes the sum."""
+    import random
+
+    rng = random.Random(5)
+    W = H = 300
+    differ = 0
+    for _ in range(300):
+        k = 50
+        px, py = rng.randrange(W), rng.randrange(H)
+        pts = [(px + rng.randrange(-9, 10), py + rng.randrange(-9, 10)) for _ in range(k)]
+        ds = _dists(W, H, px, py, pts)
+        tree = 0.0
+        for d in reversed(ds):
+            tree += d
+        differ += 4.0 * tree / (4 * k) != _chain_mean(ds)
+    assert differ > 0

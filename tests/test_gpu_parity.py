@@ -4,8 +4,8 @@ The oracle (oracle/ms_oracle.c) restates the reference's ms.rs; both sides run
 the same batch-snapshot schedule, so the output image, the coordinate map,
 the id map, the resolved list and every first-resolve score (f32) must be
 identical, not merely close.  Sizes are small enough for the oracle to finish
-in seconds; the full-size workloads are covered by property tests in
-test_gpu_fullsize.py.
+in seconds; test_gpu_fullsize.py compares the full-size workloads the same
+way.
 """
 import numpy as np
 import pytest

@@ -244,3 +244,17 @@ def test_debug_maps_oracle_properties(oracle):
     assert tuple(unc[1, 1]) == (255, 0, 0, 255)     # NaN.min(1.0) = 1.0
     assert tuple(unc[2, 3]) == (255, 0, 0, 255)
     assert tuple(unc[0, 2]) == (0, 0, 0, 0)         # not resolved
+
+
+@pytest.mark.parametrize("name", ["config0", "config1", "config2"])
+def test_exp_matches_libm_on_every_weight(wl, oracle, name):
+    """The reference weights neighbours with (f32) f64::exp(-d / mean)
+    (ms.rs:1198-1203), the C library's exp.  The oracle and the GPU share a
+    project exp that is within 2 ulp of it; this counts, over every weight
+    the full-size workload computes, the inputs whose f32 weight differs
+    between the two.  None does (6.4 M, 25.8 M and 25.8 M weights)."""
+    import os
+
+    n, diff = oracle.exp_audit(getattr(wl, name)(), nthreads=os.cpu_count() or 1)
+    assert n > 6_000_000
+    assert diff == 0, "%d of %d weights differ from the C library's exp" % (diff, n)

@@ -138,6 +138,11 @@ _PROGRESS_FN = C.CFUNCTYPE(None, C.POINTER(_Progress), C.c_void_p)
 _BUILDER_FACTORY = C.CFUNCTYPE(C.c_void_p, C.c_void_p)
 _BATCH_FILLER = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p)
 
+class _GatherPeak(C.Structure):
+    _fields_ = [("patch_gbs", C.c_double), ("random_gbs", C.c_double), ("table_bytes", C.c_double),
+                ("threads", C.c_uint32), ("patch_ms", C.c_float), ("random_ms", C.c_float)]
+
+
 # every function tsgpu.h declares: name -> (restype, argtypes)
 SIGNATURES = {
     "ts_status_str": (C.c_char_p, [C.c_int]),
@@ -219,6 +224,8 @@ SIGNATURES = {
     "ts_builder_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "ts_batch_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "ts_server_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    "ts_measure_gather_peak": (C.c_int, [C.c_int32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32,
+                                         C.POINTER(_GatherPeak)]),
 }
 
 
@@ -259,6 +266,17 @@ def image_pyramid(image, levels, device=0):
     if rc:
         raise Error(rc, "ts_image_pyramid")
     return out
+
+
+def gather_peak(width, height, k, reps=5, device=0):
+    """ts_measure_gather_peak: GB/s of 32-bit gathers the GPU serves from a
+    width x height texel table, in the cost loop's patch shape (k nearest
+    offsets around a random centre) and fully random."""
+    out = _GatherPeak()
+    rc = lib().ts_measure_gather_peak(device, width, height, k, reps, C.byref(out))
+    if rc:
+        raise Error(rc, "ts_measure_gather_peak")
+    return {f: getattr(out, f) for f, _ in out._fields_}
 
 
 def guide_map(image, target, device=0):
@@ -833,10 +851,16 @@ def autotune_batch(make_sessions, device=0, repeats=2):
     return t
 
 
-def run_spec(spec, batch_divisor=8, max_batch=0, device=0, team_max_batch=None, team_full_max_batch=256):
+def run_spec(spec, batch_divisor=8, max_batch=0, device=0, team_max_batch=None, team_full_max_batch=256,
+             tuning=None):
     """Build and run a workload spec; returns a dict shaped like the oracle's."""
     g = builder_from_spec(spec, batch_divisor, max_batch, device, team_max_batch=team_max_batch,
-                          team_full_max_batch=team_full_max_batch).build().run()
+                          team_full_max_batch=team_full_max_batch, tuning=tuning).build().run()
+    return generated_outputs(g)
+
+
+def generated_outputs(g):
+    """The outputs of a GeneratedImage as a dict shaped like the oracle's."""
     flat, score = g.resolved()
     st = g.stats()
     return {"image": g.into_image(), "coord": g.coord_map(), "id": g.id_map(), "resolved": flat,

@@ -1,6 +1,6 @@
 """Build recipe for libtsgpu.so, the CUDA (sm_103a) library behind tsgpu.h.
 
-Four translation units compile in parallel with nvcc and link into
+Five translation units compile in parallel with nvcc and link into
 texture-synthesis_gb300/_build/libtsgpu.so.  Float contraction is disabled
 everywhere (--fmad=false on the device, -ffp-contract=off on the host): the
 synthesis cost sums must round exactly as the reference's do.
@@ -20,7 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
           "-I" + CSRC, "-I" + INCLUDE]
-SOURCES = ["ts_kernels.cu", "ts_session.cpp", "ts_noalloc.cu", "ts_autotune.cpp"]
+SOURCES = ["ts_kernels.cu", "ts_session.cpp", "ts_noalloc.cu", "ts_autotune.cpp", "ts_probe.cu"]
 
 
 def _newest_input():

@@ -40,6 +40,7 @@
 #include <mutex>
 #include <utility>
 
+#include "tsgpu.h"
 #include "ts_common.h"
 #include "ts_kernels.cuh"
 
@@ -56,7 +57,8 @@ constexpr int kTeamFullThreads = 256;  // the full-evaluation form: batches of a
 constexpr int kExhCap = 2048;      // keys kept by the exhaustive k-NN at the cut distance
 constexpr int kExhAllKeys = 8192;  // keys the exhaustive k-NN sorts in shared memory directly
 constexpr int kExhSortAll = 256;   // at most this many keys are sorted without a select
-constexpr uint32_t kMaxDraws = 1u << 22;
+constexpr uint32_t kMaxDraws = TS_MAX_SAMPLE_DRAWS;  // (x, y) pairs per random candidate
+constexpr uint32_t kRcandFailed = 0x7fffu;              // map field of a random candidate whose draws ran out
 
 __device__ const double g_exp2_64[64] = {TS_EXP2_TABLE_VALUES};
 __device__ const float g_exp2_ff[128] = {TS_EXP2_FF_TABLE_VALUES};
@@ -124,29 +126,41 @@ __device__ __forceinline__ void random_candidates_body(const SessionDev &s, cons
   uint2 *out = st.rcand + (size_t)item * s.m;
   for (uint32_t t = 0; t < s.m; ++t) {
     uint64_t map64 = 0;
-    if (!gen_range_u64_bounded(g, s.n_maps, 256, map64)) {
-      set_err(s.err, kDevErrNoSample);
-      for (; t < s.m; ++t) out[t] = make_uint2(0u, 0u);  // keep every entry a valid texel
-      return;
-    }
-    const uint32_t map = (uint32_t)map64;
+    bool ok = gen_range_u64_bounded(g, s.n_maps, 256, map64);
+    const uint32_t map = ok ? (uint32_t)map64 : 0u;
     const MapDesc md = s.maps[map];
     uint32_t x = 0, y = 0;
-    bool ok = false;
-    for (uint32_t tries = 0; tries < kMaxDraws; ++tries) {
-      if (!gen_range_u32_bounded(g, md.w, 256, x) || !gen_range_u32_bounded(g, md.h, 256, y)) break;
-      if (coord_valid(s, md, (int)x, (int)y)) {
-        ok = true;
-        break;
+    if (ok) {
+      ok = false;
+      for (uint32_t tries = 0; tries < kMaxDraws; ++tries) {
+        if (!gen_range_u32_bounded(g, md.w, 256, x) || !gen_range_u32_bounded(g, md.h, 256, y)) break;
+        if (coord_valid(s, md, (int)x, (int)y)) {
+          ok = true;
+          break;
+        }
       }
     }
     if (!ok) {
-      set_err(s.err, kDevErrNoSample);
-      for (; t < s.m; ++t) out[t] = make_uint2(0u, 0u);  // keep every entry a valid texel
+      // Only an item with resolved neighbours uses its random candidates
+      // (an item without any resolves at random, ms.rs:1002-1010), so the
+      // failure is left for the resolve kernel to report when it reads one.
+      for (; t < s.m; ++t) out[t] = make_uint2(0u, kRcandFailed);
       return;
     }
     out[t] = make_uint2(x | (y << 16), map);
   }
+}
+
+// A random candidate as the resolve kernels store it: {x | y<<16, map}.  A
+// failed draw (kRcandFailed) reports TS_ERR_NO_VALID_SAMPLE and is replaced
+// by texel (0, 0) of map 0, so that nothing reads past the map table; the
+// run's result is discarded.
+__device__ __forceinline__ uint2 use_rcand(const SessionDev &s, uint2 v) {
+  if (v.y == kRcandFailed) {
+    set_err(s.err, kDevErrNoSample);
+    v = make_uint2(0u, 0u);
+  }
+  return v;
 }
 
 // Exact squared normalised distance of a neighbour at offset (dx, dy).
@@ -169,6 +183,21 @@ __device__ __forceinline__ double neighbour_dist_near(const SessionDev &s, int p
   const int R = s.dtab_r;
   const double ddx = __ldg(&s.dxt[(size_t)px * (2 * R + 1) + dx + R]);
   return __fma_rn(ddx, ddx, __ldg(&s.dy2t[(size_t)py * (2 * R + 1) + dy + R]));
+}
+
+// ---------------------------------------------------------------------------
+// The mean of a distance list whose sums are exact (SessionDev::exact_sum):
+// the in-order sum of the 4x-duplicated list (ms.rs:417-421) never rounds,
+// so it equals 4 * (the list's sum in any order of exact adds), and the mean
+// is that divided by 4n, rounded once, as the reference divides.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum_exact(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ double exact_mean(double sum, uint32_t n) {
+  return __ddiv_rn(__dmul_rn(4.0, sum), (double)(n * 4u));
 }
 
 __device__ __forceinline__ unsigned long long nb_key(uint32_t d2, int x, int y) {
@@ -300,9 +329,16 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
       // instruction (an f64 instruction costs the same whatever its active
       // lanes, and GB300's f64 pipe is narrow)
       __syncwarp();
+      double part = 0.0;
       for (uint32_t j = lane; j < s.k; j += kWarp) {
         const int32_t o = nbo[j];
-        b.dist[(size_t)j * nb + local] = neighbour_dist_near(s, px, py, off_dx(o), off_dy(o));
+        const double d = neighbour_dist_near(s, px, py, off_dx(o), off_dy(o));
+        b.dist[(size_t)j * nb + local] = d;
+        if (s.exact_sum) part = __dadd_rn(part, d);
+      }
+      if (s.exact_sum) {
+        const double sum = warp_sum_exact(part);
+        if (lane == 0) b.mean[local] = exact_mean(sum, s.k);
       }
     }
     if (lane == 0) {
@@ -340,6 +376,7 @@ __device__ __forceinline__ double mean_chain(const double *d, uint32_t n) {
 
 struct ExhShared {
   double dist[256];  // the item's neighbour distances, when the kernel also computes the mean
+  double wsum[kExhThreads / 32];  // per-warp exact distance sums (SessionDev::exact_sum)
   int32_t nbo[256];  // and their offsets
   uint32_t hist[256];
   unsigned long long keys[kExhCap];
@@ -793,18 +830,30 @@ __device__ uint32_t knn_exhaustive_item(const SessionDev &s, const StageDev &st,
   int32_t *nbo = b.nbuf + (size_t)local * k;
   const uint32_t nb = b.i1 - b.i0;
   const double x2 = s.xdiv[px + s.xdiv_off], y2 = s.ydiv[py + s.ydiv_off];
+  double part = 0.0;
   for (uint32_t i = threadIdx.x; i < nout; i += blockDim.x) {
     const unsigned long long key = sorted[i];
     const int x = (int)(key & 0xffffu) - 32768, y = (int)((key >> 16) & 0xffffu) - 32768;
     nbo[i] = pack_off(x - px, y - py);
     const double d = neighbour_dist(s, px, py, x - px, y - py, x2, y2);
     b.dist[(size_t)i * nb + local] = d;
+    if (s.exact_sum) part = __dadd_rn(part, d);
     if (with_mean) {
       sh.dist[i] = d;
       sh.nbo[i] = pack_off(x - px, y - py);
     }
   }
-  if (with_mean && mean_here) {
+  if (s.exact_sum && mean_here) {
+    // every item of the launch, fallback items included, gets its mean here
+    part = warp_sum_exact(part);
+    if ((threadIdx.x & 31) == 0) sh.wsum[threadIdx.x >> 5] = part;
+    __syncthreads();
+    if (threadIdx.x == 0 && nout > 0) {
+      double sum = 0.0;
+      for (uint32_t w = 0; w < blockDim.x / 32; ++w) sum = __dadd_rn(sum, sh.wsum[w]);
+      b.mean[local] = exact_mean(sum, nout);
+    }
+  } else if (with_mean && mean_here) {
     __syncthreads();
     if (threadIdx.x == 0 && nout > 0) b.mean[local] = mean_chain(sh.dist, nout);
   }
@@ -1349,7 +1398,7 @@ __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev
     // random candidates after the coherence ones
     const uint2 *rc = st.rcand + (size_t)item * s.m;
     for (uint32_t t = lane; t < s.m; t += kWarp) {
-      const uint2 v = rc[t];
+      const uint2 v = use_rcand(s, rc[t]);
       w.cxy[ncoh + t] = v.x;
       w.caux[ncoh + t] = v.y | kAuxNeg | (t << 16);
     }
@@ -1489,7 +1538,7 @@ __device__ __forceinline__ void resolve_team_body(const SessionDev &s, const Sta
     if (maxoff) atomicMax(&sh_maxoff, maxoff);
     const uint2 *rc = st.rcand + (size_t)item * s.m;
     for (uint32_t t = tid; t < s.m; t += T) {
-      const uint2 v = rc[t];
+      const uint2 v = use_rcand(s, rc[t]);
       w.cxy[ncoh + t] = v.x;
       w.caux[ncoh + t] = v.y | kAuxNeg | (t << 16);
     }
@@ -2247,7 +2296,7 @@ __global__ void __launch_bounds__(kTeamFullThreads) k_step_team_full(SessionDev 
       if (bad_map) atomicOr(&sh_flags, 2);
       if (maxoff) atomicMax(&sh_maxoff, maxoff);
       for (uint32_t q = t; q < s.m; q += TS) {
-        const uint2 v = q == (uint32_t)t ? rv0 : rc[q];
+        const uint2 v = use_rcand(s, q == (uint32_t)t ? rv0 : rc[q]);
         w.cxy[ncoh + q] = v.x;
         w.caux[ncoh + q] = v.y | kAuxNeg | (q << 16);
       }

@@ -83,6 +83,11 @@ struct SessionDev {
   int *err;
   unsigned long long *evals;  // candidate-cost evaluations, summed by commit
   int guide_dims_differ;  // some example guide differs in size from its map
+  // W and H are powers of two: every neighbour distance is an integer
+  // multiple of 1/max(W,H)^2 and every partial sum of a distance list stays
+  // below 2^53 such units, so the in-order f64 sum (ms.rs:417-421) is exact
+  // and any order of exact adds gives its bits (exact_sum_ok on the host)
+  int exact_sum;
   uint32_t W, H, wpr;  // wpr: 32-bit words per bitmap row
   int tiling;
   int32_t x_l, x_r, y_b, y_t;

@@ -1601,6 +1601,20 @@ void keep_pool(int dev) {
 // Device buffers of a run and the step descriptors that point into them.
 // With a pool stream, the buffers are stream-ordered pool memory (freed
 // without waiting for the device); otherwise plain cudaMalloc.
+// Whether a session's neighbour-distance sums (get_distances_to_k_neighs,
+// ms.rs:405-425) are exact.  With W and H powers of two, x / W and y / H are
+// exact, so every distance fma(dx, dx, dy * dy) is an integer multiple of
+// q = 1 / max(W, H)^2 below 8 max(W, H)^2 q (tiling mirrors included), and a
+// list of 4k such values sums below 32 k max(W, H)^2 q.  When that is below
+// 2^53 q every partial sum is representable, so the reference's in-order f64
+// adds never round and any order of exact adds yields the same double.
+bool exact_sum_ok(uint32_t W, uint32_t H, uint32_t k) {
+  auto pow2 = [](uint32_t v) { return v != 0 && (v & (v - 1)) == 0; };
+  if (!pow2(W) || !pow2(H)) return false;
+  const uint64_t M = std::max(W, H);
+  return M <= (1u << 16) && 32ull * std::max<uint32_t>(k, 1) * M * M < (1ull << 53);
+}
+
 void run_alloc(RunCtx &c, cudaStream_t pool) {
   ts_session *s = c.s;
   const Params &p = s->prm;
@@ -1710,6 +1724,7 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   sd.evals = c.d_evals.p;
   sd.W = W;
   sd.H = H;
+  sd.exact_sum = exact_sum_ok(W, H, k) ? 1 : 0;
   sd.wpr = wpr;
   sd.tiling = p.tiling ? 1 : 0;
   sd.x_l = x_l;
@@ -1875,7 +1890,9 @@ void enqueue_step(RunCtx &c, const Step &stp, cudaStream_t st, LaunchTimer &lt) 
         c.launches += 2;
       }
     }
-    if (c.k > 0 && !stp.exhaustive) {  // the exhaustive k-NN over a whole batch computes the mean itself
+    // the exhaustive k-NN over a whole batch computes the mean itself, and so
+    // do the walk and the fallback k-NN for sessions whose sums are exact
+    if (c.k > 0 && !stp.exhaustive && !sd.exact_sum) {
       lt.run(TS_KERNEL_MEAN, [&] { launch_mean(sd, stp.st, stp.bd, st); });
       ++c.launches;
     }
@@ -2170,7 +2187,7 @@ uint32_t phase_units(const Step &stp, const RunCtx &c, int phase) {
     case kPhaseRandom: return (stp.rc && c.m > 0 && !c.rc_ahead) ? stp.rc_st.n_items : 0;
     case kPhaseWalk: return (knn && !stp.exhaustive) ? stp.n : 0;
     case kPhaseExhaustive: return (knn && stp.exhaustive) ? stp.n : 0;
-    case kPhaseMean: return (knn && !stp.exhaustive) ? stp.n : 0;
+    case kPhaseMean: return (knn && !stp.exhaustive && !c.sd.exact_sum) ? stp.n : 0;
     case kPhaseResolve:
     case kPhaseTeamPart:
     case kPhaseTeamFull: return (stp.batch && stp.resolve == phase) ? stp.n : 0;
@@ -2908,8 +2925,16 @@ void server_driver(ts_server *S) {
     for (ServerReq *r : S->active)
       if (r->c->steps[r->cursor].stage < (int)r->picked.load(std::memory_order_acquire)) ready.push_back(r);
     if (ready.empty()) {
+      // Wait for a picker (or a new request), re-checking under the mutex:
+      // a picker publishes `picked` before it takes the mutex to notify, so
+      // no wake-up is lost between the check above and the wait.
       std::unique_lock<std::mutex> lk(S->mu);
-      S->cv_picked.wait_for(lk, std::chrono::microseconds(500));
+      S->cv_picked.wait_for(lk, std::chrono::microseconds(500), [&] {
+        if (S->stop || (!S->pending.empty() && !S->free_slots.empty())) return true;
+        for (ServerReq *r : S->active)
+          if (r->c->steps[r->cursor].stage < (int)r->picked.load(std::memory_order_acquire)) return true;
+        return false;
+      });
       continue;
     }
     try {
@@ -3263,6 +3288,7 @@ int ts_server_submit(ts_server *S, ts_session *s, uint64_t *ticket) {
   S->pending.push_back(r.release());
   S->stats.submitted += 1;
   S->cv_work.notify_one();
+  S->cv_picked.notify_all();  // a driver waiting on pickers admits it at once
   return TS_OK;
 }
 
