@@ -11,8 +11,15 @@ Session::run() over one session.
          flushed (a 256 MB device write) between timed steps
   e2e    the same metric through the C ABI with host buffers: build (input
          upload, pyramids) + run + reading the image back, per step
-  roofline  the resolve kernel (dominant) measured with per-launch CUDA
-         events in a separate profiled pass
+  roofline  the resolve kernels (dominant) measured with per-launch CUDA
+         events in a separate profiled pass, against the measured gather
+         ceiling (ts_measure_gather_peak: patch-shaped 32-bit gathers from a
+         table the size of the workload's example level), with the HBM copy
+         bandwidth beside it
+  parity the last timed run's outputs against the oracle's, bit for bit,
+         inside the CPU-baseline leg (outside every timed region)
+  config0, config2  the single-example 256^2 and guided 512^2 workloads,
+         measured the same way (value, e2e, roofline)
   cpu_baseline  the CPU oracle (a C port of the reference's algorithm) on
          the host cores: whole runs of the same workload, repeated for
          about 10 s
@@ -23,12 +30,14 @@ Session::run() over one session.
          before any timing (ts_autotune_session); the batched and served
          forms use those ts_autotune_batch picked on the batched mix
   served   a Poisson request stream from the batched mix (70%) and 512^2
-         inpainting requests (30%) through the served form and, for
-         comparison, through the plain path one request at a time:
-         p50/p99 latency from arrival to result and aggregate Mpx/s
+         inpainting requests (30%), 256 requests at each of 10, 25, 50, 100
+         and 200 req/s, through the served form and, for comparison,
+         through the plain path one request at a time: p50/p99 latency from
+         arrival to result and aggregate Mpx/s; then all 256 submitted at
+         once (saturation: the served form's aggregate throughput)
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                [--workload remix|batched|served]
+                [--workload remix|single|guided|batched|served]
 """
 import argparse
 import importlib
@@ -245,9 +254,31 @@ def serve_stream(ts, reqs, served=True, max_active=64, tuning=None):
     return out
 
 
-def measure_served(ts, wl, lams=(50, 200), n=64, tuning=None):
+def serve_saturated(ts, reqs, max_active=64, tuning=None):
+    """Every request of the stream submitted at once to the served form, its
+    sessions built beforehand: the server's aggregate throughput with work
+    always waiting (beside it, the batched form's on the 64-session mix)."""
+    sessions = [ts.builder_from_spec(spec).build() for _, spec in reqs]
+    px = sum(spec["out_w"] * spec["out_h"] for _, spec in reqs)
+    srv = ts.Server(max_active=max_active, tuning=tuning)
+    t0 = time.perf_counter()
+    tickets = [srv.submit(s) for s in sessions]
+    lat = []
+    for t in tickets:
+        srv.wait(t)
+        lat.append(time.perf_counter() - t0)
+    span = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    return {"requests": len(reqs), "mpx_s": px / span / 1e6, "span_ms": span * 1e3,
+            "p50_ms": _pct(lat, 50) * 1e3, "p99_ms": _pct(lat, 99) * 1e3,
+            "peak_active": st["peak_active"], "ticks": st["ticks"]}
+
+
+def measure_served(ts, wl, lams=(10, 25, 50, 100, 200), n=256, tuning=None):
     """Config 4: the Poisson stream through the served form and through the
-    plain path, at each arrival rate."""
+    plain path at each arrival rate (n requests each), then the whole
+    stream at once (saturation)."""
     warm = wl.config4_requests(6, 1000.0, seed=99)
     serve_stream(ts, warm, True, tuning=tuning)
     rows = []
@@ -255,25 +286,152 @@ def measure_served(ts, wl, lams=(50, 200), n=64, tuning=None):
         reqs = wl.config4_requests(n, float(lam))
         rows.append({"lambda_req_s": lam, "served": serve_stream(ts, reqs, True, tuning=tuning),
                      "plain": serve_stream(ts, reqs, False)})
-    return {"workload": "served_mix", "mix": "70% batched mix, 30% 512^2 inpainting", "rates": rows}
+    sat = serve_saturated(ts, wl.config4_requests(n, 1e6), tuning=tuning)
+    return {"workload": "served_mix", "mix": "70% batched mix, 30% 512^2 inpainting",
+            "requests_per_rate": n, "rates": rows, "saturated": sat}
 
 
-def measure_cpu_baseline(spec, min_seconds=10.0, max_runs=20):
+def measure_cpu_baseline(spec, min_seconds=10.0, max_runs=20, check=None):
     """The oracle (the C port of the reference's algorithm) on every host
     core: whole runs of the workload, repeated until min_seconds of CPU
-    work (at most max_runs runs)."""
+    work (at most max_runs runs).  With `check` (a GPU run's outputs), the
+    first oracle run's outputs are also compared with it bit for bit; the
+    second value returned says how that went."""
     from oracle import oracle
 
     threads = os.cpu_count() or 1
     px = spec["out_w"] * spec["out_h"]
     runs, sec = 0, 0.0
+    parity = "not checked"
     while runs < max(1, max_runs) and (runs == 0 or sec < min_seconds):
         t0 = time.perf_counter()
-        oracle.run(spec, nthreads=threads)
+        r = oracle.run(spec, nthreads=threads)
         sec += time.perf_counter() - t0
+        if runs == 0 and check is not None:
+            parity = compare_outputs(check, r)
         runs += 1
-    return {"value": px * runs / sec / 1e6, "unit": "Mpx/s", "cores": threads, "kind": "port",
-            "sample": "%d full runs of the workload (%.1f s), %d threads" % (runs, sec, threads)}
+    return ({"value": px * runs / sec / 1e6, "unit": "Mpx/s", "cores": threads, "kind": "port",
+             "sample": "%d full runs of the workload (%.1f s), %d threads" % (runs, sec, threads)}, parity)
+
+
+def compare_outputs(got, ref):
+    """'bit-exact' when image, coordinate map, id map, resolved list, every
+    f32 score (NaN-ness only for NaNs) and the eval count agree; else what
+    differs."""
+    import numpy as np
+
+    bad = []
+    for key in ("image", "coord", "id", "resolved", "scores"):
+        a, b = np.asarray(got[key]), np.asarray(ref[key])
+        if a.shape != b.shape:
+            bad.append("%s shape" % key)
+            continue
+        if key == "scores":
+            same = (a.view(np.uint32) == b.view(np.uint32)) | (np.isnan(a) & np.isnan(b))
+        else:
+            same = a == b
+        if not same.all():
+            bad.append("%s (%d places)" % (key, int((~same).sum())))
+    if got["evals"] != ref["evals"]:
+        bad.append("evals")
+    return "bit-exact" if not bad else "MISMATCH: " + ", ".join(bad)
+
+
+def bench_config(spec):
+    """The `config` object of a bench line; the same in both arms."""
+    p = spec["params"]
+    return {"workload": spec["name"], "out": [spec["out_w"], spec["out_h"]], "examples": len(spec["examples"]),
+            "k": p["nearest_neighbors"], "m": p["random_sample_locations"], "batch_divisor": 8,
+            "guided": spec.get("target_guide") is not None,
+            "l2": "GPU arm: L2 flushed between timed steps (256 MB device write)"}
+
+
+def padded_level_shape(spec):
+    """Width and height of one pyramid level of every example, padded as the
+    cost kernel reads them (a 32-texel border, one row pitch), stacked: the
+    table the gather ceiling is measured on."""
+    exs = spec["examples"]
+    pw = max(e["image"].shape[1] for e in exs) + 64
+    ph = sum(e["image"].shape[0] + 64 for e in exs)
+    return pw, ph
+
+
+def gather_roofline(ts, spec, prof, peak_cache={}):
+    """Roofline of the resolve family against the measured gather ceiling
+    (ts_measure_gather_peak on a table the size of this workload's example
+    level), with the HBM copy bandwidth beside it."""
+    kern = prof["kernels"]
+    res = kern["resolve"]
+    k = spec["params"]["nearest_neighbors"]
+    guided = spec.get("target_guide") is not None
+    per_eval = 4 * k * (2 if guided else 1)
+    alg_bytes = prof["cost_evals"] * per_eval  # example (+ guide) texels of every candidate-cost evaluation
+    achieved = alg_bytes / (res["ms"] / 1e3) / 1e9
+    shape = padded_level_shape(spec) + (k,)
+    if shape not in peak_cache:
+        peak_cache[shape] = ts.gather_peak(*shape, reps=5)
+    gp = peak_cache[shape]
+    hbm, hbm_kind = _peaks()
+    top = max(kern, key=lambda n: kern[n]["ms"])
+    out = {"kernel": "k_resolve family", "bound": "gather (L1/L2 load path)", "achieved": achieved,
+           "peak": gp["patch_gbs"], "unit": "GB/s", "frac": achieved / gp["patch_gbs"],
+           "peak_source": "measured: ts_measure_gather_peak, patch-shaped 32-bit gathers (k=%d) from a %.1f MB "
+                          "table, full occupancy" % (k, gp["table_bytes"] / 1e6),
+           "random_gather_gbs": gp["random_gbs"],
+           "hbm_peak": hbm, "hbm_frac": achieved / hbm, "hbm_peak_source": hbm_kind,
+           "alg_bytes_per_eval": per_eval,
+           "alg_bytes_per_launch": alg_bytes / max(1, res["launches"]),
+           "avg_launch_ms": res["ms"] / max(1, res["launches"]), "launches": res["launches"],
+           "kernel_share": {n: kern[n]["ms"] / max(1e-9, sum(v["ms"] for v in kern.values())) for n in kern},
+           "top_kernel": top}
+    if spec["name"] == "multi_example_tiling_512":
+        out["traffic"] = RESOLVE_DRAM_BYTES_PER_LAUNCH
+        out["traffic_source"] = "ncu capture of this workload, cold caches, bytes per resolve launch"
+    else:
+        out["traffic"] = None
+    return out
+
+
+def measure_workload(ts, spec, steps, warmup, tuning, flush):
+    """One workload: `value` (device-timed, sessions built beforehand), `e2e`
+    (build + run + image read-back through the C ABI with host buffers), and
+    the roofline of the resolve kernels from a separate profiled pass."""
+    px = spec["out_w"] * spec["out_h"]
+    for _ in range(warmup):
+        ts.builder_from_spec(spec, tuning=tuning).build().run()
+    sessions = [ts.builder_from_spec(spec, tuning=tuning).build() for _ in range(steps)]
+    gpu_ms, evals, launches, walls = [], [], [], []
+    last = None
+    for s in sessions:
+        flush()
+        t0 = time.perf_counter()
+        g = s.run()
+        walls.append(time.perf_counter() - t0)
+        st = g.stats()
+        gpu_ms.append(st["gpu_ms"])
+        evals.append(st["cost_evals"])
+        launches.append(st["kernel_launches"])
+        last = g
+    outputs = ts.generated_outputs(last)  # the last timed run's outputs, read after timing
+    value = px * len(gpu_ms) / (sum(gpu_ms) / 1e3) / 1e6
+    e2e_t = []
+    h2d = sum(e["image"].nbytes for e in spec["examples"])
+    h2d += sum(e["guide"].nbytes for e in spec["examples"] if e.get("guide") is not None)
+    if spec.get("target_guide") is not None:
+        h2d += spec["target_guide"].nbytes
+    d2h = px * 4
+    for _ in range(max(1, min(steps, 10))):
+        t1 = time.perf_counter()
+        g = ts.builder_from_spec(spec, tuning=tuning).build().run()
+        g.into_image()
+        e2e_t.append(time.perf_counter() - t1)
+    e2e = px / (sum(e2e_t) / len(e2e_t)) / 1e6
+    prof = ts.builder_from_spec(spec, profile=True, tuning=tuning).build().run().stats()
+    return {"value": value, "unit": "Mpx/s", "steps": len(gpu_ms), "ms_per_step": sum(gpu_ms) / len(gpu_ms),
+            "cost_evals_per_s": sum(evals) / (sum(gpu_ms) / 1e3), "gpu_launches": int(sum(launches) / len(launches)),
+            "wall_ms_per_step": sum(walls) / len(walls) * 1e3,
+            "e2e": {"value": e2e, "unit": "Mpx/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": gather_roofline(ts, spec, prof), "outputs": outputs}
 
 
 def run_reference_arm(args):
@@ -296,8 +454,7 @@ def run_reference_arm(args):
         "impl": "reference", "metric": "output Mpx/s", "value": value, "unit": "Mpx/s", "n_gpus": args.gpus,
         "steps": len(times), "warmup": 1, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": spec["name"], "out": [spec["out_w"], spec["out_h"]], "examples": 4,
-                   "k": 50, "m": 50, "batch_divisor": 8},
+        "config": bench_config(spec),
         "cpu_baseline": {"value": value, "unit": "Mpx/s", "cores": threads, "kind": "port",
                          "sample": "full runs of the workload, batch-snapshot schedule, %d threads" % threads},
         "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -314,7 +471,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--once", action="store_true", help="build and run one session, print its stats (for profilers)")
-    ap.add_argument("--workload", default="remix", choices=["remix", "batched", "served"])
+    ap.add_argument("--workload", default="remix", choices=["remix", "single", "guided", "batched", "served"],
+                    help="remix: the headline line (config 1, plus configs 0 and 2, batched and served objects); "
+                         "single / guided: config 0 / config 2 alone")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and served objects of the remix line")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -326,8 +485,6 @@ def main():
 
     importlib.import_module(PKG + ".build").build()
     ts = importlib.import_module(PKG)
-    import numpy as np
-
     wl = importlib.import_module(PKG + ".workloads")
     if args.workload == "batched":
         if args.once:  # one batched run of the 64-session mix (for profilers)
@@ -341,85 +498,50 @@ def main():
         return
     if args.workload == "served":
         print(json.dumps({"metric": "request latency p50/p99 and aggregate Mpx/s (served form)",
-                          **measure_served(ts, wl, lams=(10, 25, 50, 100, 200), n=64)}))
+                          **measure_served(ts, wl)}))
         return
-    spec = workload()
-    px = spec["out_w"] * spec["out_h"]
+    spec = {"remix": workload, "single": wl.config0, "guided": wl.config2}[args.workload]()
+    if args.workload != "remix":
+        args.no_extra = True
     if args.once:
         g = ts.builder_from_spec(spec).build().run()
         print(json.dumps(g.stats()))
         return
     # --- launch-shape thresholds tuned on this workload (before any timing)
     tuning = ts.autotune_session(lambda: ts.builder_from_spec(spec), repeats=3)
-    # --- device-resident throughput: sessions built before the timed region
-    for _ in range(args.warmup):
-        ts.builder_from_spec(spec, tuning=tuning).build().run()
-    sessions = [ts.builder_from_spec(spec, tuning=tuning).build() for _ in range(args.steps)]
     flush = L2Flush()
-    gpu_ms, evals, launches, walls = [], [], [], []
     with ClockSampler(0) as clk:
-        for s in sessions:
-            flush()
-            t0 = time.perf_counter()
-            g = s.run()
-            walls.append(time.perf_counter() - t0)
-            st = g.stats()
-            gpu_ms.append(st["gpu_ms"])
-            evals.append(st["cost_evals"])
-            launches.append(st["kernel_launches"])
-    wall = sum(walls)
-    ms = sum(gpu_ms) / len(gpu_ms)
-    value = px * len(gpu_ms) / (sum(gpu_ms) / 1e3) / 1e6
-    # --- end to end through the C ABI with host buffers
-    e2e_t = []
-    h2d = sum(e["image"].nbytes for e in spec["examples"])
-    d2h = px * 4
-    for _ in range(max(1, min(args.steps, 10))):
-        t1 = time.perf_counter()
-        g = ts.builder_from_spec(spec, tuning=tuning).build().run()
-        img = g.into_image()
-        e2e_t.append(time.perf_counter() - t1)
-    e2e = px / (sum(e2e_t) / len(e2e_t)) / 1e6
-    peak, peak_kind = _peaks()
-    # --- roofline of the dominant kernel: a separate pass with CUDA events
-    # around every launch on the launching stream
-    prof = ts.builder_from_spec(spec, profile=True, tuning=tuning).build().run().stats()
-    kern = prof["kernels"]
-    top = max(kern, key=lambda n: kern[n]["ms"])
-    res = kern["resolve"]
-    k = spec["params"]["nearest_neighbors"]
-    per_eval = 4 * k * (2 if spec.get("target_guide") is not None else 1)
-    alg_bytes = prof["cost_evals"] * per_eval  # example texels every candidate-cost evaluation reads
-    achieved = alg_bytes / (res["ms"] / 1e3) / 1e9
-    roofline = {"kernel": "k_resolve", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "traffic": RESOLVE_DRAM_BYTES_PER_LAUNCH,
-                "traffic_source": "ncu capture of this workload, cold caches, bytes per resolve launch",
-                "alg_bytes_per_launch": alg_bytes / max(1, res["launches"]),
-                "avg_launch_ms": res["ms"] / max(1, res["launches"]), "launches": res["launches"],
-                "kernel_share": {n: kern[n]["ms"] / max(1e-9, sum(v["ms"] for v in kern.values())) for n in kern},
-                "top_kernel": top}
+        m = measure_workload(ts, spec, args.steps, args.warmup, tuning, flush)
+    outputs = m.pop("outputs")
     line = {
-        "metric": "output Mpx/s", "value": value, "unit": "Mpx/s", "n_gpus": world, "steps": len(gpu_ms),
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "metric": "output Mpx/s", "value": m["value"], "unit": "Mpx/s", "n_gpus": world, "steps": m["steps"],
+        "warmup": args.warmup, "ms_per_step": m["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": spec["name"], "out": [spec["out_w"], spec["out_h"]], "examples": 4, "k": 50,
-                   "m": 50, "batch_divisor": 8,
-                   "l2": "flushed between timed steps (256 MB device write)" if flush.buf is not None
-                   else "not flushed (no torch on this host)"},
-        "cost_evals_per_s": sum(evals) / (sum(gpu_ms) / 1e3),
-        "gpu_launches": int(sum(launches) / len(launches)),
-        "wall_ms_per_step": wall / len(gpu_ms) * 1e3,
+        "config": bench_config(spec),
+        "cost_evals_per_s": m["cost_evals_per_s"],
+        "gpu_launches": m["gpu_launches"],
+        "wall_ms_per_step": m["wall_ms_per_step"],
         "clocks": clk.summary(),
-        "e2e": {"value": e2e, "unit": "Mpx/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": roofline,
+        "e2e": m["e2e"],
+        "roofline": m["roofline"],
         "tuning": _tuning_dict(tuning),
         "cpu_baseline": None,
+        "parity": "not checked (CPU baseline skipped)",
     }
     if not args.no_extra:
+        # configs 0 and 2 (single-example 256^2 and guided 512^2) with the
+        # default launch shapes; parity tests cover them at full size
+        for key, sp in (("config0", wl.config0()), ("config2", wl.config2())):
+            with ClockSampler(0) as c2:
+                r = measure_workload(ts, sp, max(3, args.steps // 2), args.warmup, None, flush)
+            r.pop("outputs")
+            r["clocks"] = c2.summary()
+            r["config"] = bench_config(sp)
+            line[key] = r
         line["batched"], btun = measure_batched(ts, wl)
         line["served"] = measure_served(ts, wl, tuning=btun)
     if not args.no_cpu_baseline and rank == 0:
-        line["cpu_baseline"] = measure_cpu_baseline(spec)
+        line["cpu_baseline"], line["parity"] = measure_cpu_baseline(spec, check=outputs)
     print(json.dumps(line))
 
 

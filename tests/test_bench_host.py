@@ -11,7 +11,8 @@ def test_cpu_baseline_object(wl, oracle):
     sys.path.insert(0, ROOT)
     bench = importlib.import_module("bench")
     spec = wl.config0(out=32, ex=16)
-    cb = bench.measure_cpu_baseline(spec, min_seconds=0.05, max_runs=3)
+    cb, parity = bench.measure_cpu_baseline(spec, min_seconds=0.05, max_runs=3)
+    assert parity == "not checked"
     assert cb["kind"] == "port" and cb["unit"] == "Mpx/s"
     assert cb["value"] > 0 and cb["cores"] >= 1
     assert "full runs" in cb["sample"]
@@ -47,3 +48,27 @@ def test_reference_arm_line():
     assert d["impl"] == "reference" and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_parity_check_in_cpu_baseline(wl, oracle):
+    """The CPU-baseline leg compares a run's outputs with the oracle's: an
+    identical copy reads bit-exact, a planted change to the copy is named."""
+    sys.path.insert(0, ROOT)
+    bench = importlib.import_module("bench")
+    spec = wl.config0(out=24, ex=16)
+    ref = oracle.run(spec, nthreads=2)
+    _, parity = bench.measure_cpu_baseline(spec, min_seconds=0.0, max_runs=1, check=ref)
+    assert parity == "bit-exact"
+    bad = dict(ref)
+    bad["image"] = ref["image"].copy()
+    bad["image"][3, 5, 1] ^= 1
+    _, parity = bench.measure_cpu_baseline(spec, min_seconds=0.0, max_runs=1, check=bad)
+    assert parity.startswith("MISMATCH") and "image (1 places)" in parity
+
+
+def test_config_same_in_both_arms(wl):
+    sys.path.insert(0, ROOT)
+    bench = importlib.import_module("bench")
+    spec = bench.workload()
+    assert bench.bench_config(spec) == bench.bench_config(wl.config1())
+    assert bench.bench_config(spec)["workload"] == "multi_example_tiling_512"

@@ -9,7 +9,12 @@
 // own input and output buffers; the intermediate data of the resize passes
 // (an f32 image, the downscaled image, the filter taps) lives in one
 // file-scope device array of fixed size, kNoAllocScratchBytes, which every
-// GPU that loads the library holds until the process exits.
+// GPU that loads the library holds until the process exits.  The call copies
+// nothing from host memory with cudaMemcpy: the taps travel as kernel
+// parameters, so enqueueing never waits for the caller's stream.
+#include <string.h>
+
+#include <algorithm>
 #include <mutex>
 
 #include <cuda_runtime.h>
@@ -48,6 +53,37 @@ unsigned char *g_scratch[kMaxDevices] = {};
 uint32_t g_host_taps[2][kTapsEntries * 4];
 float g_host_weights[2][kWeightCap];
 
+// The filter taps reach the device inside kernel parameters, which a launch
+// copies when it is made: no host-to-device copy from pageable memory (such
+// a copy may wait for the stream), and the host buffers above are free for
+// the next resize as soon as the launch returns.  32,004 bytes of
+// parameters, within the 32,764 bytes a launch may carry.
+constexpr uint32_t kPutWords = 8000;
+struct PutWords {
+  uint32_t n;
+  uint32_t w[kPutWords];
+};
+PutWords g_put;  // guarded by g_mutex
+
+__global__ void k_put_words(uint32_t *dst, const __grid_constant__ PutWords p) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) dst[i] = p.w[i];
+}
+
+// Stores n words from host memory at dst (device) in launches of at most
+// kPutWords words each.
+cudaError_t put_words(uint32_t *dst, const void *src, size_t n, cudaStream_t st) {
+  const uint32_t *w = (const uint32_t *)src;
+  for (size_t i = 0; i < n; i += kPutWords) {
+    const uint32_t c = (uint32_t)std::min<size_t>(kPutWords, n - i);
+    g_put.n = c;
+    memcpy(g_put.w, w + i, (size_t)c * 4);
+    k_put_words<<<(c + 255) / 256, 256, 0, st>>>(dst + i, g_put);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 // Scratch regions, offsets from the start of the array.
 constexpr size_t kOffTmp = 0;
 constexpr size_t kOffSmall = kOffTmp + kTmpBytes;
@@ -66,15 +102,10 @@ int resize_noalloc(unsigned char *base, const uint8_t *src, uint32_t w, uint32_t
   const long wv = ts::axis_taps_into(f, h, nh, g_host_taps[0], g_host_weights[0], kWeightCap);
   const long wh = ts::axis_taps_into(f, w, nw, g_host_taps[1], g_host_weights[1], kWeightCap);
   if (wv < 0 || wh < 0) return TS_ERR_LIMIT;
-  // pageable-source copies stage the host data before returning, so the
-  // host tap buffers may be refilled by the next resize
-  if (cudaMemcpyAsync(base + kOffTaps0, g_host_taps[0], (size_t)nh * 16, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-      cudaMemcpyAsync(base + kOffTaps1, g_host_taps[1], (size_t)nw * 16, cudaMemcpyHostToDevice, st) != cudaSuccess)
-    return TS_ERR_CUDA;
-  if ((wv && cudaMemcpyAsync(base + kOffWeights0, g_host_weights[0], (size_t)wv * 4, cudaMemcpyHostToDevice, st) !=
-                 cudaSuccess) ||
-      (wh && cudaMemcpyAsync(base + kOffWeights1, g_host_weights[1], (size_t)wh * 4, cudaMemcpyHostToDevice, st) !=
-                 cudaSuccess))
+  if (put_words((uint32_t *)(base + kOffTaps0), g_host_taps[0], (size_t)nh * 4, st) != cudaSuccess ||
+      put_words((uint32_t *)(base + kOffTaps1), g_host_taps[1], (size_t)nw * 4, st) != cudaSuccess ||
+      put_words((uint32_t *)(base + kOffWeights0), g_host_weights[0], (size_t)wv, st) != cudaSuccess ||
+      put_words((uint32_t *)(base + kOffWeights1), g_host_weights[1], (size_t)wh, st) != cudaSuccess)
     return TS_ERR_CUDA;
   float *tmp = (float *)(base + kOffTmp);
   // the f32 image starts at zero, as a fresh buffer does in ts_image_pyramid
@@ -88,6 +119,7 @@ int resize_noalloc(unsigned char *base, const uint8_t *src, uint32_t w, uint32_t
   } else if (cudaMemsetAsync(dst, 0, (size_t)nw * nh * 4, st) != cudaSuccess) {
     return TS_ERR_CUDA;
   }
+  // no error was pending when the call began, so this one is the resize's
   return cudaGetLastError() == cudaSuccess ? TS_OK : TS_ERR_CUDA;
 }
 
@@ -100,6 +132,9 @@ extern "C" int ts_image_pyramid_noalloc(const uint8_t *d_rgba, uint32_t width, u
   if (width > kMaxSideNoAlloc || height > kMaxSideNoAlloc || (uint64_t)width * height > kMaxPixels ||
       levels > kMaxLevels)
     return TS_ERR_LIMIT;
+  // An error left by the caller's own work stays theirs: report it without
+  // clearing it, and enqueue nothing.
+  if (cudaPeekAtLastError() != cudaSuccess) return TS_ERR_CUDA;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return TS_ERR_CUDA;
   cudaStream_t st = (cudaStream_t)stream;
