@@ -420,17 +420,28 @@ def measure_workload(ts, spec, steps, warmup, tuning, flush):
     if spec.get("target_guide") is not None:
         h2d += spec["target_guide"].nbytes
     d2h = px * 4
+    parts = []
     for _ in range(max(1, min(steps, 10))):
         t1 = time.perf_counter()
-        g = ts.builder_from_spec(spec, tuning=tuning).build().run()
+        sess = ts.builder_from_spec(spec, tuning=tuning).build()
+        t2 = time.perf_counter()
+        g = sess.run()
+        t3 = time.perf_counter()
         g.into_image()
-        e2e_t.append(time.perf_counter() - t1)
+        t4 = time.perf_counter()
+        e2e_t.append(t4 - t1)
+        st = g.stats()
+        parts.append({"build_ms": (t2 - t1) * 1e3, "run_ms": (t3 - t2) * 1e3, "image_ms": (t4 - t3) * 1e3,
+                      **{k: st[k] for k in ("host_plan_ms", "host_alloc_ms", "host_enqueue_ms", "host_wait_ms",
+                                            "host_finish_ms", "upload_ms", "readback_ms", "gpu_ms")}})
     e2e = px / (sum(e2e_t) / len(e2e_t)) / 1e6
+    breakdown = {k: sum(p[k] for p in parts) / len(parts) for k in parts[0]}
     prof = ts.builder_from_spec(spec, profile=True, tuning=tuning).build().run().stats()
     return {"value": value, "unit": "Mpx/s", "steps": len(gpu_ms), "ms_per_step": sum(gpu_ms) / len(gpu_ms),
             "cost_evals_per_s": sum(evals) / (sum(gpu_ms) / 1e3), "gpu_launches": int(sum(launches) / len(launches)),
             "wall_ms_per_step": sum(walls) / len(walls) * 1e3,
-            "e2e": {"value": e2e, "unit": "Mpx/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": e2e, "unit": "Mpx/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "breakdown_ms": breakdown},
             "roofline": gather_roofline(ts, spec, prof), "outputs": outputs}
 
 

@@ -222,16 +222,18 @@ int ts_image_pyramid_noalloc(const uint8_t *d_rgba, uint32_t width, uint32_t hei
  * width x height 32-bit texels (plus a 12-texel border) that the call
  * allocates, fills and frees:
  *   patch_gbs   a pseudo-random centre per thread and the k offsets nearest
- *               the origin around it, four loads in flight (the cost loop's
- *               access shape);
- *   random_gbs  independent pseudo-random texels, four in flight.
- * Both count 4 bytes per load; the best of `reps` timed launches (CUDA
- * events) after one warm-up.  k <= 256, sides <= 16384. */
+ *               the origin around it (the cost loop's access shape);
+ *   random_gbs  independent pseudo-random texels.
+ * Both count 4 bytes per load, are timed with four and with eight loads in
+ * flight per thread (the faster is reported, its depth in *_ilp), and take
+ * the best of `reps` timed launches (CUDA events) after one warm-up.
+ * k <= 256, sides <= 16384. */
 typedef struct ts_gather_peak {
   double patch_gbs, random_gbs;
   double table_bytes;
   uint32_t threads;
   float patch_ms, random_ms;
+  int32_t patch_ilp, random_ilp;
 } ts_gather_peak;
 int ts_measure_gather_peak(int32_t device, uint32_t width, uint32_t height, uint32_t k, int32_t reps,
                            ts_gather_peak *out);

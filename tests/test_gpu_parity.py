@@ -237,3 +237,25 @@ def test_gpu_matches_golden_fixture(ts, path):
     ref = {k: d["out_" + k] for k in KEYS}
     ref["evals"] = int(d["out_evals"])
     assert_same(got, ref, os.path.basename(path))
+
+
+@pytest.mark.parametrize("case", ["translucent", "translucent_guided", "tiny_levels"])
+def test_alpha_channel_cost_paths(ts, oracle, wl, case):
+    """The cost loops skip the alpha term only when every texel a run can
+    compare has alpha 255 (its term is then LUT[0] = 0).  Examples or guides
+    with other alpha values, and pyramids with an all-zero level (a
+    downscale with a zero side), take the four-channel loop; both must
+    match the oracle."""
+    rng = np.random.default_rng(17)
+    if case == "tiny_levels":
+        spec = wl.config0(out=32, ex=12)  # 12 >> 4 == 0: the coarsest level is all zeros
+        spec["params"]["backtrack_stages"] = 5
+    elif case == "translucent":
+        spec = wl.config0(out=40, ex=24)
+        spec["examples"][0]["image"][..., 3] = rng.integers(0, 256, (24, 24), dtype=np.uint8)
+    else:
+        spec = wl.config2(out=48, ex=24)
+        g = spec["examples"][0]["guide"]
+        g[..., 3] = rng.integers(200, 256, g.shape[:2], dtype=np.uint8)
+    got, ref = run_both(ts, oracle, spec)
+    assert_same(got, ref, case)

@@ -140,7 +140,8 @@ _BATCH_FILLER = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p)
 
 class _GatherPeak(C.Structure):
     _fields_ = [("patch_gbs", C.c_double), ("random_gbs", C.c_double), ("table_bytes", C.c_double),
-                ("threads", C.c_uint32), ("patch_ms", C.c_float), ("random_ms", C.c_float)]
+                ("threads", C.c_uint32), ("patch_ms", C.c_float), ("random_ms", C.c_float),
+                ("patch_ilp", C.c_int32), ("random_ilp", C.c_int32)]
 
 
 # every function tsgpu.h declares: name -> (restype, argtypes)

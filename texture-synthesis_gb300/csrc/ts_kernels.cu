@@ -54,6 +54,7 @@ constexpr int kWalkWarps = 8;
 constexpr int kExhThreads = 256;
 constexpr int kTeamThreads = 128;
 constexpr int kTeamFullThreads = 256;  // the full-evaluation form: batches of at most ~1000 items
+constexpr int kStepWideThreads = 512;  // the fused small-step kernel on steps of at most one item per SM
 constexpr int kExhCap = 2048;      // keys kept by the exhaustive k-NN at the cut distance
 constexpr int kExhAllKeys = 8192;  // keys the exhaustive k-NN sorts in shared memory directly
 constexpr int kExhSortAll = 256;   // at most this many keys are sorted without a select
@@ -376,7 +377,7 @@ __device__ __forceinline__ double mean_chain(const double *d, uint32_t n) {
 
 struct ExhShared {
   double dist[256];  // the item's neighbour distances, when the kernel also computes the mean
-  double wsum[kExhThreads / 32];  // per-warp exact distance sums (SessionDev::exact_sum)
+  double wsum[16];  // per-warp exact distance sums (SessionDev::exact_sum), up to 512 threads
   int32_t nbo[256];  // and their offsets
   uint32_t hist[256];
   unsigned long long keys[kExhCap];
@@ -934,13 +935,25 @@ __device__ __forceinline__ uint32_t texel(const uint32_t *lv, const MapDesc &md,
 
 // Sum of the four channel LUT terms in channel order, starting from acc.
 // The byte offsets of the four entries come straight from the packed
-// differences (d >> (8c - 2)) & 0x3fc.
+// differences (d >> (8c - 2)) & 0x3fc.  kOpaque (StageDev::opaque): the
+// alpha difference is always 0 and its term +-0, which leaves the sum as it
+// is, so only the colour channels are looked up.
+template <bool kOpaque = false>
 __device__ __forceinline__ float lut4(const float *lut, uint32_t d, float acc) {
   const char *lb = (const char *)lut;
   acc = __fadd_rn(acc, *(const float *)(lb + ((d << 2) & 0x3fcu)));
   acc = __fadd_rn(acc, *(const float *)(lb + ((d >> 6) & 0x3fcu)));
   acc = __fadd_rn(acc, *(const float *)(lb + ((d >> 14) & 0x3fcu)));
-  acc = __fadd_rn(acc, *(const float *)(lb + ((d >> 22) & 0x3fcu)));
+  if (!kOpaque) acc = __fadd_rn(acc, *(const float *)(lb + ((d >> 22) & 0x3fcu)));
+  return acc;
+}
+// The same with the stage's flag at run time (the alpha lookup predicated).
+__device__ __forceinline__ float lut4r(const float *lut, uint32_t d, float acc, int opaque) {
+  const char *lb = (const char *)lut;
+  acc = __fadd_rn(acc, *(const float *)(lb + ((d << 2) & 0x3fcu)));
+  acc = __fadd_rn(acc, *(const float *)(lb + ((d >> 6) & 0x3fcu)));
+  acc = __fadd_rn(acc, *(const float *)(lb + ((d >> 14) & 0x3fcu)));
+  if (!opaque) acc = __fadd_rn(acc, *(const float *)(lb + ((d >> 22) & 0x3fcu)));
   return acc;
 }
 
@@ -996,8 +1009,8 @@ __device__ __forceinline__ bool candidate_cost(const SessionDev &s, const StageD
 
 // The same on the padded images, for items whose neighbour offsets all lie
 // within kPad: no bounds checks, gathers issued four neighbours ahead.
-template <bool kGuided>
-__device__ __forceinline__ bool candidate_cost_padded(const SessionDev &s, const StageDev &st, const WarpSmem &w,
+template <bool kGuided, bool kOpaque>
+__device__ __forceinline__ bool candidate_cost_padded_v(const SessionDev &s, const StageDev &st, const WarpSmem &w,
                                                       const float *lc, const float *lg, uint32_t nk, uint32_t cxy,
                                                       uint32_t aux, float bound, float &out) {
   const uint32_t map = aux & 0x7fffu;
@@ -1021,8 +1034,8 @@ __device__ __forceinline__ bool candidate_cost_padded(const SessionDev &s, const
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      float nps = lut4(lc, __vabsdiffu4(nr[u].y, t[u]), 0.0f);
-      if (kGuided) nps = lut4(lg, __vabsdiffu4(nr[u].z, gt[u]), nps);
+      float nps = lut4<kOpaque>(lc, __vabsdiffu4(nr[u].y, t[u]), 0.0f);
+      if (kGuided) nps = lut4<kOpaque>(lg, __vabsdiffu4(nr[u].z, gt[u]), nps);
       score = __fadd_rn(score, __fmul_rn(nps, __uint_as_float(nr[u].w)));
     }
     if (score >= bound) return false;
@@ -1030,13 +1043,22 @@ __device__ __forceinline__ bool candidate_cost_padded(const SessionDev &s, const
   for (; j < nk; ++j) {
     const uint4 nr = w.nbr[j];
     const int lin = sg * w.lin[j];
-    float nps = lut4(lc, __vabsdiffu4(nr.y, __ldg(base + lin)), 0.0f);
-    if (kGuided) nps = lut4(lg, __vabsdiffu4(nr.z, __ldg(gbase + lin)), nps);
+    float nps = lut4<kOpaque>(lc, __vabsdiffu4(nr.y, __ldg(base + lin)), 0.0f);
+    if (kGuided) nps = lut4<kOpaque>(lg, __vabsdiffu4(nr.z, __ldg(gbase + lin)), nps);
     score = __fadd_rn(score, __fmul_rn(nps, __uint_as_float(nr.w)));
   }
   if (score >= bound) return false;
   out = score;
   return true;
+}
+
+// The loop in two versions, chosen per stage (a uniform branch).
+template <bool kGuided>
+__device__ __forceinline__ bool candidate_cost_padded(const SessionDev &s, const StageDev &st, const WarpSmem &w,
+                                                      const float *lc, const float *lg, uint32_t nk, uint32_t cxy,
+                                                      uint32_t aux, float bound, float &out) {
+  if (st.opaque) return candidate_cost_padded_v<kGuided, true>(s, st, w, lc, lg, nk, cxy, aux, bound, out);
+  return candidate_cost_padded_v<kGuided, false>(s, st, w, lc, lg, nk, cxy, aux, bound, out);
 }
 
 // Per-neighbour set-up of an item: weight (find_best_match, ms.rs:1198-1203,
@@ -1588,8 +1610,8 @@ __device__ __forceinline__ void resolve_team_body(const SessionDev &s, const Sta
         for (int u = 0; u < 8; ++u) {
           if (ii[u] < total) {
             const uint4 nr = w.nbr[jj[u]];
-            float nps = lut4(lc, __vabsdiffu4(nr.y, tx[u]), 0.0f);
-            if (s.guided) nps = lut4(lg, __vabsdiffu4(nr.z, gx[u]), nps);
+            float nps = lut4r(lc, __vabsdiffu4(nr.y, tx[u]), 0.0f, st.opaque);
+            if (s.guided) nps = lut4r(lg, __vabsdiffu4(nr.z, gx[u]), nps, st.opaque);
             term[ii[u]] = __fmul_rn(nps, __uint_as_float(nr.w));
           }
         }
@@ -2049,9 +2071,18 @@ __global__ void k_random_candidates_multi(MultiLaunch ml) {
   random_candidates_body(*v.s, v.d->rc, v.vb);
 }
 
+// The commit of a pending batch of redo items, spread over the launch's
+// threads (PendingCommit).
+__device__ __forceinline__ void pending_commit(const SessionDev &s, const PendingCommit &pc) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pc.n; i += gridDim.x * blockDim.x)
+    commit_item(s, pc.st, pc.b, i, pc.b.res[i]);
+}
+
 template <bool kWin>
-__global__ void __launch_bounds__(kWalkWarps *kWarp, 4) k_knn_walk(SessionDev s, StageDev st, BatchDev b) {
+__global__ void __launch_bounds__(kWalkWarps *kWarp, 4)
+    k_knn_walk(SessionDev s, StageDev st, BatchDev b, const __grid_constant__ PendingCommit pc) {
   pdl_enter();
+  if (pc.n) pending_commit(s, pc);
   knn_walk_body<kWin>(s, st, b, blockIdx.x, gridDim.x);
 }
 __global__ void __launch_bounds__(kWalkWarps *kWarp, 4) k_knn_walk_multi(MultiLaunch ml) {
@@ -2061,9 +2092,10 @@ __global__ void __launch_bounds__(kWalkWarps *kWarp, 4) k_knn_walk_multi(MultiLa
 }
 
 __global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive(SessionDev s, StageDev st, BatchDev b, uint32_t cap,
-                                                                 int all_items) {
+                                                                 int all_items,
+                                                                 const __grid_constant__ PendingCommit pc) {
   pdl_enter();
-  pdl_enter();
+  if (pc.n) pending_commit(s, pc);
   knn_exhaustive_body(s, st, b, all_items, cap, blockIdx.x, gridDim.x);
 }
 __global__ void __launch_bounds__(kExhThreads) k_knn_exhaustive_multi(MultiLaunch ml) {
@@ -2193,15 +2225,17 @@ __global__ void __launch_bounds__(T) k_resolve_team_multi(MultiLaunch ml) {
 // occupancy, mirror and cell records of those pixels; this k-NN reads the
 // first n_res points and their mirror bits only (the cell grid is not
 // searched here; a key buffer overflow rescans the points).
-constexpr int kStepSetupThreads = kTeamFullThreads - kWarp;  // warps 1..7
-
+// Barrier of the set-up warps (all but warp 0): TS threads.
+template <int TS>
 __device__ __forceinline__ void setup_bar() {
-  asm volatile("bar.sync 1, %0;" ::"n"(kStepSetupThreads) : "memory");
+  asm volatile("bar.sync 1, %0;" ::"n"(TS) : "memory");
 }
 
-__global__ void __launch_bounds__(kTeamFullThreads) k_step_team_full(SessionDev s, StageDev st, BatchDev b,
-                                                                      uint32_t cap) {
-  constexpr int T = kTeamFullThreads, NW = T / kWarp, TS = kStepSetupThreads;
+// T = 256, or 512 for steps of at most one item per SM, where the extra
+// warps shorten each item's latency-bound k-NN and gathers.
+template <int T>
+__global__ void __launch_bounds__(T) k_step_team_full(SessionDev s, StageDev st, BatchDev b, uint32_t cap) {
+  constexpr int NW = T / kWarp, TS = T - kWarp;
   __shared__ ExhShared sh;
   __shared__ double tab[64];
   __shared__ float tab_ff[128];
@@ -2271,7 +2305,7 @@ __global__ void __launch_bounds__(kTeamFullThreads) k_step_team_full(SessionDev 
         if (j < nk) valid = neighbour_records(s, st, px, py, j, sh.nbo[j], 0.0f, w, cxy, aux, maxoff, bad_map);
         const uint32_t bal = __ballot_sync(0xffffffffu, valid);
         if (lane == 0) wcnt[warp] = __popc(bal);
-        setup_bar();
+        setup_bar<TS>();
         uint32_t base = ncoh, total = 0;
 #pragma unroll
         for (int i = 1; i < NW; ++i) {
@@ -2284,7 +2318,7 @@ __global__ void __launch_bounds__(kTeamFullThreads) k_step_team_full(SessionDev 
           w.caux[slot] = aux;
         }
         ncoh += total;
-        setup_bar();
+        setup_bar<TS>();
       }
 #pragma unroll
       for (int u = 0; u < kLutPer; ++u) {
@@ -2301,7 +2335,7 @@ __global__ void __launch_bounds__(kTeamFullThreads) k_step_team_full(SessionDev 
         w.caux[ncoh + q] = v.y | kAuxNeg | (q << 16);
       }
       if (t == 0) sh_ncoh = ncoh;
-      setup_bar();
+      setup_bar<TS>();
       if (!(sh_flags & 2) && !st.slow_lut) {
         // every candidate's LUT sums nps(c, j), before the weights exist
         const uint32_t nc = ncoh + s.m, total = nc * nk;
@@ -2314,7 +2348,7 @@ __global__ void __launch_bounds__(kTeamFullThreads) k_step_team_full(SessionDev 
                                            (unsigned long long)((cxy >> 16) + kPad) * md.pw + ((cxy & 0xffffu) + kPad);
             cb[c] = off | ((aux & kAuxNeg) ? (1ull << 63) : 0ull);
           }
-          setup_bar();
+          setup_bar<TS>();
           constexpr int kRound = 16;  // gathers in flight per thread
           for (uint32_t i0 = t; i0 < total; i0 += kRound * TS) {
             uint32_t tx[kRound], gx[kRound], ii[kRound], jj[kRound];
@@ -2336,8 +2370,8 @@ __global__ void __launch_bounds__(kTeamFullThreads) k_step_team_full(SessionDev 
             for (int u = 0; u < kRound; ++u) {
               if (ii[u] < total) {
                 const uint4 nr = w.nbr[jj[u]];
-                float nps = lut4(lc, __vabsdiffu4(nr.y, tx[u]), 0.0f);
-                if (s.guided) nps = lut4(lg, __vabsdiffu4(nr.z, gx[u]), nps);
+                float nps = lut4r(lc, __vabsdiffu4(nr.y, tx[u]), 0.0f, st.opaque);
+                if (s.guided) nps = lut4r(lg, __vabsdiffu4(nr.z, gx[u]), nps, st.opaque);
                 term[ii[u]] = nps;
               }
             }
@@ -2535,7 +2569,9 @@ cudaError_t configure_kernels(uint32_t k, uint32_t m) {
   if (fsm <= kTeamFullMaxSmem) {
     e = raise_smem(k_resolve_team<kTeamFullThreads, true>, fsm);
     if (e != cudaSuccess) return e;
-    return raise_smem(k_step_team_full, std::max<size_t>(fsm, (size_t)kExhAllKeys * 8));
+    e = raise_smem(k_step_team_full<kTeamFullThreads>, std::max<size_t>(fsm, (size_t)kExhAllKeys * 8));
+    if (e != cudaSuccess) return e;
+    return raise_smem(k_step_team_full<kStepWideThreads>, std::max<size_t>(fsm, (size_t)kExhAllKeys * 8));
   }
   return cudaSuccess;
 }
@@ -2634,13 +2670,15 @@ void launch_random_candidates(const SessionDev &s, const StageDev &st, cudaStrea
   launch_pdl(k_random_candidates, cdiv(st.n_items, 128), 128, 0, stream, s, st);
 }
 
-void launch_knn_walk(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
+void launch_knn_walk(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream,
+                     const PendingCommit &pc) {
   const uint32_t n = b.i1 - b.i0;
-  if (n == 0) return;
+  if (n == 0 && pc.n == 0) return;
+  const uint32_t grid = std::max(cdiv(n, kWalkWarps), cdiv(pc.n, kWalkWarps * kWarp));
   if (b.walk_window)
-    launch_pdl(k_knn_walk<true>, cdiv(n, kWalkWarps), kWalkWarps * kWarp, kWalkWinBytes, stream, s, st, b);
+    launch_pdl(k_knn_walk<true>, grid, kWalkWarps * kWarp, kWalkWinBytes, stream, s, st, b, pc);
   else
-    launch_pdl(k_knn_walk<false>, cdiv(n, kWalkWarps), kWalkWarps * kWarp, 0, stream, s, st, b);
+    launch_pdl(k_knn_walk<false>, grid, kWalkWarps * kWarp, 0, stream, s, st, b, pc);
 }
 
 uint32_t exh_key_cap(const SessionDev &s, const BatchDev &b) {
@@ -2652,12 +2690,13 @@ uint32_t exh_key_cap(const SessionDev &s, const BatchDev &b) {
 }
 
 void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchDev &b, bool all_items,
-                           cudaStream_t stream) {
+                           cudaStream_t stream, const PendingCommit &pc) {
   const uint32_t n = b.i1 - b.i0;
-  if (n == 0) return;
-  const uint32_t grid = n < 608u ? n : 608u;  // 152 SMs x 4 CTAs, grid-stride beyond
+  if (n == 0 && pc.n == 0) return;
+  uint32_t grid = n < 608u ? n : 608u;  // 152 SMs x 4 CTAs, grid-stride beyond
+  grid = std::max(grid, std::min(608u, cdiv(pc.n, kExhThreads)));
   const uint32_t cap = exh_key_cap(s, b);
-  launch_pdl(k_knn_exhaustive, grid, kExhThreads, (size_t)cap * 8, stream, s, st, b, cap, all_items ? 1 : 0);
+  launch_pdl(k_knn_exhaustive, grid, kExhThreads, (size_t)cap * 8, stream, s, st, b, cap, all_items ? 1 : 0, pc);
 }
 
 void launch_mean(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
@@ -2694,7 +2733,10 @@ void launch_step_team_full(const SessionDev &s, const StageDev &st, const BatchD
   const uint32_t grid = n < 608u ? n : 608u;
   const uint32_t cap = exh_key_cap(s, b);
   const size_t smem = std::max<size_t>((size_t)cap * 8, team_full_smem_bytes(s.k, s.m));
-  launch_pdl(k_step_team_full, grid, kTeamFullThreads, smem, stream, s, st, b, cap);
+  if (n <= 152u)  // at most one item per SM of a GB300
+    launch_pdl(k_step_team_full<kStepWideThreads>, grid, kStepWideThreads, smem, stream, s, st, b, cap);
+  else
+    launch_pdl(k_step_team_full<kTeamFullThreads>, grid, kTeamFullThreads, smem, stream, s, st, b, cap);
 }
 
 void launch_commit(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {

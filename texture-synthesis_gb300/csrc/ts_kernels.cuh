@@ -108,6 +108,10 @@ constexpr int kKnnTabRadius = 36;
 struct StageDev {
   uint32_t level;
   int slow_lut;            // LUT holds a non-finite value: exact sequential argmin
+  // Every texel the cost loop can compare has alpha 255 and both LUTs hold
+  // +-0 at |a - b| = 0: the alpha channel's term adds +-0 to a partial sum,
+  // which leaves it unchanged, so the fast cost loops skip it
+  int opaque;
   const float *lut;        // [2][256]: content, guide
   uint64_t stage_seed;
   const uint32_t *items;   // item -> pixel for this stage
@@ -202,11 +206,23 @@ bool team_full_fits(uint32_t k, uint32_t m);
 
 // Launchers (stream-ordered, no synchronisation).
 void launch_random_candidates(const SessionDev &s, const StageDev &st, cudaStream_t stream);
-void launch_knn_walk(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
+// The commit of an earlier step that a k-NN launch makes before its own
+// work (n = 0: none).  Only for batches of redo items: their commit writes
+// colour, state and the eval count, which the k-NN kernels never read, and
+// appends nothing to the resolved list, bitmap or cell counts, which they
+// do read.
+struct PendingCommit {
+  StageDev st;
+  BatchDev b;
+  uint32_t n;
+};
+
+void launch_knn_walk(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream,
+                     const PendingCommit &pc = PendingCommit{});
 // all_items: every item of the batch (and the mean too); otherwise the items
 // the walk left in fb_list.
 void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchDev &b, bool all_items,
-                           cudaStream_t stream);
+                           cudaStream_t stream, const PendingCommit &pc = PendingCommit{});
 void launch_mean(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
 void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
 // One CTA per item; `full` scores every candidate completely (lowest latency,

@@ -10,10 +10,12 @@
 //
 //   patch   each thread takes a pseudo-random centre in the table and reads
 //           the texels at centre + offset_j for the k offsets nearest the
-//           origin, (d^2, dy, dx) order, four loads in flight (the cost
-//           loop's access shape, without its LUT work and early exit);
-//   random  each thread reads independent pseudo-random texels, four in
-//           flight (no spatial locality: the L2 gather rate).
+//           origin, (d^2, dy, dx) order, four or eight loads in flight
+//           (the cost loop's access shape, without its LUT work and early
+//           exit);
+//   random  each thread reads independent pseudo-random texels, four or
+//           eight in flight (no spatial locality: the L2 gather rate).
+// Each is timed at both depths and the faster is kept.
 //
 // The table is allocated and filled here, sized by the caller (the example
 // level of the workload being measured).  Measurement only: no counterpart
@@ -41,6 +43,7 @@ __device__ __forceinline__ uint32_t mix32(uint32_t v) {
   return v;
 }
 
+template <int ILP>
 __global__ void __launch_bounds__(kProbeThreads) k_gather_patch(const uint32_t *table, uint32_t pitch, uint32_t cw,
                                                                 uint32_t ch, const int32_t *lin_g, uint32_t k,
                                                                 uint32_t iters, uint32_t *sink) {
@@ -54,31 +57,32 @@ __global__ void __launch_bounds__(kProbeThreads) k_gather_patch(const uint32_t *
     const uint32_t cx = kProbeRadius + (h & 0xffffu) % cw, cy = kProbeRadius + (h >> 16) % ch;
     const uint32_t *base = table + (size_t)cy * pitch + cx;
     uint32_t j = 0;
-    for (; j + 4 <= k; j += 4) {
-      uint32_t t[4];
+    for (; j + ILP <= k; j += ILP) {
+      uint32_t t[ILP];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) t[u] = __ldg(base + lin[j + u]);
+      for (int u = 0; u < ILP; ++u) t[u] = __ldg(base + lin[j + u]);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) acc += t[u];
+      for (int u = 0; u < ILP; ++u) acc += t[u];
     }
     for (; j < k; ++j) acc += __ldg(base + lin[j]);
   }
   sink[tid] = acc;
 }
 
+template <int ILP>
 __global__ void __launch_bounds__(kProbeThreads) k_gather_random(const uint32_t *table, uint32_t words,
                                                                  uint32_t loads, uint32_t *sink) {
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t acc = 0, h = mix32(tid + 0x51ed270bu);
-  for (uint32_t i = 0; i < loads; i += 4) {
-    uint32_t t[4];
+  for (uint32_t i = 0; i < loads; i += ILP) {
+    uint32_t t[ILP];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < ILP; ++u) {
       h = mix32(h + (uint32_t)u);
       t[u] = __ldg(table + h % words);
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) acc += t[u];
+    for (int u = 0; u < ILP; ++u) acc += t[u];
   }
   sink[tid] = acc;
 }
@@ -127,7 +131,7 @@ extern "C" int ts_measure_gather_peak(int32_t device, uint32_t width, uint32_t h
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return TS_ERR_CUDA;
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather_patch, kProbeThreads, 0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather_patch<8>, kProbeThreads, 0) != cudaSuccess)
     return TS_ERR_CUDA;
   const uint32_t blocks = (uint32_t)(sms * std::max(per_sm, 1));
   const uint32_t threads = blocks * kProbeThreads;
@@ -148,7 +152,7 @@ extern "C" int ts_measure_gather_peak(int32_t device, uint32_t width, uint32_t h
   float patch_ms = 0.0f, rand_ms = 0.0f;
   // a launch reads about 2 GB of texels: long enough to time, short enough to repeat
   const uint32_t iters = std::max(1u, (uint32_t)(2e9 / 4.0 / k / threads));
-  const uint32_t loads = std::max(4u, (uint32_t)(1e9 / 4.0 / threads) & ~3u);
+  const uint32_t loads = std::max(8u, (uint32_t)(1e9 / 4.0 / threads) & ~7u);
   do {
     if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&table, words * 4) != cudaSuccess || cudaMalloc(&sink, (size_t)threads * 4) != cudaSuccess ||
@@ -161,13 +165,23 @@ extern "C" int ts_measure_gather_peak(int32_t device, uint32_t width, uint32_t h
       rc = TS_ERR_CUDA;
       break;
     }
-    auto patch = [&] { k_gather_patch<<<blocks, kProbeThreads, 0, st>>>(table, pitch, width, height, lin, k, iters, sink); };
-    auto rnd = [&] { k_gather_random<<<blocks, kProbeThreads, 0, st>>>(table, (uint32_t)words, loads, sink); };
-    if (best_ms(patch, std::max(1, reps), st, patch_ms) != cudaSuccess ||
-        best_ms(rnd, std::max(1, reps), st, rand_ms) != cudaSuccess) {
+    // four and eight loads in flight per thread; the faster of the two
+    auto patch4 = [&] { k_gather_patch<4><<<blocks, kProbeThreads, 0, st>>>(table, pitch, width, height, lin, k, iters, sink); };
+    auto patch8 = [&] { k_gather_patch<8><<<blocks, kProbeThreads, 0, st>>>(table, pitch, width, height, lin, k, iters, sink); };
+    auto rnd4 = [&] { k_gather_random<4><<<blocks, kProbeThreads, 0, st>>>(table, (uint32_t)words, loads, sink); };
+    auto rnd8 = [&] { k_gather_random<8><<<blocks, kProbeThreads, 0, st>>>(table, (uint32_t)words, loads, sink); };
+    float p4 = 0, p8 = 0, r4 = 0, r8 = 0;
+    if (best_ms(patch4, std::max(1, reps), st, p4) != cudaSuccess ||
+        best_ms(patch8, std::max(1, reps), st, p8) != cudaSuccess ||
+        best_ms(rnd4, std::max(1, reps), st, r4) != cudaSuccess ||
+        best_ms(rnd8, std::max(1, reps), st, r8) != cudaSuccess) {
       rc = TS_ERR_CUDA;
       break;
     }
+    patch_ms = std::min(p4, p8);
+    rand_ms = std::min(r4, r8);
+    out->patch_ilp = p8 < p4 ? 8 : 4;
+    out->random_ilp = r8 < r4 ? 8 : 4;
   } while (false);
   if (st) cudaStreamSynchronize(st);
   cudaFree(table);

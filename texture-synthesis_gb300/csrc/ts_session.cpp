@@ -21,6 +21,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <functional>
 #include <mutex>
 #include <unordered_map>
 #include <memory>
@@ -601,6 +602,10 @@ struct ts_session {
   DevBuf<uint8_t> masks;
   DevBuf<MapDesc> d_maps;
   DevBuf<GuideDesc> d_gdesc;
+  // every texel a run can compare has alpha 255: all examples (ignored ones
+  // too, random init copies them), guides and the target guide are opaque,
+  // and no pyramid level is a zero image (a downscale with a zero side)
+  bool opaque = false;
   EventHandle ready;  // recorded after build()'s device work; runs wait for it
   bool consumed = false;
   std::string err;
@@ -1064,6 +1069,22 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
       s->filtered.push_back(e);
     }
     s->n_maps = (uint32_t)s->maps.size();
+    {
+      // constant alpha 255 stays 255 through the pyramid's resizes (their
+      // weights are normalised, and the u8 result is rounded), unless a
+      // level's downscale has a zero side
+      const uint32_t sh = s->n_levels - 1;
+      auto opaque = [&](const Image &im) {
+        if (sh < 32 && ((im.w >> sh) == 0 || (im.h >> sh) == 0)) return false;
+        for (size_t i = 0; i < (size_t)im.w * im.h; ++i)
+          if (im.px[4 * i + 3] != 255) return false;
+        return true;
+      };
+      bool op = sh < 32;
+      for (uint32_t e = 0; op && e < s->n_ex; ++e) op = opaque(imgs[e]) && (!s->guided || opaque(guides[e]));
+      if (op && s->guided) op = opaque(tg);
+      s->opaque = op;
+    }
     // padded copies share one row pitch, the widest map's, so that a
     // neighbour offset is one texel offset on every map
     uint32_t pitch = 0;
@@ -1287,6 +1308,8 @@ struct RunCtx {
   size_t res_total = 0;                // resolved-list length at the end of the run
   std::vector<uint32_t> unresolved;    // pixels not yet picked (the pick chain's state)
   size_t picked_stages = 0;            // stages whose items are known
+  bool parallel_picks = false;         // draws of large stages on the shared host pool (single-session runs)
+  std::vector<uint64_t> draws;         // a stage's random indices, before the swap-removes
   int32_t x_l = 0, y_b = 0;
   uint64_t dev_bytes = 0;  // device memory run_alloc takes
   // device state
@@ -1559,21 +1582,110 @@ void run_plan(ts_session *s, RunCtx &c) {
 // The pick chain of the next stage (pick_random_unresolved, ms.rs:380-389,
 // redo items first, ms.rs:905-915): fills its items and extends the
 // resolved list with each batch's appended items, in the reference's order.
+// A small pool of host threads shared by every single-session run: it
+// computes the random draws of the large stages of the pick chain.  One job
+// at a time (runs that find it busy compute their draws themselves).
+class DrawPool {
+ public:
+  static DrawPool &get() {
+    static DrawPool *pool = new DrawPool();  // never destroyed: its threads sleep on it until exit
+    return *pool;
+  }
+  // fn(a, b) over [0, n) in chunks of `grain`, on the pool and the caller;
+  // false (nothing done) when another run holds the pool
+  bool run(size_t n, size_t grain, const std::function<void(size_t, size_t)> &fn) {
+    std::unique_lock<std::mutex> job(job_mu_, std::try_to_lock);
+    if (!job.owns_lock() || workers_.empty()) return false;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      fn_ = &fn;
+      n_ = n;
+      grain_ = grain;
+      next_ = 0;
+      left_ = (n + grain - 1) / grain;
+    }
+    cv_.notify_all();
+    work();
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return left_ == 0; });
+    fn_ = nullptr;
+    return true;
+  }
+
+ private:
+  DrawPool() {
+    const unsigned hc = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned nw = std::min(7u, hc > 2 ? hc - 2 : 0u);
+    for (unsigned i = 0; i < nw; ++i) workers_.emplace_back([this] { loop(); });
+    for (auto &t : workers_) t.detach();  // they sleep until the process exits
+  }
+  void loop() {
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return fn_ != nullptr && next_ * grain_ < n_; });
+      }
+      work();
+    }
+  }
+  // Chunks are claimed under the mutex, so a claim always belongs to the
+  // job that is current when it is made.
+  void work() {
+    for (;;) {
+      const std::function<void(size_t, size_t)> *fn;
+      size_t a, b;
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (!fn_ || next_ * grain_ >= n_) return;
+        fn = fn_;
+        a = next_ * grain_;
+        b = std::min(n_, a + grain_);
+        ++next_;
+      }
+      (*fn)(a, b);
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--left_ == 0) done_cv_.notify_all();
+    }
+  }
+  std::mutex job_mu_, mu_;
+  std::condition_variable cv_, done_cv_;
+  std::vector<std::thread> workers_;
+  const std::function<void(size_t, size_t)> *fn_ = nullptr;
+  size_t n_ = 0, grain_ = 1, next_ = 0, left_ = 0;
+};
+
+// pick_random_unresolved (ms.rs:380-389) for a stage's items: redo item i
+// is resolved[i + locked]; new item i swap-removes
+// Pcg32::seed_from_u64(seed + i).gen_range(0..len) from the unresolved list.
+// len is known in advance (the list shrinks by one per new item), so the
+// draws are independent of one another and of the list; only the
+// swap-removes that consume them run in order.
 void run_pick(RunCtx &c) {
   const StagePlan &sp = c.plan[c.picked_stages++];
   std::vector<uint32_t> &unresolved = c.unresolved;
   uint32_t *it = c.items.data() + sp.items_off;
-  for (uint32_t i = 0; i < sp.n_items; ++i) {
-    if (i < sp.redo) {
-      it[i] = c.resolved[i + c.locked];
-    } else {
-      Pcg32 r = pcg_from_u64(sp.seed + (uint64_t)i);
-      const uint64_t idx = gen_range_u64(r, unresolved.size());
-      it[i] = unresolved[idx];
-      unresolved[idx] = unresolved.back();
-      unresolved.pop_back();
+  const uint32_t redo = std::min(sp.redo, sp.n_items);
+  for (uint32_t i = 0; i < redo; ++i) it[i] = c.resolved[i + c.locked];
+  const size_t n_new = sp.n_items - redo, len0 = unresolved.size();
+  if (n_new > len0) throw Failure{TS_ERR_INVALID_RANGE, "more new items than unresolved pixels"};
+  c.draws.resize(n_new);
+  uint64_t *dr = c.draws.data();
+  const std::function<void(size_t, size_t)> draw = [&](size_t a, size_t b) {
+    for (size_t q = a; q < b; ++q) {
+      Pcg32 r = pcg_from_u64(sp.seed + (uint64_t)(redo + q));
+      dr[q] = gen_range_u64(r, len0 - q);
     }
+  };
+  constexpr size_t kGrain = 8192;
+  if (!(c.parallel_picks && n_new >= 4 * kGrain && DrawPool::get().run(n_new, kGrain, draw))) draw(0, n_new);
+  uint32_t *un = unresolved.data();
+  size_t len = len0;
+  for (size_t q = 0; q < n_new; ++q) {
+    const uint64_t idx = dr[q];
+    it[redo + q] = un[idx];
+    un[idx] = un[--len];
   }
+  unresolved.resize(len);
   for (const BatchPlan &bp : sp.batches)
     for (uint32_t t = bp.append_from; t < bp.i1; ++t) c.resolved.push_back(it[t]);
 }
@@ -1758,6 +1870,7 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
     sdv.level = sp.level;
     sdv.slow_lut = sp.slow_lut ? 1 : 0;
     sdv.lut = c.d_lut.p + si * 512;
+    sdv.opaque = (s->opaque && !sp.slow_lut && c.luts[si * 512] == 0.0f && c.luts[si * 512 + 256] == 0.0f) ? 1 : 0;
     sdv.stage_seed = sp.seed;
     sdv.items = c.d_items.p + sp.items_off;
     sdv.redo = sp.redo;
@@ -1852,10 +1965,30 @@ void run_upload(RunCtx &c, cudaStream_t st) {
     CUDA_TRY(cudaMemcpyAsync(c.d_items.p, c.items.data(), c.items.size() * 4, cudaMemcpyHostToDevice, st));
 }
 
+// Whether the commit of step `stp` can be left to the first k-NN launch of
+// `next`, the following step of the same stage: stp holds only redo items
+// (nothing is appended to the resolved list, the bitmap or the cell
+// counts), and next starts with a walk or an exhaustive k-NN launch, not
+// the fused small-step kernel, which reads colours.
+bool can_defer_commit(const RunCtx &c, const Step &stp, const Step *next) {
+  if (!stp.batch || stp.bd.fused_commit || c.k == 0 || stp.bd.append_from < stp.bd.i1) return false;
+  if (!next || !next->batch || next->ls || next->stage != stp.stage) return false;
+  return !(next->exhaustive && next->resolve == kPhaseTeamFull && team_full_fits(c.sd.k, c.sd.m));
+}
+
 // The launches of one step of one session, with the single-session
-// kernels (parameters by value).
-void enqueue_step(RunCtx &c, const Step &stp, cudaStream_t st, LaunchTimer &lt) {
+// kernels (parameters by value).  pending: an earlier step whose commit
+// this step's first k-NN launch makes; defer: leave this step's commit to
+// the next step (can_defer_commit).
+void enqueue_step(RunCtx &c, const Step &stp, cudaStream_t st, LaunchTimer &lt, const Step *pending = nullptr,
+                  bool defer = false) {
   const SessionDev &sd = c.sd;
+  PendingCommit pc{};
+  if (pending) {
+    pc.st = pending->st;
+    pc.b = pending->bd;
+    pc.n = pending->bd.i1 - pending->bd.i0;
+  }
   if (stp.ls) {
     lt.run(TS_KERNEL_LEVEL_SWITCH, [&] { launch_level_switch(sd, stp.ls_level, stp.ls_n_res, st); });
     ++c.launches;
@@ -1882,10 +2015,10 @@ void enqueue_step(RunCtx &c, const Step &stp, cudaStream_t st, LaunchTimer &lt) 
     }
     if (c.k > 0) {
       if (stp.exhaustive) {
-        lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, stp.st, stp.bd, true, st); });
+        lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, stp.st, stp.bd, true, st, pc); });
         ++c.launches;
       } else {
-        lt.run(TS_KERNEL_KNN_WALK, [&] { launch_knn_walk(sd, stp.st, stp.bd, st); });
+        lt.run(TS_KERNEL_KNN_WALK, [&] { launch_knn_walk(sd, stp.st, stp.bd, st, pc); });
         lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, stp.st, stp.bd, false, st); });
         c.launches += 2;
       }
@@ -1901,7 +2034,7 @@ void enqueue_step(RunCtx &c, const Step &stp, cudaStream_t st, LaunchTimer &lt) 
     else
       lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve_team(sd, stp.st, stp.bd, stp.resolve == kPhaseTeamFull, st); });
     c.launches += 1;
-    if (!stp.bd.fused_commit) {
+    if (!stp.bd.fused_commit && !defer) {
       lt.run(TS_KERNEL_COMMIT, [&] { launch_commit(sd, stp.st, stp.bd, st); });
       c.launches += 1;
     }
@@ -1916,12 +2049,16 @@ void run_enqueue_plain(RunCtx &c, cudaStream_t st, LaunchTimer &lt, ts_progress_
   for (const StagePlan &sp : c.plan)
     if (stage >= 0 && (&sp - c.plan.data()) < stage) overall_current += sp.n_items;
   std::vector<uint8_t> prog_img;
-  for (const Step &stp : c.steps) {
+  const Step *pending = nullptr;  // a step whose commit the next step's k-NN launch makes
+  for (size_t i = 0; i < c.steps.size(); ++i) {
+    const Step &stp = c.steps[i];
     if (stage >= 0 && stp.stage != stage) continue;
     const StagePlan &sp = c.plan[stp.stage];
     lt.stage = sp.p_stage;
     lt.items = sp.n_items;
-    enqueue_step(c, stp, st, lt);
+    const bool defer = can_defer_commit(c, stp, i + 1 < c.steps.size() ? &c.steps[i + 1] : nullptr);
+    enqueue_step(c, stp, st, lt, pending, defer);
+    pending = defer ? &stp : nullptr;
     if (stp.batch) {
       ++c.batches;
       c.resolves += stp.n;
@@ -2035,6 +2172,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
       return ms;
     };
     c.want_rc_ahead = true;
+    c.parallel_picks = true;
     run_plan(s, c);
     const double plan_ms = lap();
     run_alloc(c, st);
@@ -3188,7 +3326,9 @@ ts_server *ts_server_new(int32_t device, uint64_t hbm_budget_bytes, uint32_t max
   S->driver = std::thread(server_driver, S.get());
   S->completer = std::thread(server_completer, S.get());
   const unsigned hc = std::max(1u, std::thread::hardware_concurrency());
-  for (unsigned i = 0; i < std::min(4u, std::max(1u, hc / 4)); ++i) S->pickers.emplace_back(server_picker, S.get());
+  // half the host threads (at most eight) run pick chains: with many
+  // requests waiting they, not the device, bound the server's throughput
+  for (unsigned i = 0; i < std::min(8u, std::max(1u, hc / 2)); ++i) S->pickers.emplace_back(server_picker, S.get());
   return S.release();
 }
 
