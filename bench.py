@@ -272,7 +272,9 @@ def serve_saturated(ts, reqs, max_active=64, tuning=None):
     srv.close()
     return {"requests": len(reqs), "mpx_s": px / span / 1e6, "span_ms": span * 1e3,
             "p50_ms": _pct(lat, 50) * 1e3, "p99_ms": _pct(lat, 99) * 1e3,
-            "peak_active": st["peak_active"], "ticks": st["ticks"]}
+            "peak_active": st["peak_active"], "ticks": st["ticks"],
+            "driver_ms": {"ticks": st["driver_tick_us"] / 1e3, "ring_wait": st["driver_ring_wait_us"] / 1e3,
+                          "pick_wait": st["driver_pick_wait_us"] / 1e3}}
 
 
 def measure_served(ts, wl, lams=(10, 25, 50, 100, 200), n=256, tuning=None):
@@ -482,9 +484,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--once", action="store_true", help="build and run one session, print its stats (for profilers)")
-    ap.add_argument("--workload", default="remix", choices=["remix", "single", "guided", "batched", "served"],
+    ap.add_argument("--workload", default="remix",
+                    choices=["remix", "single", "guided", "batched", "served", "gather_peak"],
                     help="remix: the headline line (config 1, plus configs 0 and 2, batched and served objects); "
-                         "single / guided: config 0 / config 2 alone")
+                         "single / guided: config 0 / config 2 alone; gather_peak: the gather ceiling alone")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and served objects of the remix line")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -497,6 +500,10 @@ def main():
     importlib.import_module(PKG + ".build").build()
     ts = importlib.import_module(PKG)
     wl = importlib.import_module(PKG + ".workloads")
+    if args.workload == "gather_peak":
+        # the gather ceiling alone, on the remix workload's table (for profilers)
+        print(json.dumps(ts.gather_peak(*padded_level_shape(workload()), 50, reps=3)))
+        return
     if args.workload == "batched":
         if args.once:  # one batched run of the 64-session mix (for profilers)
             b = ts.Batch()

@@ -192,12 +192,21 @@ __device__ __forceinline__ double neighbour_dist_near(const SessionDev &s, int p
 // so it equals 4 * (the list's sum in any order of exact adds), and the mean
 // is that divided by 4n, rounded once, as the reference divides.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double warp_sum_exact(double v) {
+// A neighbour's distance in units of SessionDev::exact_q: an integer (the
+// distances are exact), summed in integers instead of f64 adds.
+__device__ __forceinline__ unsigned long long exact_units(const SessionDev &s, int dx, int dy) {
+  return ((unsigned long long)(uint32_t)(dx * dx) << s.exact_sx) + ((unsigned long long)(uint32_t)(dy * dy) << s.exact_sy);
+}
+__device__ __forceinline__ unsigned long long warp_sum_units(unsigned long long v) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_xor_sync(0xffffffffu, v, o));
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
-__device__ __forceinline__ double exact_mean(double sum, uint32_t n) {
+// The mean from the list's sum in units: below 2^53, so its conversion and
+// the scaling by the power of two exact_q are exact; 4 * that is the
+// reference's in-order sum, divided by 4n and rounded once.
+__device__ __forceinline__ double exact_mean(const SessionDev &s, unsigned long long units, uint32_t n) {
+  const double sum = __dmul_rn(__ull2double_rn(units), s.exact_q);
   return __ddiv_rn(__dmul_rn(4.0, sum), (double)(n * 4u));
 }
 
@@ -330,16 +339,15 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
       // instruction (an f64 instruction costs the same whatever its active
       // lanes, and GB300's f64 pipe is narrow)
       __syncwarp();
-      double part = 0.0;
+      unsigned long long part = 0;
       for (uint32_t j = lane; j < s.k; j += kWarp) {
         const int32_t o = nbo[j];
-        const double d = neighbour_dist_near(s, px, py, off_dx(o), off_dy(o));
-        b.dist[(size_t)j * nb + local] = d;
-        if (s.exact_sum) part = __dadd_rn(part, d);
+        b.dist[(size_t)j * nb + local] = neighbour_dist_near(s, px, py, off_dx(o), off_dy(o));
+        if (s.exact_sum) part += exact_units(s, off_dx(o), off_dy(o));
       }
       if (s.exact_sum) {
-        const double sum = warp_sum_exact(part);
-        if (lane == 0) b.mean[local] = exact_mean(sum, s.k);
+        part = warp_sum_units(part);
+        if (lane == 0) b.mean[local] = exact_mean(s, part, s.k);
       }
     }
     if (lane == 0) {
@@ -377,7 +385,7 @@ __device__ __forceinline__ double mean_chain(const double *d, uint32_t n) {
 
 struct ExhShared {
   double dist[256];  // the item's neighbour distances, when the kernel also computes the mean
-  double wsum[16];  // per-warp exact distance sums (SessionDev::exact_sum), up to 512 threads
+  unsigned long long wsum[16];  // per-warp distance sums in units (SessionDev::exact_sum), up to 512 threads
   int32_t nbo[256];  // and their offsets
   uint32_t hist[256];
   unsigned long long keys[kExhCap];
@@ -831,14 +839,14 @@ __device__ uint32_t knn_exhaustive_item(const SessionDev &s, const StageDev &st,
   int32_t *nbo = b.nbuf + (size_t)local * k;
   const uint32_t nb = b.i1 - b.i0;
   const double x2 = s.xdiv[px + s.xdiv_off], y2 = s.ydiv[py + s.ydiv_off];
-  double part = 0.0;
+  unsigned long long part = 0;
   for (uint32_t i = threadIdx.x; i < nout; i += blockDim.x) {
     const unsigned long long key = sorted[i];
     const int x = (int)(key & 0xffffu) - 32768, y = (int)((key >> 16) & 0xffffu) - 32768;
     nbo[i] = pack_off(x - px, y - py);
     const double d = neighbour_dist(s, px, py, x - px, y - py, x2, y2);
     b.dist[(size_t)i * nb + local] = d;
-    if (s.exact_sum) part = __dadd_rn(part, d);
+    if (s.exact_sum) part += exact_units(s, x - px, y - py);
     if (with_mean) {
       sh.dist[i] = d;
       sh.nbo[i] = pack_off(x - px, y - py);
@@ -846,13 +854,13 @@ __device__ uint32_t knn_exhaustive_item(const SessionDev &s, const StageDev &st,
   }
   if (s.exact_sum && mean_here) {
     // every item of the launch, fallback items included, gets its mean here
-    part = warp_sum_exact(part);
+    part = warp_sum_units(part);
     if ((threadIdx.x & 31) == 0) sh.wsum[threadIdx.x >> 5] = part;
     __syncthreads();
     if (threadIdx.x == 0 && nout > 0) {
-      double sum = 0.0;
-      for (uint32_t w = 0; w < blockDim.x / 32; ++w) sum = __dadd_rn(sum, sh.wsum[w]);
-      b.mean[local] = exact_mean(sum, nout);
+      unsigned long long sum = 0;
+      for (uint32_t w = 0; w < blockDim.x / 32; ++w) sum += sh.wsum[w];
+      b.mean[local] = exact_mean(s, sum, nout);
     }
   } else if (with_mean && mean_here) {
     __syncthreads();
@@ -2267,7 +2275,16 @@ __global__ void __launch_bounds__(T) k_step_team_full(SessionDev s, StageDev st,
       continue;
     }
     if (warp == 0) {
-      if (lane == 0) {
+      if (s.exact_sum) {
+        unsigned long long part = 0;
+        for (uint32_t j = lane; j < nk; j += kWarp) part += exact_units(s, off_dx(sh.nbo[j]), off_dy(sh.nbo[j]));
+        part = warp_sum_units(part);
+        if (lane == 0) {
+          const double mean = exact_mean(s, part, nk);
+          sh_mean = mean;
+          b.mean[local] = mean;
+        }
+      } else if (lane == 0) {
         const double mean = mean_chain(sh.dist, nk);
         sh_mean = mean;
         b.mean[local] = mean;

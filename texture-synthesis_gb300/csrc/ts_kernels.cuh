@@ -88,6 +88,11 @@ struct SessionDev {
   // below 2^53 such units, so the in-order f64 sum (ms.rs:417-421) is exact
   // and any order of exact adds gives its bits (exact_sum_ok on the host)
   int exact_sum;
+  // with exact_sum: a neighbour at integer offset (dx, dy) lies at distance
+  // ((dx^2 << exact_sx) + (dy^2 << exact_sy)) * exact_q, exact_q =
+  // 1 / max(W, H)^2, exact_sx = 2 log2(max(W, H) / W), exact_sy likewise
+  uint32_t exact_sx, exact_sy;
+  double exact_q;
   uint32_t W, H, wpr;  // wpr: 32-bit words per bitmap row
   int tiling;
   int32_t x_l, x_r, y_b, y_t;

@@ -1837,6 +1837,17 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   sd.W = W;
   sd.H = H;
   sd.exact_sum = exact_sum_ok(W, H, k) ? 1 : 0;
+  if (sd.exact_sum) {
+    const uint32_t M = std::max(W, H);
+    auto lg2 = [](uint32_t v) {
+      uint32_t l = 0;
+      while ((1u << l) < v) ++l;
+      return l;
+    };
+    sd.exact_sx = 2 * (lg2(M) - lg2(W));
+    sd.exact_sy = 2 * (lg2(M) - lg2(H));
+    sd.exact_q = std::ldexp(1.0, -2 * (int)lg2(M));
+  }
   sd.wpr = wpr;
   sd.tiling = p.tiling ? 1 : 0;
   sd.x_l = x_l;
@@ -3063,6 +3074,7 @@ void server_driver(ts_server *S) {
     for (ServerReq *r : S->active)
       if (r->c->steps[r->cursor].stage < (int)r->picked.load(std::memory_order_acquire)) ready.push_back(r);
     if (ready.empty()) {
+      const double w0 = host_ms();
       // Wait for a picker (or a new request), re-checking under the mutex:
       // a picker publishes `picked` before it takes the mutex to notify, so
       // no wake-up is lost between the check above and the wait.
@@ -3073,11 +3085,18 @@ void server_driver(ts_server *S) {
           if (r->c->steps[r->cursor].stage < (int)r->picked.load(std::memory_order_acquire)) return true;
         return false;
       });
+      S->stats.driver_pick_wait_us += (uint64_t)((host_ms() - w0) * 1e3);
       continue;
     }
+    const double t_tick0 = host_ms();
     try {
       ts_server::Ring &R = S->ring[ri];
-      if (R.used) CUDA_TRY(cudaEventSynchronize(R.ev));  // the slot's previous tick is done
+      double ring_wait = 0.0;
+      if (R.used) {  // the slot's previous tick is done
+        const double w0 = host_ms();
+        CUDA_TRY(cudaEventSynchronize(R.ev));
+        ring_wait = host_ms() - w0;
+      }
       for (ServerReq *r : ready) {
         // items of the stages picked so far, in stream order before the launches
         RunCtx &c = *r->c;
@@ -3213,6 +3232,8 @@ void server_driver(ts_server *S) {
         std::lock_guard<std::mutex> lk(S->mu);
         S->stats.ticks += 1;
         S->stats.launches += tick_launches;
+        S->stats.driver_ring_wait_us += (uint64_t)(ring_wait * 1e3);
+        S->stats.driver_tick_us += (uint64_t)((host_ms() - t_tick0 - ring_wait) * 1e3);
         for (ServerReq *r : finished) S->completing.push_back(r);
         if (!finished.empty()) S->cv_complete.notify_one();
       }
@@ -3377,7 +3398,7 @@ int ts_server_resolve_team(ts_server *S, uint32_t team_max_items, uint32_t full_
   return TS_OK;
 }
 int ts_server_tuning(ts_server *S, const ts_tuning *t) {
-  if (!t) return TS_ERR_NULL;
+  if (!S || !t) return TS_ERR_NULL;
   return ts_server_resolve_team(S, t->team_max_items, t->team_full_max_items);
 }
 
