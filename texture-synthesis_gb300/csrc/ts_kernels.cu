@@ -202,6 +202,13 @@ __device__ __forceinline__ unsigned long long warp_sum_units(unsigned long long 
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+// A neighbour's distance from its packed offset, for sessions with exact
+// sums: its units, converted (exact below 2^53) and scaled by the power of
+// two exact_q, equal fma(dx, dx, dy * dy) of get_distances_to_k_neighs
+// (ms.rs:405-425) bit for bit.
+__device__ __forceinline__ double exact_dist(const SessionDev &s, int32_t off) {
+  return __dmul_rn(__ull2double_rn(exact_units(s, off_dx(off), off_dy(off))), s.exact_q);
+}
 // The mean from the list's sum in units: below 2^53, so its conversion and
 // the scaling by the power of two exact_q are exact; 4 * that is the
 // reference's in-order sum, divided by 4n and rounded once.
@@ -339,11 +346,15 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
       // instruction (an f64 instruction costs the same whatever its active
       // lanes, and GB300's f64 pipe is narrow)
       __syncwarp();
+      // (sessions with exact sums store no distances: the resolve derives
+      // each one from its offset, exact_dist)
       unsigned long long part = 0;
       for (uint32_t j = lane; j < s.k; j += kWarp) {
         const int32_t o = nbo[j];
-        b.dist[(size_t)j * nb + local] = neighbour_dist_near(s, px, py, off_dx(o), off_dy(o));
-        if (s.exact_sum) part += exact_units(s, off_dx(o), off_dy(o));
+        if (s.exact_sum)
+          part += exact_units(s, off_dx(o), off_dy(o));
+        else
+          b.dist[(size_t)j * nb + local] = neighbour_dist_near(s, px, py, off_dx(o), off_dy(o));
       }
       if (s.exact_sum) {
         part = warp_sum_units(part);
@@ -845,8 +856,10 @@ __device__ uint32_t knn_exhaustive_item(const SessionDev &s, const StageDev &st,
     const int x = (int)(key & 0xffffu) - 32768, y = (int)((key >> 16) & 0xffffu) - 32768;
     nbo[i] = pack_off(x - px, y - py);
     const double d = neighbour_dist(s, px, py, x - px, y - py, x2, y2);
-    b.dist[(size_t)i * nb + local] = d;
-    if (s.exact_sum) part += exact_units(s, x - px, y - py);
+    if (s.exact_sum)
+      part += exact_units(s, x - px, y - py);
+    else
+      b.dist[(size_t)i * nb + local] = d;
     if (with_mean) {
       sh.dist[i] = d;
       sh.nbo[i] = pack_off(x - px, y - py);
@@ -1124,7 +1137,8 @@ __device__ __forceinline__ bool neighbour_setup(const SessionDev &s, const Stage
                                                 double avg, const double *tab, const float *tab_ff,
                                                 const WarpSmem &w, uint32_t &cxy, uint32_t &aux, bool &nan_w,
                                                 int &maxoff, bool &bad_map) {
-  const float wv = neighbour_weight(b.dist[(size_t)j * nb + local], avg, tab, tab_ff);
+  const double d = s.exact_sum ? exact_dist(s, off) : b.dist[(size_t)j * nb + local];
+  const float wv = neighbour_weight(d, avg, tab, tab_ff);
   nan_w |= (wv != wv);
   return neighbour_records<kG>(s, st, px, py, j, off, wv, w, cxy, aux, maxoff, bad_map);
 }
