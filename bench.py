@@ -62,6 +62,13 @@ FALLBACK_HBM_GBS = 6800.0
 # (one pass; ncu flushes the caches before each launch, so this is a
 # cold-cache upper bound of the live traffic).
 RESOLVE_DRAM_BYTES_PER_LAUNCH = 1038.67e6 / 131
+# The load path, measured in the unit both kernels share: 32-byte L1 sectors
+# requested per second by global loads (l1tex__t_sectors_pipe_lsu_mem_global_op_ld.sum
+# / gpu__time_duration.sum).  k_resolve_lean on a 13,124-item step of this
+# workload against ts_measure_gather_peak's patch kernel on this workload's
+# table (profiles/k_resolve_lean_multi_example_512.md and
+# profiles/gather_peak_probe_multi_example_512.md, ncu, one launch each).
+LOAD_PATH_SECTORS_PER_S = {"k_resolve_lean": 123.1e9, "gather_probe": 405.4e9}
 
 
 def _peaks():
@@ -156,6 +163,15 @@ def _tuning_dict(t):
     return {"team_max_items": t.team_max_items, "team_full_max_items": t.team_full_max_items,
             "walk_window_max_items": t.walk_window_max_items, "trials": t.trials,
             "tuned_ms": t.gpu_ms, "default_ms": t.default_gpu_ms}
+
+
+_T0 = time.perf_counter()
+
+
+def _progress(msg):
+    """One line on stderr per finished part of the run (stdout keeps the
+    JSON line alone)."""
+    print("[bench %7.1f s] %s" % (time.perf_counter() - _T0, msg), file=sys.stderr, flush=True)
 
 
 def _pct(v, q):
@@ -274,7 +290,7 @@ def serve_saturated(ts, reqs, max_active=64, tuning=None):
             "p50_ms": _pct(lat, 50) * 1e3, "p99_ms": _pct(lat, 99) * 1e3,
             "peak_active": st["peak_active"], "ticks": st["ticks"],
             "driver_ms": {"ticks": st["driver_tick_us"] / 1e3, "ring_wait": st["driver_ring_wait_us"] / 1e3,
-                          "pick_wait": st["driver_pick_wait_us"] / 1e3}}
+                          "pick_wait": st["driver_pick_wait_us"] / 1e3, "launch_calls": st["driver_launch_us"] / 1e3}}
 
 
 def measure_served(ts, wl, lams=(10, 25, 50, 100, 200), n=256, tuning=None):
@@ -286,9 +302,12 @@ def measure_served(ts, wl, lams=(10, 25, 50, 100, 200), n=256, tuning=None):
     rows = []
     for lam in lams:
         reqs = wl.config4_requests(n, float(lam))
-        rows.append({"lambda_req_s": lam, "served": serve_stream(ts, reqs, True, tuning=tuning),
-                     "plain": serve_stream(ts, reqs, False)})
+        rows.append({"lambda_req_s": lam, "served": serve_stream(ts, reqs, True, tuning=tuning)})
+        _progress("served stream at %g req/s" % lam)
+        rows[-1]["plain"] = serve_stream(ts, reqs, False)
+        _progress("plain stream at %g req/s" % lam)
     sat = serve_saturated(ts, wl.config4_requests(n, 1e6), tuning=tuning)
+    _progress("served saturation")
     return {"workload": "served_mix", "mix": "70% batched mix, 30% 512^2 inpainting",
             "requests_per_rate": n, "rates": rows, "saturated": sat}
 
@@ -389,6 +408,12 @@ def gather_roofline(ts, spec, prof, peak_cache={}):
     if spec["name"] == "multi_example_tiling_512":
         out["traffic"] = RESOLVE_DRAM_BYTES_PER_LAUNCH
         out["traffic_source"] = "ncu capture of this workload, cold caches, bytes per resolve launch"
+        # the bytes above are the reference's; the kernel skips repeated
+        # candidates and stops candidates early, so its own load-path use is
+        # the fraction of the ceiling's sector rate that its loads reach
+        out["load_path_frac"] = LOAD_PATH_SECTORS_PER_S["k_resolve_lean"] / LOAD_PATH_SECTORS_PER_S["gather_probe"]
+        out["load_path_source"] = ("ncu: L1 sectors/s of k_resolve_lean over those of the gather probe on this "
+                                   "workload's table (profiles/)")
     else:
         out["traffic"] = None
     return out
@@ -527,9 +552,11 @@ def main():
         return
     # --- launch-shape thresholds tuned on this workload (before any timing)
     tuning = ts.autotune_session(lambda: ts.builder_from_spec(spec), repeats=3)
+    _progress("tuned (%d trials)" % tuning.trials)
     flush = L2Flush()
     with ClockSampler(0) as clk:
         m = measure_workload(ts, spec, args.steps, args.warmup, tuning, flush)
+    _progress("%s measured" % args.workload)
     outputs = m.pop("outputs")
     line = {
         "metric": "output Mpx/s", "value": m["value"], "unit": "Mpx/s", "n_gpus": world, "steps": m["steps"],
@@ -556,10 +583,13 @@ def main():
             r["clocks"] = c2.summary()
             r["config"] = bench_config(sp)
             line[key] = r
+            _progress("%s measured" % key)
         line["batched"], btun = measure_batched(ts, wl)
+        _progress("batched measured")
         line["served"] = measure_served(ts, wl, tuning=btun)
     if not args.no_cpu_baseline and rank == 0:
         line["cpu_baseline"], line["parity"] = measure_cpu_baseline(spec, check=outputs)
+        _progress("cpu baseline measured")
     print(json.dumps(line))
 
 

@@ -397,10 +397,11 @@ typedef struct ts_server_stats {
   uint64_t peak_bytes;    /* most budget charged at once */
   uint64_t budget_bytes;
   uint64_t output_pixels, cost_evals;
-  /* host time of the driver thread, microseconds: enqueueing ticks,
-   * waiting for a ring slot (the device running behind), waiting for
-   * pickers (the pick chains running behind) */
-  uint64_t driver_tick_us, driver_ring_wait_us, driver_pick_wait_us;
+  /* host time of the driver thread, microseconds: enqueueing ticks (of
+   * which the kernel launch calls take driver_launch_us), waiting for a ring
+   * slot (the device running behind), waiting for pickers (the pick chains
+   * running behind) */
+  uint64_t driver_tick_us, driver_ring_wait_us, driver_pick_wait_us, driver_launch_us;
 } ts_server_stats;
 /* hbm_budget_bytes 0: half the device's free memory; max_active 0: 64
  * session slots.  NULL if the device cannot be used. */

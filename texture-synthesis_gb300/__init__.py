@@ -108,7 +108,7 @@ class _ServerStats(C.Structure):
     _fields_ = [(f, C.c_uint64) for f in ("submitted", "admitted", "completed", "failed", "ticks", "launches",
                                           "peak_active", "peak_bytes", "budget_bytes", "output_pixels",
                                           "cost_evals", "driver_tick_us", "driver_ring_wait_us",
-                                          "driver_pick_wait_us")]
+                                          "driver_pick_wait_us", "driver_launch_us")]
 
 
 class _LaunchRecord(C.Structure):

@@ -183,6 +183,14 @@ struct DevBuf {
     }
     return e;
   }
+  // Stream-ordered pool memory that outlives the stream it was made on: it
+  // is freed on the legacy stream, for buffers whose users have all
+  // finished when they go (a session's pyramids and tables).
+  cudaError_t alloc_kept(size_t count, cudaStream_t st) {
+    const cudaError_t e = alloc_on(count, st);
+    fs = nullptr;
+    return e;
+  }
   void free_on(cudaStream_t st) { fs = st; }
   size_t bytes() const { return p ? n * sizeof(T) : 0; }
 };
@@ -609,6 +617,14 @@ struct ts_session {
   EventHandle ready;  // recorded after build()'s device work; runs wait for it
   bool consumed = false;
   std::string err;
+  // The pyramids are stream-ordered pool memory freed on the legacy stream:
+  // wait for build()'s own work first (a run waits for its work itself).
+  ~ts_session() {
+    if (ready.e) cudaEventSynchronize(ready.e);
+  }
+  ts_session() = default;
+  ts_session(ts_session &&) = default;
+  ts_session &operator=(ts_session &&) = default;
 };
 
 struct ts_generated {
@@ -953,6 +969,10 @@ int check_limits(const ts_builder &b, uint32_t W, uint32_t H, std::string &err) 
 
 }  // namespace
 
+namespace {
+void keep_pool(int dev);
+}  // namespace
+
 extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
   BUILDER_GUARD(b);
   if (!out) return TS_ERR_NULL;
@@ -1002,6 +1022,7 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
   s->guided = b->has_target;
   try {
     CUDA_TRY(cudaSetDevice(p.device));
+    keep_pool(p.device);
     StreamGuard sg;
     CUDA_TRY(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
     const cudaStream_t st = sg.s;
@@ -1096,8 +1117,8 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
       md.poff = ptexels;
       ptexels += (uint64_t)md.pw * md.ph * s->n_levels;
     }
-    CUDA_TRY(s->levels.alloc(texels));
-    CUDA_TRY(s->masks.alloc(mask_bytes));
+    CUDA_TRY(s->levels.alloc_kept(texels, st));
+    CUDA_TRY(s->masks.alloc_kept(mask_bytes, st));
     std::vector<PyramidJob> pyr;  // every pyramid of the session, built together below
     for (uint32_t f = 0; f < s->n_maps; ++f) {
       const uint32_t e = s->filtered[f];
@@ -1105,12 +1126,12 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
       if (s->maps[f].mask_off >= 0) {
         std::vector<uint8_t> mb((size_t)s->maps[f].w * s->maps[f].h);
         for (size_t i = 0; i < mb.size(); ++i) mb[i] = masks[e].px[4 * i] != 0 ? 1 : 0;
-        CUDA_TRY(cudaMemcpy(s->masks.p + s->maps[f].mask_off, mb.data(), mb.size(), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpyAsync(s->masks.p + s->maps[f].mask_off, mb.data(), mb.size(), cudaMemcpyHostToDevice, st));
       }
     }
-    CUDA_TRY(s->plevels.alloc(ptexels));
-    CUDA_TRY(s->d_maps.alloc(s->n_maps));
-    CUDA_TRY(cudaMemcpy(s->d_maps.p, s->maps.data(), s->n_maps * sizeof(MapDesc), cudaMemcpyHostToDevice));
+    CUDA_TRY(s->plevels.alloc_kept(ptexels, st));
+    CUDA_TRY(s->d_maps.alloc_kept(s->n_maps, st));
+    CUDA_TRY(cudaMemcpyAsync(s->d_maps.p, s->maps.data(), s->n_maps * sizeof(MapDesc), cudaMemcpyHostToDevice, st));
     // guides: every example (unfiltered order) plus the target guide
     std::vector<GuideDesc> gd(std::max<uint32_t>(s->n_ex, 1));
     if (s->guided) {
@@ -1125,11 +1146,11 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
       // padded fast path needs its size to equal the map's
       for (uint32_t f = 0; f < s->n_maps; ++f)
         if (f >= s->n_ex || gd[f].w != s->maps[f].w || gd[f].h != s->maps[f].h) s->guide_dims_differ = true;
-      CUDA_TRY(s->guides.alloc(gtex));
+      CUDA_TRY(s->guides.alloc_kept(gtex, st));
       for (uint32_t e = 0; e < s->n_ex; ++e)
         pyr.push_back(PyramidJob{&guides[e], p.backtrack_stages, s->guides.p + gd[e].off});
-      if (!s->guide_dims_differ) CUDA_TRY(s->pguides.alloc(ptexels));
-      CUDA_TRY(s->tguide.alloc((size_t)W * H * s->n_levels));
+      if (!s->guide_dims_differ) CUDA_TRY(s->pguides.alloc_kept(ptexels, st));
+      CUDA_TRY(s->tguide.alloc_kept((size_t)W * H * s->n_levels, st));
       pyr.push_back(PyramidJob{&tg, p.backtrack_stages, s->tguide.p});
     }
     device_pyramids(pyr, st);
@@ -1142,8 +1163,8 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
       for (uint32_t f = 0; f < s->n_maps; ++f)
         launch_pad(s->guides.p + gd[f].off, gd[f].w, gd[f].h, s->n_levels, pitch, s->pguides.p + s->maps[f].poff, st);
     CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(s->d_gdesc.alloc(gd.size()));
-    CUDA_TRY(cudaMemcpy(s->d_gdesc.p, gd.data(), gd.size() * sizeof(GuideDesc), cudaMemcpyHostToDevice));
+    CUDA_TRY(s->d_gdesc.alloc_kept(gd.size(), st));
+    CUDA_TRY(cudaMemcpyAsync(s->d_gdesc.p, gd.data(), gd.size() * sizeof(GuideDesc), cudaMemcpyHostToDevice, st));
     // the pyramids are still being built: run() waits for this event on the
     // device, so its host planning overlaps them
     CUDA_TRY(cudaEventCreateWithFlags(&s->ready.e, cudaEventDisableTiming));
@@ -1579,9 +1600,6 @@ void run_plan(ts_session *s, RunCtx &c) {
                 c.cells.size() * 4 + c.init_list.size() * 4;
 }
 
-// The pick chain of the next stage (pick_random_unresolved, ms.rs:380-389,
-// redo items first, ms.rs:905-915): fills its items and extends the
-// resolved list with each batch's appended items, in the reference's order.
 // A small pool of host threads shared by every single-session run: it
 // computes the random draws of the large stages of the pick chain.  One job
 // at a time (runs that find it busy compute their draws themselves).
@@ -1710,9 +1728,6 @@ void keep_pool(int dev) {
   done.push_back(dev);
 }
 
-// Device buffers of a run and the step descriptors that point into them.
-// With a pool stream, the buffers are stream-ordered pool memory (freed
-// without waiting for the device); otherwise plain cudaMalloc.
 // Whether a session's neighbour-distance sums (get_distances_to_k_neighs,
 // ms.rs:405-425) are exact.  With W and H powers of two, x / W and y / H are
 // exact, so every distance fma(dx, dx, dy * dy) is an integer multiple of
@@ -1727,6 +1742,9 @@ bool exact_sum_ok(uint32_t W, uint32_t H, uint32_t k) {
   return M <= (1u << 16) && 32ull * std::max<uint32_t>(k, 1) * M * M < (1ull << 53);
 }
 
+// Device buffers of a run and the step descriptors that point into them.
+// With a pool stream, the buffers are stream-ordered pool memory (freed
+// without waiting for the device); otherwise plain cudaMalloc.
 void run_alloc(RunCtx &c, cudaStream_t pool) {
   ts_session *s = c.s;
   const Params &p = s->prm;
@@ -2916,6 +2934,7 @@ struct ServerReq {
 };
 
 constexpr uint32_t kServerRing = 8;  // ticks in flight
+constexpr size_t kLoneSteps = 16;    // steps of a tick that holds a single request
 
 }  // namespace
 
@@ -2929,6 +2948,7 @@ struct ts_server {
   std::condition_variable cv_work, cv_done, cv_complete, cv_pick, cv_picked;
   std::deque<ServerReq *> to_pick;  // requests whose later stages are still to be picked
   std::deque<ServerReq *> pending;
+  std::atomic<uint32_t> n_pending{0};  // pending.size(), read by the driver without the mutex
   std::unordered_map<uint64_t, ServerReq *> reqs;  // submitted, not yet collected
   std::deque<ServerReq *> completing;              // steps done, waiting for read-back
   std::vector<uint32_t> free_slots;
@@ -3016,7 +3036,8 @@ void server_admit(ts_server *S, ServerReq *r) {
   CUDA_TRY(cudaMemcpyAsync(S->d_sess.p + r->slot, &c.sd, sizeof(SessionDev), cudaMemcpyHostToDevice, S->ust));
   CUDA_TRY(cudaMemcpyAsync(S->d_tabs.p + r->slot, &tab, sizeof(tab), cudaMemcpyHostToDevice, S->ust));
   CUDA_TRY(cudaEventCreateWithFlags(&r->up_ev, cudaEventDisableTiming));
-  CUDA_TRY(cudaEventCreateWithFlags(&r->ev, cudaEventDisableTiming));
+  // the completion thread sleeps on this one instead of spinning beside the driver
+  CUDA_TRY(cudaEventCreateWithFlags(&r->ev, cudaEventDisableTiming | cudaEventBlockingSync));
   CUDA_TRY(cudaEventRecord(r->up_ev, S->ust));
   CUDA_TRY(cudaStreamWaitEvent(S->st, r->up_ev, 0));
 }
@@ -3041,6 +3062,7 @@ void server_driver(ts_server *S) {
         // within the budget, or alone on the device
         if (!S->active.empty() && S->used + r->bytes > S->budget) break;
         S->pending.pop_front();
+        S->n_pending.store((uint32_t)S->pending.size(), std::memory_order_relaxed);
         r->slot = S->free_slots.back();
         S->free_slots.pop_back();
         r->slotted = true;
@@ -3091,7 +3113,7 @@ void server_driver(ts_server *S) {
     const double t_tick0 = host_ms();
     try {
       ts_server::Ring &R = S->ring[ri];
-      double ring_wait = 0.0;
+      double ring_wait = 0.0, launch_ms = 0.0;
       if (R.used) {  // the slot's previous tick is done
         const double w0 = host_ms();
         CUDA_TRY(cudaEventSynchronize(R.ev));
@@ -3125,13 +3147,47 @@ void server_driver(ts_server *S) {
       launches.clear();
       for (ServerReq *r : ready) r->c->steps[r->cursor].resolve = form;
       uint64_t tick_launches = 0;
+      size_t lone_steps = 1;  // steps the tick advances a lone session by
       if (ready.size() == 1) {
-        // one session in the tick: its step with the single-session kernels
-        // (no segment lookups at the start of every block)
-        RunCtx &c = *ready[0]->c;
+        // one session in the tick: its steps with the single-session kernels
+        // (no segment lookups at the start of every block).  While nothing
+        // waits for admission it takes up to kLoneSteps consecutive steps
+        // whose items are picked, as the plain path would (a redo-only
+        // batch's commit then rides in the next step's first k-NN launch),
+        // so that the host's per-tick work does not pace a lone request; a
+        // request that arrives meanwhile joins at the next tick.
+        ServerReq *r0 = ready[0];
+        RunCtx &c = *r0->c;
         const uint64_t before = c.launches;
         LaunchTimer lt;
-        enqueue_step(c, c.steps[ready[0]->cursor], S->st, lt);
+        const double l0 = host_ms();
+        // only stages whose items went up above: a picker may have
+        // published more since
+        const uint32_t uploaded = r0->uploaded;
+        const size_t limit = S->n_pending.load(std::memory_order_relaxed) ? 1 : kLoneSteps;
+        auto usable = [&](size_t t) { return t < c.steps.size() && c.steps[t].stage < (int)uploaded; };
+        const Step *pending = nullptr;
+        size_t n = 0;
+        while (n < limit && usable(r0->cursor + n)) {
+          Step &stp = c.steps[r0->cursor + n];
+          if (n > 0)
+            stp.resolve = stp.n > S->team_max_items                                        ? kPhaseResolve
+                          : (stp.n <= S->team_full_max_items && team_full_fits(c.k, c.m)) ? kPhaseTeamFull
+                                                                                           : kPhaseTeamPart;
+          const bool more = n + 1 < limit && usable(r0->cursor + n + 1);
+          if (more) {
+            Step &nx = c.steps[r0->cursor + n + 1];
+            nx.resolve = nx.n > S->team_max_items                                        ? kPhaseResolve
+                         : (nx.n <= S->team_full_max_items && team_full_fits(c.k, c.m)) ? kPhaseTeamFull
+                                                                                         : kPhaseTeamPart;
+          }
+          const bool defer = more && can_defer_commit(c, stp, &c.steps[r0->cursor + n + 1]);
+          enqueue_step(c, stp, S->st, lt, pending, defer);
+          pending = defer ? &stp : nullptr;
+          ++n;
+        }
+        lone_steps = n;
+        launch_ms += host_ms() - l0;
         tick_launches = c.launches - before;
       } else {
         for (int ph = 0; ph < kPhases; ++ph) {
@@ -3196,7 +3252,9 @@ void server_driver(ts_server *S) {
           ml.n_lean = pl.n_lean;
           ml.lean_blocks = pl.lean_blocks;
           ml.key_cap = pl.key_cap;
+          const double l0 = host_ms();
           launch_multi(pl.phase, ml, pl.blocks, pl.smem, S->st);
+          launch_ms += host_ms() - l0;
         }
         tick_launches = launches.size();
         for (const PlannedLaunch &pl : launches)
@@ -3215,12 +3273,15 @@ void server_driver(ts_server *S) {
           continue;
         }
         RunCtx &c = *r->c;
-        const Step &stp = c.steps[r->cursor];
-        if (stp.batch) {
-          ++c.batches;
-          c.resolves += stp.n;
+        for (size_t q = 0; q < lone_steps; ++q) {
+          const Step &stp = c.steps[r->cursor];
+          if (stp.batch) {
+            ++c.batches;
+            c.resolves += stp.n;
+          }
+          ++r->cursor;
         }
-        if (++r->cursor == c.steps.size()) {
+        if (r->cursor == c.steps.size()) {
           CUDA_TRY(cudaEventRecord(r->ev, S->st));
           finished.push_back(r);
         } else {
@@ -3233,6 +3294,7 @@ void server_driver(ts_server *S) {
         S->stats.ticks += 1;
         S->stats.launches += tick_launches;
         S->stats.driver_ring_wait_us += (uint64_t)(ring_wait * 1e3);
+        S->stats.driver_launch_us += (uint64_t)(launch_ms * 1e3);
         S->stats.driver_tick_us += (uint64_t)((host_ms() - t_tick0 - ring_wait) * 1e3);
         for (ServerReq *r : finished) S->completing.push_back(r);
         if (!finished.empty()) S->cv_complete.notify_one();
@@ -3252,6 +3314,7 @@ void server_driver(ts_server *S) {
         S->completing.push_back(r);
       }
       S->pending.clear();
+      S->n_pending.store(0, std::memory_order_relaxed);
       S->cv_complete.notify_one();
     }
   }
@@ -3259,6 +3322,8 @@ void server_driver(ts_server *S) {
 
 void server_completer(ts_server *S) {
   if (cudaSetDevice(S->device) != cudaSuccess) return;
+  EventHandle copied;  // the read-back copies' end, waited on without spinning
+  if (cudaEventCreateWithFlags(&copied.e, cudaEventDisableTiming | cudaEventBlockingSync) != cudaSuccess) return;
   for (;;) {
     ServerReq *r = nullptr;
     {
@@ -3272,7 +3337,8 @@ void server_completer(ts_server *S) {
       try {
         CUDA_TRY(cudaEventSynchronize(r->ev));
         run_readback(*r->c, S->cst);
-        CUDA_TRY(cudaStreamSynchronize(S->cst));
+        CUDA_TRY(cudaEventRecord(copied.e, S->cst));
+        CUDA_TRY(cudaEventSynchronize(copied.e));
         run_finish(*r->c);
         r->result = r->c->g.release();
       } catch (const Failure &f) {
@@ -3447,6 +3513,7 @@ int ts_server_submit(ts_server *S, ts_session *s, uint64_t *ticket) {
     S->cv_pick.notify_one();
   }
   S->pending.push_back(r.release());
+  S->n_pending.store((uint32_t)S->pending.size(), std::memory_order_relaxed);
   S->stats.submitted += 1;
   S->cv_work.notify_one();
   S->cv_picked.notify_all();  // a driver waiting on pickers admits it at once
