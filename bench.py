@@ -459,8 +459,9 @@ def measure_workload(ts, spec, steps, warmup, tuning, flush):
         e2e_t.append(t4 - t1)
         st = g.stats()
         parts.append({"build_ms": (t2 - t1) * 1e3, "run_ms": (t3 - t2) * 1e3, "image_ms": (t4 - t3) * 1e3,
-                      **{k: st[k] for k in ("host_plan_ms", "host_alloc_ms", "host_enqueue_ms", "host_wait_ms",
-                                            "host_finish_ms", "upload_ms", "readback_ms", "gpu_ms")}})
+                      **{k: st[k] for k in ("host_plan_ms", "host_alloc_ms", "host_enqueue_ms", "host_pick_ms",
+                                            "host_launch_ms", "host_wait_ms", "host_finish_ms", "upload_ms",
+                                            "readback_ms", "gpu_ms")}})
     e2e = px / (sum(e2e_t) / len(e2e_t)) / 1e6
     breakdown = {k: sum(p[k] for p in parts) / len(parts) for k in parts[0]}
     prof = ts.builder_from_spec(spec, profile=True, tuning=tuning).build().run().stats()

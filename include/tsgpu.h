@@ -153,6 +153,11 @@ typedef struct ts_run_stats {
   /* Device time of the initial uploads and of reading the results back
    * (CUDA events; part of gpu_ms). */
   double upload_ms, readback_ms;
+  /* Parts of host_enqueue_ms: waiting for the pick chain
+   * (pick_random_unresolved, on its own host thread) to finish a stage, and
+   * the rest (uploads, launches and stream-order calls, and the read-back
+   * copies, which wait for the device). */
+  double host_pick_ms, host_launch_ms;
 } ts_run_stats;
 
 const char *ts_status_str(int status);

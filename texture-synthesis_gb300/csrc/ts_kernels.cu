@@ -104,6 +104,37 @@ __device__ __forceinline__ bool occupied(const SessionDev &s, int x, int y) {
   return (__ldg(&s.mir[(size_t)ys * s.wpr + (xs >> 5)]) >> (xs & 31)) & 1u;
 }
 
+// Whether pixel p is in a tree of n points (SessionDev::rank); always true
+// when the bitmap is the tree itself.
+__device__ __forceinline__ bool in_tree(const SessionDev &s, uint32_t p, uint32_t n) {
+  return !s.rank || __ldg(&s.rank[p]) - 1u < n;
+}
+
+// occupied() against the tree of an item whose batch starts with n points:
+// with SessionDev::rank the bitmap may hold later points too, so a set bit
+// is checked against the tree position of the pixel it stands for.
+__device__ __forceinline__ bool occupied_n(const SessionDev &s, int x, int y, uint32_t n) {
+  if (!occupied(s, x, y)) return false;
+  if (!s.rank) return true;
+  const int xs = modi(x, (int)s.W), ys = modi(y, (int)s.H);  // a mirror stands for its wrapped pixel
+  return in_tree(s, (uint32_t)ys * s.W + (uint32_t)xs, n);
+}
+
+// Resolved-list length at the start of the batch of stage item `item`
+// (BatchDev::btab), else the launch's own.
+__device__ __forceinline__ uint32_t item_nres(const BatchDev &b, uint32_t item) {
+  if (!b.btab) return b.n_res;
+  uint32_t lo = 0, hi = b.nbt;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(&b.btab[mid].x) <= item)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return __ldg(&b.btab[lo].y);
+}
+
 __device__ __forceinline__ bool mir_bit(const SessionDev &s, uint32_t x, uint32_t y) {
   return (s.mir[(size_t)y * s.wpr + (x >> 5)] >> (x & 31)) & 1u;
 }
@@ -295,6 +326,7 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
     const uint32_t pixel = st.items[b.i0 + local];
     const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
     int32_t *nbo = b.nbuf + (size_t)local * s.k;
+    const uint32_t n_tree = item_nres(b, b.i0 + local);
     uint32_t count = 0;
     const uint32_t tab_n = b.grid_first ? 0u : s.knn_tab_n;
     // 64 table entries per round, two per lane, both looked up before either
@@ -316,7 +348,7 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
     // two more rounds or fewer will do (dense steps end here)
     uint32_t c = 0;
     while (c < tab_n) {
-      round(c, [&](int dx, int dy) { return occupied(s, px + dx, py + dy); });
+      round(c, [&](int dx, int dy) { return occupied_n(s, px + dx, py + dy, n_tree); });
       c += 2 * kWarp;
       if (count >= s.k) break;
       if (kWin && (count == 0 || (uint64_t)(s.k - count) * c > (uint64_t)count * kWalkDirect)) break;
@@ -335,7 +367,9 @@ __device__ __forceinline__ void knn_walk_body(const SessionDev &s, const StageDe
       for (; c < tab_n; c += 2 * kWarp) {
         round(c, [&](int dx, int dy) {
           const int i = dx + kKnnTabRadius;
-          return ((win[(dy + kKnnTabRadius) * kWinWords + (i >> 5)] >> (i & 31)) & 1u) != 0u;
+          // (a set bit of a later point fails its tree check)
+          return ((win[(dy + kKnnTabRadius) * kWinWords + (i >> 5)] >> (i & 31)) & 1u) != 0u &&
+                 (!s.rank || occupied_n(s, px + dx, py + dy, n_tree));
         });
         if (count >= s.k) break;
       }
@@ -528,7 +562,7 @@ __device__ __forceinline__ const unsigned long long *sort_first(unsigned long lo
 // and the OR of the d2 in sh.prefix.
 __device__ __forceinline__ uint32_t ring_base(uint32_t r) { return r == 0 ? 0u : 4u * r * (r - 1u) + 1u; }
 
-__device__ void grid_collect(const SessionDev &s, int px, int py, uint32_t k, ExhShared &sh,
+__device__ void grid_collect(const SessionDev &s, int px, int py, uint32_t k, uint32_t n_tree, ExhShared &sh,
                              unsigned long long *all, uint32_t cap) {
   if (threadIdx.x == 0) {
     sh.total = 0;
@@ -567,10 +601,16 @@ __device__ void grid_collect(const SessionDev &s, int px, int py, uint32_t k, Ex
             uint64_t wv = __ldg(&row[wi]);
             if (sh5 + kCell > 32) wv |= (uint64_t)__ldg(&row[wi + 1]) << 32;
             bits = (uint32_t)(wv >> sh5) & ((1u << kCell) - 1u);
+            if (s.rank)  // set bits of later points (k-NN made ahead) do not count
+              for (uint32_t t = bits; t;) {
+                const int bp = __ffs(t) - 1;
+                t &= t - 1u;
+                if (!in_tree(s, (uint32_t)y * s.W + (uint32_t)(x0 + bp), n_tree)) bits &= ~(1u << bp);
+              }
           } else {
             bits = 0;
             for (int xx = 0; xx < kCell; ++xx)
-              if (occupied(s, x0 + xx, y)) bits |= 1u << xx;
+              if (occupied_n(s, x0 + xx, y, n_tree)) bits |= 1u << xx;
           }
           while (bits) {
             const int bp = __ffs(bits) - 1;
@@ -615,7 +655,7 @@ __device__ uint32_t knn_exhaustive_item(const SessionDev &s, const StageDev &st,
   const uint32_t pixel = st.items[b.i0 + local];
   const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
   const uint32_t k = s.k;
-  const uint32_t n_res = b.n_res;
+  const uint32_t n_res = item_nres(b, b.i0 + local);
   auto d2of = [&](int x, int y) -> uint32_t {
     const int dx = x - px, dy = y - py;
     return (uint32_t)(dx * dx + dy * dy);
@@ -633,7 +673,7 @@ __device__ uint32_t knn_exhaustive_item(const SessionDev &s, const StageDev &st,
   // instead, which hold the k nearest.
   const int lane = threadIdx.x & 31;
   const bool grid = use_grid && s.cells != nullptr && n_res > kExhGridFrom;
-  if (grid) grid_collect(s, px, py, k, sh, all, cap);
+  if (grid) grid_collect(s, px, py, k, n_res, sh, all, cap);
   // kPts points per thread and round: their loads (the point, then its
   // mirror bit) are all in flight together
   constexpr int kPts = 4;
@@ -690,7 +730,7 @@ __device__ uint32_t knn_exhaustive_item(const SessionDev &s, const StageDev &st,
   uint32_t total = sh.total;
   if (use_grid && !grid && total > cap && s.cells != nullptr) {
     __syncthreads();
-    grid_collect(s, px, py, k, sh, all, cap);
+    grid_collect(s, px, py, k, n_res, sh, all, cap);
     total = sh.total;
   }
   const unsigned long long *sorted;
@@ -1097,11 +1137,29 @@ __device__ __forceinline__ float neighbour_weight(double dj, double avg, const d
   return wv;
 }
 
+// Batch-start colour and state of output pixel p: the image, unless the
+// previous batch step left its commit to this launch (BatchDev::prev_tag)
+// and p is one of its pixels, whose values the shadow holds.  All loads are
+// issued together.  Tags of this launch's own deferred pixels never equal
+// prev_tag.
+__device__ __forceinline__ void start_pixel(const SessionDev &s, const BatchDev &b, uint32_t p, bool want_colour,
+                                            uint32_t &colour, uint4 &state) {
+  colour = want_colour ? s.color[p] : 0u;
+  state = s.state[p];
+  if (b.prev_tag) {
+    const uint4 h0 = s.shadow[2 * (size_t)p], h1 = s.shadow[2 * (size_t)p + 1];
+    if (h0.x == b.prev_tag) {
+      colour = want_colour ? h0.y : 0u;
+      state = h1;
+    }
+  }
+}
+
 // Everything of neighbour_setup but the weight, which the record gets as wv.
 template <bool kG = true>
-__device__ __forceinline__ bool neighbour_records(const SessionDev &s, const StageDev &st, int px, int py, uint32_t j,
-                                                  int32_t off, float wv, const WarpSmem &w, uint32_t &cxy,
-                                                  uint32_t &aux, int &maxoff, bool &bad_map) {
+__device__ __forceinline__ bool neighbour_records(const SessionDev &s, const StageDev &st, const BatchDev &b, int px,
+                                                  int py, uint32_t j, int32_t off, float wv, const WarpSmem &w,
+                                                  uint32_t &cxy, uint32_t &aux, int &maxoff, bool &bad_map) {
   const int W = (int)s.W, H = (int)s.H;
   maxoff = max(maxoff, max(abs(off_dx(off)), abs(off_dy(off))));
   const int nx = px + off_dx(off), ny = py + off_dy(off);
@@ -1111,13 +1169,16 @@ __device__ __forceinline__ bool neighbour_records(const SessionDev &s, const Sta
     qy = modi(ny, H);
   }
   const bool inb = (unsigned)qx < s.W && (unsigned)qy < s.H;
-  const uint32_t pat = inb ? s.color[(size_t)qy * s.W + qx] : kOutside;
+  // colour and state of the neighbour (inb: (qx, qy) is its wrapped point)
+  const int wx = modi(nx, W), wy = modi(ny, H);
+  uint32_t pat;
+  uint4 sv;
+  start_pixel(s, b, (uint32_t)wy * s.W + (uint32_t)wx, inb, pat, sv);
+  if (!inb) pat = kOutside;
   uint32_t gpat = 0;
   if (kG && s.guided) gpat = inb ? __ldg(&s.tguide[(size_t)st.level * s.W * s.H + (size_t)qy * s.W + qx]) : kOutside;
   w.nbr[j] = make_uint4((uint32_t)off, pat, gpat, __float_as_uint(wv));
   w.lin[j] = off_dy(off) * (int)s.ppitch + off_dx(off);
-  const int wx = modi(nx, W), wy = modi(ny, H);
-  const uint4 sv = s.state[(size_t)wy * s.W + wx];
   const uint32_t map = sv.z;
   if (map >= s.n_maps) {
     bad_map = true;
@@ -1140,7 +1201,7 @@ __device__ __forceinline__ bool neighbour_setup(const SessionDev &s, const Stage
   const double d = s.exact_sum ? exact_dist(s, off) : b.dist[(size_t)j * nb + local];
   const float wv = neighbour_weight(d, avg, tab, tab_ff);
   nan_w |= (wv != wv);
-  return neighbour_records<kG>(s, st, px, py, j, off, wv, w, cxy, aux, maxoff, bad_map);
+  return neighbour_records<kG>(s, st, b, px, py, j, off, wv, w, cxy, aux, maxoff, bad_map);
 }
 
 // Candidate 0's exact score (better_match, ms.rs:1225-1288, with no bound):
@@ -1235,7 +1296,7 @@ __device__ __forceinline__ void add_cell_point(const SessionDev &s, int x, int y
 // update + flush_resolved of one item (ms.rs:296-377): its colour and state,
 // its place in the resolved list, the bitmap, mirrors and cell counts.
 __device__ __forceinline__ void commit_item(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
-                                            const Result &r) {
+                                            const Result &r, bool count_evals = true) {
   const uint32_t p = r.pixel;
   if (r.cmap >= s.n_maps || p >= s.W * s.H) {
     set_err(s.err, kDevErrIndex);
@@ -1249,12 +1310,13 @@ __device__ __forceinline__ void commit_item(const SessionDev &s, const StageDev 
   }
   s.state[p] = make_uint4(r.srcxy, r.idp, r.idm, r.cmap);
   s.color[p] = s.levels[md.off + (size_t)st.level * md.w * md.h + (size_t)sy * md.w + sx];
-  if (r.ncand) atomicAdd(s.evals, (unsigned long long)r.ncand);
+  if (count_evals && r.ncand) atomicAdd(s.evals, (unsigned long long)r.ncand);
   if (r.flags & kResAppend) {
     const uint32_t item = b.i0 + local;
     const uint32_t pos = b.n_res + (item - b.append_from);
-    s.resolved[pos] = p;
     s.rscore[pos] = r.score;
+    if (s.rank) return;  // k-NN made ahead: k_tree_append entered the point already
+    s.resolved[pos] = p;
     const uint32_t x = p % s.W, y = p / s.W;
     atomicOr(&s.occ[(size_t)y * s.wpr + (x >> 5)], 1u << (x & 31));
     add_cell_point(s, (int)x, (int)y);
@@ -1278,10 +1340,21 @@ __device__ __forceinline__ void commit_item(const SessionDev &s, const StageDev 
 // reads its pixel, state or bit during the batch), else kept for k_commit.
 __device__ __forceinline__ void emit_result(const SessionDev &s, const StageDev &st, const BatchDev &b, uint32_t local,
                                             const Result &r) {
-  if (b.fused_commit)
+  if (b.fused_commit) {
     commit_item(s, st, b, local, r);
-  else
+  } else {
     b.res[local] = r;
+    if (b.defer_tag && r.cmap < s.n_maps && r.pixel < s.W * s.H) {
+      // what the commit will write, for the next step's readers (start_pixel)
+      const MapDesc md = s.maps[r.cmap];
+      const uint32_t sx = r.srcxy & 0xffffu, sy = r.srcxy >> 16;
+      if (sx < md.w && sy < md.h) {
+        const uint32_t col = s.levels[md.off + (size_t)st.level * md.w * md.h + (size_t)sy * md.w + sx];
+        s.shadow[2 * (size_t)r.pixel] = make_uint4(b.defer_tag, col, 0u, 0u);
+        s.shadow[2 * (size_t)r.pixel + 1] = make_uint4(r.srcxy, r.idp, r.idm, r.cmap);
+      }
+    }
+  }
 }
 
 // The winning candidate as an update (ms.rs:976-1001): source coordinate and
@@ -1300,7 +1373,10 @@ __device__ void write_result(const SessionDev &s, const StageDev &st, const Warp
     const uint32_t j = aux >> 16;
     const int32_t off = (int32_t)w.nbr[j].x;
     const int wx = modi(px + off_dx(off), (int)s.W), wy = modi(py + off_dy(off), (int)s.H);
-    idp = s.state[(size_t)wy * s.W + wx].y;
+    uint32_t unused;
+    uint4 sv;
+    start_pixel(s, b, (uint32_t)wy * s.W + (uint32_t)wx, false, unused, sv);
+    idp = sv.y;
   }
   Result r;
   r.pixel = pixel;
@@ -2085,6 +2161,49 @@ __device__ __forceinline__ SegView find_segment(const MultiLaunch &ml) {
   return v;
 }
 
+// The tree entries of a chunk of appended stage items, for k-NN made ahead
+// of the resolves (SessionDev::rank): what the commits of those items
+// enter in flush_resolved (ms.rs:296-331), the resolved-list slot, bitmap
+// and mirror bits and cell counts, plus the tree position.  The appended
+// pixels and their order come from the pick chain alone, so this runs
+// before their resolves; the k-NN kernels check every set bit against the
+// item's own tree length.
+__global__ void k_tree_append(SessionDev s, StageDev st, uint32_t a0, uint32_t a1, uint32_t pos0, uint32_t nomir_end) {
+  pdl_enter();
+  const uint32_t i = a0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a1) return;
+  const uint32_t p = st.items[i];
+  if (p >= s.W * s.H) {
+    set_err(s.err, kDevErrIndex);
+    return;
+  }
+  const uint32_t pos = pos0 + (i - a0);
+  s.resolved[pos] = p;
+  s.rank[p] = pos + 1u;
+  const uint32_t x = p % s.W, y = p / s.W;
+  atomicOr(&s.occ[(size_t)y * s.wpr + (x >> 5)], 1u << (x & 31));
+  add_cell_point(s, (int)x, (int)y);
+  if (s.tiling && i >= nomir_end) {
+    atomicOr(&s.mir[(size_t)y * s.wpr + (x >> 5)], 1u << (x & 31));
+    if ((int)x < s.x_l)
+      add_cell_point(s, (int)x + (int)s.W, (int)y);
+    else if ((int)x > s.x_r)
+      add_cell_point(s, (int)x - (int)s.W, (int)y);
+    if ((int)y < s.y_b)
+      add_cell_point(s, (int)x, (int)y + (int)s.H);
+    else if ((int)y > s.y_t)
+      add_cell_point(s, (int)x, (int)y - (int)s.H);
+  }
+}
+
+// Tree positions of the initial tree (random-init or locked pixels).
+__global__ void k_rank_init(SessionDev s, uint32_t n) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const uint32_t p = s.resolved[e];
+  if (p < s.W * s.H) s.rank[p] = e + 1u;
+}
+
 __global__ void k_random_candidates(SessionDev s, StageDev st) {
   pdl_enter(); random_candidates_body(s, st, blockIdx.x); }
 __global__ void k_random_candidates_multi(MultiLaunch ml) {
@@ -2096,8 +2215,14 @@ __global__ void k_random_candidates_multi(MultiLaunch ml) {
 // The commit of a pending batch of redo items, spread over the launch's
 // threads (PendingCommit).
 __device__ __forceinline__ void pending_commit(const SessionDev &s, const PendingCommit &pc) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pc.n; i += gridDim.x * blockDim.x)
-    commit_item(s, pc.st, pc.b, i, pc.b.res[i]);
+  uint32_t evals = 0;  // one atomic per warp instead of one per item
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pc.n; i += gridDim.x * blockDim.x) {
+    const Result r = pc.b.res[i];
+    evals += r.ncand;
+    commit_item(s, pc.st, pc.b, i, r, false);
+  }
+  evals = __reduce_add_sync(0xffffffffu, evals);
+  if ((threadIdx.x & 31) == 0 && evals) atomicAdd(s.evals, (unsigned long long)evals);
 }
 
 template <bool kWin>
@@ -2202,13 +2327,20 @@ __global__ void __launch_bounds__(128) k_mean_multi(MultiLaunch ml) {
   mean_body(*v.s, v.d->b, v.vb);
 }
 
-__global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve(SessionDev s, StageDev st, BatchDev b) {
+// pc: the previous batch step's deferred commit (BatchDev::prev_tag), made
+// here by every thread of the grid before its own item; this launch's
+// readers of those pixels take their values from pc.b.res instead.
+__global__ void __launch_bounds__(kResolveWarps *kWarp, 8)
+    k_resolve(SessionDev s, StageDev st, BatchDev b, const __grid_constant__ PendingCommit pc) {
   pdl_enter();
+  if (pc.n) pending_commit(s, pc);
   resolve_body<false>(s, st, b, blockIdx.x, gridDim.x);
 }
 // Sessions without guides (the guide terms compiled out).
-__global__ void __launch_bounds__(kResolveWarps *kWarp, 9) k_resolve_lean(SessionDev s, StageDev st, BatchDev b) {
+__global__ void __launch_bounds__(kResolveWarps *kWarp, 9)
+    k_resolve_lean(SessionDev s, StageDev st, BatchDev b, const __grid_constant__ PendingCommit pc) {
   pdl_enter();
+  if (pc.n) pending_commit(s, pc);
   resolve_body<true>(s, st, b, blockIdx.x, gridDim.x);
 }
 __global__ void __launch_bounds__(kResolveWarps *kWarp, 8) k_resolve_multi(MultiLaunch ml) {
@@ -2224,8 +2356,10 @@ __global__ void __launch_bounds__(kResolveWarps *kWarp, 9) k_resolve_multi_lean(
 }
 
 template <int T, bool kFull>
-__global__ void __launch_bounds__(T) k_resolve_team(SessionDev s, StageDev st, BatchDev b) {
+__global__ void __launch_bounds__(T)
+    k_resolve_team(SessionDev s, StageDev st, BatchDev b, const __grid_constant__ PendingCommit pc) {
   pdl_enter();
+  if (pc.n) pending_commit(s, pc);
   resolve_team_body<T, kFull>(s, st, b, blockIdx.x, gridDim.x);
 }
 template <int T, bool kFull>
@@ -2333,7 +2467,7 @@ __global__ void __launch_bounds__(T) k_step_team_full(SessionDev s, StageDev st,
         const uint32_t j = j0 + t;
         bool valid = false;
         uint32_t cxy = 0, aux = 0;
-        if (j < nk) valid = neighbour_records(s, st, px, py, j, sh.nbo[j], 0.0f, w, cxy, aux, maxoff, bad_map);
+        if (j < nk) valid = neighbour_records(s, st, b, px, py, j, sh.nbo[j], 0.0f, w, cxy, aux, maxoff, bad_map);
         const uint32_t bal = __ballot_sync(0xffffffffu, valid);
         if (lane == 0) wcnt[warp] = __popc(bal);
         setup_bar<TS>();
@@ -2736,26 +2870,30 @@ void launch_mean(const SessionDev &s, const StageDev &st, const BatchDev &b, cud
   launch_pdl(k_mean_staged, cdiv(n, kMeanThreads), kMeanThreads, (size_t)s.k * kMeanThreads * 8, stream, s, st, b);
 }
 
-void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
+void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream,
+                    const PendingCommit &pc) {
   const uint32_t n = b.i1 - b.i0;
-  if (n == 0) return;
+  if (n == 0 && pc.n == 0) return;
   const size_t smem = resolve_smem_bytes(s.k, s.m, s.guided);
+  const uint32_t grid = std::max(cdiv(n, kResolveWarps), cdiv(pc.n, kResolveWarps * kWarp));
   if (s.guided)
-    launch_pdl(k_resolve, cdiv(n, kResolveWarps), kResolveWarps * kWarp, smem, stream, s, st, b);
+    launch_pdl(k_resolve, grid, kResolveWarps * kWarp, smem, stream, s, st, b, pc);
   else
-    launch_pdl(k_resolve_lean, cdiv(n, kResolveWarps), kResolveWarps * kWarp, smem, stream, s, st, b);
+    launch_pdl(k_resolve_lean, grid, kResolveWarps * kWarp, smem, stream, s, st, b, pc);
 }
 
 void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev &b, bool full,
-                         cudaStream_t stream) {
+                         cudaStream_t stream, const PendingCommit &pc) {
   const uint32_t n = b.i1 - b.i0;
-  if (n == 0) return;
-  const uint32_t grid = n < 152u * 16u ? n : 152u * 16u;
+  if (n == 0 && pc.n == 0) return;
+  uint32_t grid = n < 152u * 16u ? n : 152u * 16u;
+  grid = std::max(grid, std::min(152u * 16u, cdiv(pc.n, kTeamThreads)));
   if (full && team_full_smem_bytes(s.k, s.m) <= kTeamFullMaxSmem)
     launch_pdl(k_resolve_team<kTeamFullThreads, true>, grid, kTeamFullThreads, team_full_smem_bytes(s.k, s.m), stream, s,
-               st, b);
+               st, b, pc);
   else
-    launch_pdl(k_resolve_team<kTeamThreads, false>, grid, kTeamThreads, team_smem_bytes(s.k, s.m), stream, s, st, b);
+    launch_pdl(k_resolve_team<kTeamThreads, false>, grid, kTeamThreads, team_smem_bytes(s.k, s.m), stream, s, st, b,
+               pc);
 }
 
 void launch_step_team_full(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream) {
@@ -2786,6 +2924,17 @@ void launch_pad(const uint32_t *src, uint32_t w, uint32_t h, uint32_t levels, ui
   const size_t n = (size_t)pitch * (h + 2 * kPad) * levels;
   if (n == 0) return;
   k_pad<<<(uint32_t)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, stream>>>(src, w, h, levels, pitch, dst);
+}
+
+void launch_tree_append(const SessionDev &s, const StageDev &st, uint32_t a0, uint32_t a1, uint32_t pos0,
+                        uint32_t nomir_end, cudaStream_t stream) {
+  if (a1 <= a0) return;
+  launch_pdl(k_tree_append, cdiv(a1 - a0, 256), 256, 0, stream, s, st, a0, a1, pos0, nomir_end);
+}
+
+void launch_rank_init(const SessionDev &s, uint32_t n, cudaStream_t stream) {
+  if (n == 0) return;
+  k_rank_init<<<cdiv(n, 256), 256, 0, stream>>>(s, n);
 }
 
 void launch_scatter_init(const uint32_t *list, uint32_t n, uint32_t *color, uint4 *state, uint32_t *res,

@@ -102,6 +102,18 @@ struct SessionDev {
   uint32_t *cells;
   int32_t cox, coy;
   uint32_t cgw, cgh;
+  // Tree positions, for k-NN made ahead of the resolves (plain path,
+  // k_tree_append): rank[p] = 1 + p's index in the resolved list, 0 while p
+  // has none.  The bitmap, mirror bits, cell counts and resolved list then
+  // already hold the points of whole chunks of later batches; a point is in
+  // an item's tree when its index is below the item's batch-start length.
+  // Null: the bitmap is the tree itself (commits grow it).
+  uint32_t *rank;
+  // k-NN ahead: for the pixels whose commit a batch step left to the next
+  // step's resolve launch (BatchDev::defer_tag), the colour and state that
+  // commit writes: shadow[2p] = {tag, colour, 0, 0}, shadow[2p + 1] = state;
+  // zeroed at the start
+  uint4 *shadow;
 };
 
 constexpr int kCell = 8;
@@ -139,6 +151,17 @@ struct BatchDev {
   int grid_first;        // sparse step: search the cell grid without walking the offset table first
   int walk_window;       // small step (latency-bound): the single-session walk lets sparse items walk a shared-memory bitmap window
   int fused_commit;      // only new items: the resolve kernels commit each item themselves (no k_commit)
+  // k-NN made ahead over several batches (SessionDev::rank): btab[j] =
+  // {first stage item, resolved-list length at the start} of the j-th batch
+  // the launch covers, ascending; null: every item's tree has n_res points
+  const uint2 *btab;
+  uint32_t nbt;
+  // Commit of a batch left to the next step (k-NN ahead): a launch with
+  // defer_tag != 0 keeps its results in res and their colour and state in
+  // SessionDev::shadow under that tag; the next batch step (prev_tag == the
+  // tag) commits them while it runs (PendingCommit) and reads a tagged
+  // pixel's batch-start colour and state from the shadow instead of the image
+  uint32_t defer_tag, prev_tag;
 };
 
 // One batch step of one session as the multi-session kernels read it.
@@ -229,11 +252,13 @@ void launch_knn_walk(const SessionDev &s, const StageDev &st, const BatchDev &b,
 void launch_knn_exhaustive(const SessionDev &s, const StageDev &st, const BatchDev &b, bool all_items,
                            cudaStream_t stream, const PendingCommit &pc = PendingCommit{});
 void launch_mean(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
-void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream);
+void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream,
+                    const PendingCommit &pc = PendingCommit{});
 // One CTA per item; `full` scores every candidate completely (lowest latency,
 // for batches far too small to fill the GPU), otherwise candidate 0 first
 // and the rest with early exit.
-void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev &b, bool full, cudaStream_t stream);
+void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev &b, bool full, cudaStream_t stream,
+                         const PendingCommit &pc = PendingCommit{});
 // One step of a batch whose neighbours the exhaustive k-NN finds, resolved
 // in the full-evaluation team form (when team_full_fits): both in one
 // launch, one CTA per item.
@@ -244,6 +269,13 @@ void launch_level_switch(const SessionDev &s, uint32_t level, uint32_t n_res, cu
 // Initial state of the pixels set before the first stage (random init):
 // list[6i..6i+6] = {pixel, colour, state.x, state.y, state.z, state.w};
 // res[i] = pixel (the resolved list starts with them, in list order).
+// k-NN ahead (SessionDev::rank): the tree entries of stage items [a0, a1),
+// every one appended at resolved-list index pos0 + (i - a0); items below
+// nomir_end (a batch that met an empty tree) get no tiling mirrors.
+void launch_tree_append(const SessionDev &s, const StageDev &st, uint32_t a0, uint32_t a1, uint32_t pos0,
+                        uint32_t nomir_end, cudaStream_t stream);
+// rank of the first n resolved-list entries (the initial tree).
+void launch_rank_init(const SessionDev &s, uint32_t n, cudaStream_t stream);
 void launch_scatter_init(const uint32_t *list, uint32_t n, uint32_t *color, uint4 *state, uint32_t *res,
                          cudaStream_t stream);
 

@@ -22,13 +22,15 @@
 #include <condition_variable>
 #include <deque>
 #include <functional>
+#include <map>
+#include <memory>
 #include <mutex>
 #include <unordered_map>
-#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
 
+#include <cuda.h>  // green-context types (entry points through cudaGetDriverEntryPointByVersion)
 #include <cuda_runtime.h>
 
 #include "../../include/tsgpu.h"
@@ -1290,6 +1292,23 @@ struct Step {
   bool exhaustive = false;       // exhaustive k-NN over the whole batch
   int resolve = kPhaseResolve;   // kPhaseResolve, kPhaseTeamPart or kPhaseTeamFull
   uint32_t n = 0;                // items of the batch
+  uint32_t stage_i0 = 0;         // the batch's first item within its stage
+  uint32_t bidx = 0;             // index of the batch in the run (RunCtx::btab)
+  int knn_wait = -1;             // k-NN ahead: the chunk whose k-NN this step waits for first
+};
+
+// k-NN made ahead of the resolves (RunCtx::knn_ahead): consecutive batch
+// steps of one stage whose neighbour lists one launch (or a walk and its
+// fallback launch) computes on the k-NN stream.
+struct KnnChunk {
+  int stage = 0;
+  StageDev st{};                // the stage's items
+  BatchDev b{};                 // stage items [b.i0, b.i1); each item's tree length from b.btab
+  bool all_exhaustive = false;  // exhaustive k-NN for every item (else the walk, then its fallbacks)
+  // tree entries of the chunk's appended items, made just before its k-NN:
+  // items [a0, a1) at resolved-list index pos0 on; none below nomir_end
+  // gets tiling mirrors
+  uint32_t a0 = 0, a1 = 0, pos0 = 0, nomir_end = 0;
 };
 
 // Everything one run holds between planning and reading back.
@@ -1326,6 +1345,23 @@ struct RunCtx {
   bool want_rc_ahead = false, rc_ahead = false;
   std::vector<int> rc_step;
   std::vector<EventHandle> rc_ev;
+  // knn_ahead: the neighbour lists and means of every batch are made on a
+  // k-NN stream, chunk by chunk, as soon as a stage's items are up (they
+  // depend on the pick chain's order only: which pixels are in the tree at
+  // each batch start); the resolves wait for their chunk's event.  Plain
+  // path, k > 0, exact distance sums.
+  bool want_knn_ahead = false, knn_ahead = false;
+  std::vector<KnnChunk> knn_chunks;
+  std::vector<EventHandle> knn_ev;  // per chunk: its k-NN is done
+  std::vector<EventHandle> items_ev;  // per stage: its items are on the device
+  std::vector<uint2> btab;          // every batch: {first stage item, tree length at its start}
+  // knn_ahead: a batch step whose commit the next step's resolve launch
+  // makes (its results in one of two result buffers, alternating)
+  bool pend = false;
+  int pend_stage = -1;
+  StageDev pend_st{};
+  BatchDev pend_bd{};
+  uint32_t pend_n = 0, defer_parity = 0;
   size_t res_total = 0;                // resolved-list length at the end of the run
   std::vector<uint32_t> unresolved;    // pixels not yet picked (the pick chain's state)
   size_t picked_stages = 0;            // stages whose items are known
@@ -1346,6 +1382,11 @@ struct RunCtx {
   std::vector<TabPart> tab_parts;
   PinnedBuf<uint8_t> ptab;
   DevBuf<uint32_t> d_color, d_occ, d_mir, d_res, d_items, d_ncnt, d_fbl, d_fbc, d_cells, d_init;
+  DevBuf<uint32_t> d_rank, d_kncnt, d_kfbl, d_kfbc;  // knn_ahead
+  DevBuf<int32_t> d_knbuf;
+  DevBuf<double> d_kmean;
+  DevBuf<uint2> d_btab;
+  DevBuf<uint4> d_shadow;
   DevBuf<uint4> d_state;
   DevBuf<float> d_rscore, d_lut;
   DevBuf<double> d_xdiv, d_ydiv, d_dist, d_dxt, d_dy2t, d_mean;
@@ -1742,6 +1783,75 @@ bool exact_sum_ok(uint32_t W, uint32_t H, uint32_t k) {
   return M <= (1u << 16) && 32ull * std::max<uint32_t>(k, 1) * M * M < (1ull << 53);
 }
 
+// Side streams of a run (the k-NN and random candidates made ahead) run on a
+// green context that holds all SMs but kReservedSms.  A running block cannot
+// be preempted, so side blocks on every SM would hold up each launch of the
+// resolve chain, which in the first stage is a long chain of small
+// latency-bound launches; the reserved SMs take those at once.  Created once
+// per device and kept; where the driver offers no green contexts the side
+// streams are ordinary (low-priority) streams.
+constexpr unsigned kReservedSms = 16;
+
+struct GreenSide {
+  bool ok = false;
+  CUgreenCtx g = nullptr;
+  CUresult (*stream_create)(CUstream *, CUgreenCtx, unsigned, int) = nullptr;
+};
+
+template <typename F>
+bool driver_entry(const char *name, F &fn) {
+  void *v = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &v, 13000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !v)
+    return false;
+  fn = (F)v;
+  return true;
+}
+
+const GreenSide &green_side(int dev) {
+  static std::mutex mu;
+  static std::map<int, GreenSide> sides;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = sides.find(dev);
+  if (it != sides.end()) return it->second;
+  GreenSide &gs = sides[dev];
+  CUresult (*device_get)(CUdevice *, int) = nullptr;
+  CUresult (*get_resource)(CUdevice, CUdevResource *, CUdevResourceType) = nullptr;
+  CUresult (*split)(CUdevResource *, unsigned *, const CUdevResource *, CUdevResource *, unsigned, unsigned) = nullptr;
+  CUresult (*make_desc)(CUdevResourceDesc *, CUdevResource *, unsigned) = nullptr;
+  CUresult (*create)(CUgreenCtx *, CUdevResourceDesc, CUdevice, unsigned) = nullptr;
+  if (!driver_entry("cuDeviceGet", device_get) || !driver_entry("cuDeviceGetDevResource", get_resource) ||
+      !driver_entry("cuDevSmResourceSplitByCount", split) || !driver_entry("cuDevResourceGenerateDesc", make_desc) ||
+      !driver_entry("cuGreenCtxCreate", create) || !driver_entry("cuGreenCtxStreamCreate", gs.stream_create))
+    return gs;
+  CUdevice cd;
+  CUdevResource all{}, part{}, rest{};
+  unsigned groups = 1;
+  CUdevResourceDesc desc;
+  if (device_get(&cd, dev) != CUDA_SUCCESS || get_resource(cd, &all, CU_DEV_RESOURCE_TYPE_SM) != CUDA_SUCCESS ||
+      all.sm.smCount <= kReservedSms + all.sm.minSmPartitionSize)
+    return gs;
+  if (split(&part, &groups, &all, &rest, 0, all.sm.smCount - kReservedSms) != CUDA_SUCCESS || groups != 1 ||
+      part.sm.smCount >= all.sm.smCount || make_desc(&desc, &part, 1) != CUDA_SUCCESS ||
+      create(&gs.g, desc, cd, CU_GREEN_CTX_DEFAULT_STREAM) != CUDA_SUCCESS)
+    return gs;
+  gs.ok = true;
+  return gs;
+}
+
+// A side stream of priority prio on the device's green context (green_side),
+// else an ordinary one.
+cudaError_t side_stream(int dev, int prio, cudaStream_t *out) {
+  const GreenSide &gs = green_side(dev);
+  CUstream cs = nullptr;
+  if (gs.ok && gs.stream_create(&cs, gs.g, CU_STREAM_NON_BLOCKING, prio) == CUDA_SUCCESS) {
+    *out = (cudaStream_t)cs;
+    return cudaSuccess;
+  }
+  return cudaStreamCreateWithPriority(out, cudaStreamNonBlocking, prio);
+}
+
 // Device buffers of a run and the step descriptors that point into them.
 // With a pool stream, the buffers are stream-ordered pool memory (freed
 // without waiting for the device); otherwise plain cudaMalloc.
@@ -1769,9 +1879,48 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   } zl, tl, wl;
   const size_t kk = std::max<uint32_t>(k, 1), mb = max_batch_items;
   const size_t rc_n = c.rc_ahead ? c.items.size() * m : (size_t)std::max<uint64_t>(rc_items, mb) * m;
+  // k-NN ahead: the batch table and the chunks (consecutive batches of a
+  // stage with one k-NN form, each at least as large as the stage's items
+  // before it, so that a chunk's k-NN overlaps the resolves of the ones
+  // before)
+  c.knn_ahead = c.want_knn_ahead && k > 0 && exact_sum_ok(W, H, k);
+  c.btab.clear();
+  c.knn_chunks.clear();
+  std::vector<std::pair<uint32_t, uint32_t>> chunk_batches;  // [first, last) batch of each chunk
+  std::vector<uint32_t> stage_bt_base(plan.size(), 0);        // each stage's first batch
+  if (c.knn_ahead) {
+    constexpr uint32_t kChunkMinItems = 64;
+    for (size_t si = 0; si < plan.size(); ++si) {
+      const StagePlan &sp = plan[si];
+      const uint32_t bt_base = stage_bt_base[si] = (uint32_t)c.btab.size();
+      for (const BatchPlan &bp : sp.batches) c.btab.push_back(make_uint2(bp.i0, bp.n_res));
+      auto form = [&](const BatchPlan &bp) {
+        return (bp.exhaustive ? 1 : 0) | (bp.grid_first ? 2 : 0) | ((bp.i1 - bp.i0) <= p.walk_window_max ? 4 : 0);
+      };
+      uint32_t covered = 0;
+      size_t j = 0;
+      while (j < sp.batches.size()) {
+        const size_t j0 = j;
+        uint32_t items = 0;
+        while (j < sp.batches.size() && form(sp.batches[j]) == form(sp.batches[j0]) &&
+               (j == j0 || items < std::max(kChunkMinItems, covered))) {
+          items += sp.batches[j].i1 - sp.batches[j].i0;
+          ++j;
+        }
+        chunk_batches.push_back({bt_base + (uint32_t)j0, bt_base + (uint32_t)j});
+        KnnChunk ch;
+        ch.stage = (int)si;
+        c.knn_chunks.push_back(ch);
+        covered += items;
+      }
+    }
+  }
+  const size_t n_chunks = c.knn_chunks.size(), n_kitems = c.knn_ahead ? c.items.size() : 0;
   // zeroed: colour and state first (uploaded instead when dense_init)
   const size_t z_color = zl.add(N * 4), z_state = zl.add(N * sizeof(uint4)), z_rscore = zl.add(c.res_total * 4),
-               z_fbc = zl.add(c.n_batches * 4), z_err = zl.add(sizeof(int)), z_evals = zl.add(8);
+               z_fbc = zl.add(c.n_batches * 4), z_err = zl.add(sizeof(int)), z_evals = zl.add(8),
+               z_rank = zl.add(c.knn_ahead ? N * 4 : 0), z_kfbc = zl.add(n_chunks * 4),
+               z_shadow = zl.add(c.knn_ahead ? 2 * N * sizeof(uint4) : 0);
   // uploaded tables
   c.tab_parts.clear();
   auto T = [&](const auto &v) {
@@ -1781,11 +1930,14 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
     return o;
   };
   const size_t t_lut = T(c.luts), t_tab = T(c.tab), t_xdiv = T(c.xdiv), t_ydiv = T(c.ydiv), t_dxt = T(c.dxt),
-               t_dy2t = T(c.dy2t), t_cells = T(c.cells), t_occ = T(c.occ), t_mir = T(c.mir), t_init = T(c.init_list);
+               t_dy2t = T(c.dy2t), t_cells = T(c.cells), t_occ = T(c.occ), t_mir = T(c.mir), t_init = T(c.init_list),
+               t_btab = T(c.btab);
   // scratch
   const size_t w_res = wl.add(c.res_total * 4), w_items = wl.add(c.items.size() * 4), w_nbuf = wl.add(mb * kk * 4),
                w_ncnt = wl.add(mb * 4), w_dist = wl.add(mb * kk * 8), w_mean = wl.add(mb * 8), w_fbl = wl.add(mb * 4),
-               w_result = wl.add(mb * sizeof(Result)), w_rcand = wl.add(rc_n * 8);
+               w_result = wl.add((c.knn_ahead ? 2 : 1) * mb * sizeof(Result)), w_rcand = wl.add(rc_n * 8),
+               w_knbuf = wl.add(n_kitems * kk * 4), w_kncnt = wl.add(n_kitems * 4), w_kmean = wl.add(n_kitems * 8),
+               w_kfbl = wl.add(n_kitems * 4);
   CUDA_TRY(A(c.d_zero, zl.off));
   CUDA_TRY(A(c.d_tabs, tl.off));
   CUDA_TRY(A(c.d_work, wl.off));
@@ -1808,6 +1960,14 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   c.d_occ.view(tb + t_occ, c.occ.size());
   c.d_mir.view(tb + t_mir, c.mir.size());
   c.d_init.view(tb + t_init, c.init_list.size());
+  c.d_btab.view(tb + t_btab, c.btab.size());
+  c.d_rank.view(z + z_rank, c.knn_ahead ? N : 0);
+  c.d_shadow.view(z + z_shadow, c.knn_ahead ? 2 * N : 0);
+  c.d_kfbc.view(z + z_kfbc, n_chunks);
+  c.d_knbuf.view(wk + w_knbuf, n_kitems * kk);
+  c.d_kncnt.view(wk + w_kncnt, n_kitems);
+  c.d_kmean.view(wk + w_kmean, n_kitems);
+  c.d_kfbl.view(wk + w_kfbl, n_kitems);
   c.d_res.view(wk + w_res, c.res_total);
   c.d_items.view(wk + w_items, c.items.size());
   c.d_nbuf.view(wk + w_nbuf, mb * kk);
@@ -1815,7 +1975,7 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   c.d_dist.view(wk + w_dist, mb * kk);
   c.d_mean.view(wk + w_mean, mb);
   c.d_fbl.view(wk + w_fbl, mb);
-  c.d_result.view(wk + w_result, mb);
+  c.d_result.view(wk + w_result, (c.knn_ahead ? 2 : 1) * mb);
   c.d_rcand.view(wk + w_rcand, rc_n);
   const std::vector<int32_t> &tab = c.tab;
 
@@ -1879,9 +2039,13 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   sd.coy = c.coy;
   sd.cgw = c.cgw;
   sd.cgh = c.cgh;
+  sd.rank = c.knn_ahead ? c.d_rank.p : nullptr;
+  sd.shadow = c.knn_ahead ? c.d_shadow.p : nullptr;
+  c.pend = false;
 
   // ---- the steps ----
   size_t fb_index = 0;
+  uint32_t bidx = 0;
   c.rc_step.assign(plan.size(), -1);
   for (size_t si = 0; si < plan.size(); ++si) {
     const StagePlan &sp = plan[si];
@@ -1939,6 +2103,14 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
         bd.mean = c.d_mean.p;
         bd.res = c.d_result.p;
         stp.n = bp.i1 - bp.i0;
+        stp.stage_i0 = bp.i0;
+        stp.bidx = bidx++;
+        if (c.knn_ahead) {  // the chunk's lists, made ahead on the k-NN stream
+          const size_t g0 = (size_t)sp.items_off + bp.i0;
+          bd.nbuf = c.d_knbuf.p + g0 * kk;
+          bd.ncnt = c.d_kncnt.p + g0;
+          bd.mean = c.d_kmean.p + g0;
+        }
         stp.exhaustive = bp.exhaustive;
         bd.grid_first = bp.grid_first ? 1 : 0;
         bd.walk_window = (bp.i1 - bp.i0) <= p.walk_window_max ? 1 : 0;
@@ -1955,6 +2127,49 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
     }
     if (c.steps.size() == first) c.steps.push_back(pending);  // a stage without batches
     c.steps.back().stage_end = true;
+  }
+  // ---- the k-NN chunks ----
+  if (c.knn_ahead) {
+    std::vector<size_t> step_of(c.btab.size(), 0);
+    for (size_t t = 0; t < c.steps.size(); ++t)
+      if (c.steps[t].batch) step_of[c.steps[t].bidx] = t;
+    for (size_t q = 0; q < c.knn_chunks.size(); ++q) {
+      KnnChunk &ch = c.knn_chunks[q];
+      const StagePlan &sp = plan[ch.stage];
+      const uint32_t bt0 = chunk_batches[q].first, bt1 = chunk_batches[q].second;
+      c.steps[step_of[bt0]].knn_wait = (int)q;
+      // the chunk's batches as indices into the stage's list
+      const size_t sb0 = bt0 - stage_bt_base[ch.stage], sb1 = bt1 - stage_bt_base[ch.stage];
+      const BatchPlan &b0 = sp.batches[sb0], &bl = sp.batches[sb1 - 1];
+      ch.st = StageDev{};
+      ch.st.level = sp.level;
+      ch.st.stage_seed = sp.seed;
+      ch.st.items = c.d_items.p + sp.items_off;
+      ch.st.n_items = sp.n_items;
+      ch.st.redo = sp.redo;
+      BatchDev &kb = ch.b;
+      kb = BatchDev{};
+      kb.i0 = b0.i0;
+      kb.i1 = bl.i1;
+      kb.n_res = bl.n_res;  // the largest tree of the chunk (sizes the exhaustive key buffer)
+      kb.append_from = kb.i1;
+      const size_t g0 = (size_t)sp.items_off + kb.i0;
+      kb.nbuf = c.d_knbuf.p + g0 * kk;
+      kb.ncnt = c.d_kncnt.p + g0;
+      kb.mean = c.d_kmean.p + g0;
+      kb.fb_list = c.d_kfbl.p + g0;
+      kb.fb_count = c.d_kfbc.p + q;
+      kb.grid_first = b0.grid_first ? 1 : 0;
+      kb.walk_window = (b0.i1 - b0.i0) <= p.walk_window_max ? 1 : 0;
+      kb.btab = c.d_btab.p + bt0;
+      kb.nbt = bt1 - bt0;
+      ch.all_exhaustive = b0.exhaustive;
+      ch.a0 = std::max(kb.i0, sp.redo);
+      ch.a1 = std::max(kb.i1, sp.redo);
+      ch.pos0 = sp.n_res_start + (ch.a0 - sp.redo);
+      for (size_t j = sb0; j < sb1; ++j)
+        if (sp.batches[j].n_res == 0) ch.nomir_end = std::max(ch.nomir_end, sp.batches[j].i1);
+    }
   }
 }
 
@@ -1990,7 +2205,7 @@ void run_upload(RunCtx &c, cudaStream_t st) {
     launch_scatter_init(c.d_init.p, (uint32_t)(c.init_list.size() / 6), c.d_color.p, c.d_state.p, c.d_res.p, st);
     ++c.launches;
   }
-  if (!c.items.empty() && c.picked_stages == c.plan.size() && !c.items_async)
+  if (!c.items_async && !c.items.empty() && c.picked_stages == c.plan.size())
     CUDA_TRY(cudaMemcpyAsync(c.d_items.p, c.items.data(), c.items.size() * 4, cudaMemcpyHostToDevice, st));
 }
 
@@ -2003,6 +2218,98 @@ bool can_defer_commit(const RunCtx &c, const Step &stp, const Step *next) {
   if (!stp.batch || stp.bd.fused_commit || c.k == 0 || stp.bd.append_from < stp.bd.i1) return false;
   if (!next || !next->batch || next->ls || next->stage != stp.stage) return false;
   return !(next->exhaustive && next->resolve == kPhaseTeamFull && team_full_fits(c.sd.k, c.sd.m));
+}
+
+// k-NN ahead: the chunks of stage `stage` on the k-NN stream kst, once its
+// items are up: each chunk's tree entries, then its neighbour lists and
+// means, then its event.
+void run_enqueue_knn(RunCtx &c, cudaStream_t kst, LaunchTimer &lt, int stage) {
+  const SessionDev &sd = c.sd;
+  const cudaStream_t main_st = lt.st;
+  lt.st = kst;
+  for (size_t q = 0; q < c.knn_chunks.size(); ++q) {
+    const KnnChunk &ch = c.knn_chunks[q];
+    if (ch.stage != stage) continue;
+    lt.items = ch.b.i1 - ch.b.i0;
+    if (ch.a1 > ch.a0) {
+      lt.run(TS_KERNEL_COMMIT, [&] { launch_tree_append(sd, ch.st, ch.a0, ch.a1, ch.pos0, ch.nomir_end, kst); });
+      ++c.launches;
+    }
+    if (ch.all_exhaustive) {
+      lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, ch.st, ch.b, true, kst, PendingCommit{}); });
+      ++c.launches;
+    } else {
+      lt.run(TS_KERNEL_KNN_WALK, [&] { launch_knn_walk(sd, ch.st, ch.b, kst, PendingCommit{}); });
+      lt.run(TS_KERNEL_KNN_EXHAUSTIVE, [&] { launch_knn_exhaustive(sd, ch.st, ch.b, false, kst, PendingCommit{}); });
+      c.launches += 2;
+    }
+    CUDA_TRY(cudaEventCreateWithFlags(&c.knn_ev[q].e, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventRecord(c.knn_ev[q].e, kst));
+  }
+  lt.st = main_st;
+}
+
+// k-NN ahead: the commit a batch step left to the next step, as its own
+// launch (before a level switch, at a stage's end).
+void commit_pending(RunCtx &c, cudaStream_t st, LaunchTimer &lt) {
+  if (!c.pend) return;
+  lt.items = c.pend_n;
+  lt.run(TS_KERNEL_COMMIT, [&] { launch_commit(c.sd, c.pend_st, c.pend_bd, st); });
+  ++c.launches;
+  c.pend = false;
+}
+
+// k-NN ahead: step t on the main stream.  Its neighbour lists come from the
+// k-NN stream (the step waits for its chunk's event first), so a batch step
+// is its resolve launch alone: a batch of new items commits inside it; any
+// other batch keeps its results and tags their pixels, and the next batch
+// step's launch commits them while it runs, its readers taking those pixels'
+// batch-start values from the kept results.
+void enqueue_step_ahead(RunCtx &c, size_t t, cudaStream_t st, LaunchTimer &lt) {
+  const SessionDev &sd = c.sd;
+  const Step &stp = c.steps[t];
+  if (c.pend && (stp.ls || !stp.batch || stp.stage != c.pend_stage)) commit_pending(c, st, lt);
+  if (stp.knn_wait >= 0) CUDA_TRY(cudaStreamWaitEvent(st, c.knn_ev[stp.knn_wait].e, 0));
+  if (stp.ls) {
+    lt.run(TS_KERNEL_LEVEL_SWITCH, [&] { launch_level_switch(sd, stp.ls_level, stp.ls_n_res, st); });
+    ++c.launches;
+  }
+  if (stp.rc) {
+    if (c.rc_ahead) {
+      CUDA_TRY(cudaStreamWaitEvent(st, c.rc_ev[stp.stage].e, 0));
+    } else {
+      lt.run(TS_KERNEL_RANDOM_CANDIDATES, [&] { launch_random_candidates(sd, stp.rc_st, st); });
+      ++c.launches;
+    }
+  }
+  if (!stp.batch) return;
+  BatchDev bd = stp.bd;
+  PendingCommit pc{};
+  if (c.pend) {
+    pc.st = c.pend_st;
+    pc.b = c.pend_bd;
+    pc.n = c.pend_n;
+    bd.prev_tag = c.pend_bd.defer_tag;
+  }
+  if (!bd.fused_commit) {
+    bd.defer_tag = (uint32_t)t + 1;
+    bd.res = c.d_result.p + (c.defer_parity ? c.max_batch_items : 0);
+    c.defer_parity ^= 1u;
+  }
+  lt.items = stp.n;
+  if (stp.resolve == kPhaseResolve)
+    lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve(sd, stp.st, bd, st, pc); });
+  else
+    lt.run(TS_KERNEL_RESOLVE, [&] { launch_resolve_team(sd, stp.st, bd, stp.resolve == kPhaseTeamFull, st, pc); });
+  c.launches += 1;
+  c.pend = !bd.fused_commit;
+  if (c.pend) {
+    c.pend_st = stp.st;
+    c.pend_bd = bd;
+    c.pend_bd.prev_tag = 0;
+    c.pend_n = stp.n;
+    c.pend_stage = stp.stage;
+  }
 }
 
 // The launches of one step of one session, with the single-session
@@ -2085,9 +2392,14 @@ void run_enqueue_plain(RunCtx &c, cudaStream_t st, LaunchTimer &lt, ts_progress_
     const StagePlan &sp = c.plan[stp.stage];
     lt.stage = sp.p_stage;
     lt.items = sp.n_items;
-    const bool defer = can_defer_commit(c, stp, i + 1 < c.steps.size() ? &c.steps[i + 1] : nullptr);
-    enqueue_step(c, stp, st, lt, pending, defer);
-    pending = defer ? &stp : nullptr;
+    if (c.knn_ahead) {
+      enqueue_step_ahead(c, i, st, lt);
+      if (stp.stage_end) commit_pending(c, st, lt);  // nothing waits across a stage's end
+    } else {
+      const bool defer = can_defer_commit(c, stp, i + 1 < c.steps.size() ? &c.steps[i + 1] : nullptr);
+      enqueue_step(c, stp, st, lt, pending, defer);
+      pending = defer ? &stp : nullptr;
+    }
     if (stp.batch) {
       ++c.batches;
       c.resolves += stp.n;
@@ -2183,14 +2495,38 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
   const auto t_wall0 = std::chrono::steady_clock::now();
   StreamGuard sg;  // declared first: the run's pool buffers are freed on it before it goes
   StreamGuard rg;  // side stream of the random candidates made ahead
+  StreamGuard kg;  // k-NN stream (knn_ahead)
   // the items go up stage by stage from pinned memory, so that the device
   // runs a stage while the host picks the next one
   PinnedBuf<uint32_t> pitems;
   RunCtx c;
+  // The pick chain (pick_random_unresolved, ms.rs:380-389) on its own host
+  // thread from the plan on, stage after stage, so that a stage's picks
+  // never wait behind the launches of the one before; the launching thread
+  // takes each stage once it is picked.  Declared after c: it is joined
+  // before c goes.
+  struct PickThread {
+    std::thread th;
+    std::mutex mu;
+    std::condition_variable cv;
+    size_t done = 0;  // stages picked
+    bool failed = false;
+    Failure fail{};
+    std::atomic<bool> stop{false};
+    ~PickThread() {
+      stop = true;
+      if (th.joinable()) th.join();
+    }
+  } pk;
   try {
     CUDA_TRY(cudaSetDevice(s->prm.device));
     keep_pool(s->prm.device);
-    CUDA_TRY(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
+    // the resolve chain on the highest priority, the work made ahead on the
+    // side streams on the lowest: blocks of the chain's next launch take the
+    // first free SMs
+    int prio_low = 0, prio_high = 0;
+    CUDA_TRY(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+    CUDA_TRY(cudaStreamCreateWithPriority(&sg.s, cudaStreamNonBlocking, prio_high));
     const cudaStream_t st = sg.s;
     if (s->ready.e) CUDA_TRY(cudaStreamWaitEvent(st, s->ready.e, 0));
     auto t = std::chrono::steady_clock::now();
@@ -2201,8 +2537,30 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
       return ms;
     };
     c.want_rc_ahead = true;
+    c.want_knn_ahead = true;
     c.parallel_picks = true;
     run_plan(s, c);
+    c.items_async = true;  // each stage's items go up once the pick thread has them
+    pk.th = std::thread([&c, &pk] {
+      try {
+        for (size_t q = 0; q < c.plan.size() && !pk.stop; ++q) {
+          run_pick(c);
+          std::lock_guard<std::mutex> lk(pk.mu);
+          pk.done = q + 1;
+          pk.cv.notify_one();
+        }
+      } catch (const Failure &f) {
+        std::lock_guard<std::mutex> lk(pk.mu);
+        pk.failed = true;
+        pk.fail = f;
+        pk.cv.notify_one();
+      } catch (...) {
+        std::lock_guard<std::mutex> lk(pk.mu);
+        pk.failed = true;
+        pk.fail = Failure{TS_ERR_OUT_OF_MEMORY, "out of host memory"};
+        pk.cv.notify_one();
+      }
+    });
     const double plan_ms = lap();
     run_alloc(c, st);
     CUDA_TRY(pitems.alloc(c.items.size()));
@@ -2214,13 +2572,24 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     ev_rb.create();
     CUDA_TRY(cudaEventRecord(ev.a, st));
     run_upload(c, st);
+    if (c.knn_ahead) {
+      // the initial tree's positions; the k-NN stream starts after them
+      launch_rank_init(c.sd, (uint32_t)c.locked, st);
+      if (c.locked) ++c.launches;
+      CUDA_TRY(side_stream(s->prm.device, prio_low, &kg.s));
+      c.knn_ev.resize(c.knn_chunks.size());
+      c.items_ev.resize(c.plan.size());
+    }
     CUDA_TRY(cudaEventRecord(ev_up.a, st));
     LaunchTimer lt;
     lt.on = s->prm.profile;
     if (c.rc_ahead) {
       // every stage's random candidates depend on the examples and the
       // stage plan only: a side stream makes them while the first stages run
-      CUDA_TRY(cudaStreamCreateWithFlags(&rg.s, cudaStreamNonBlocking));
+      if (c.knn_ahead)
+        CUDA_TRY(side_stream(s->prm.device, prio_low, &rg.s));
+      else
+        CUDA_TRY(cudaStreamCreateWithPriority(&rg.s, cudaStreamNonBlocking, prio_low));
       EventHandle fork;
       CUDA_TRY(cudaEventCreateWithFlags(&fork.e, cudaEventDisableTiming));
       CUDA_TRY(cudaEventRecord(fork.e, st));
@@ -2239,13 +2608,28 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
       }
     }
     lt.st = st;
+    double pick_ms = 0.0;
     for (size_t si = 0; si < c.plan.size(); ++si) {
-      run_pick(c);
+      const auto p0 = std::chrono::steady_clock::now();
+      {
+        std::unique_lock<std::mutex> lk(pk.mu);
+        pk.cv.wait(lk, [&] { return pk.done > si || pk.failed; });
+        if (pk.done <= si) throw pk.fail;
+      }
+      pick_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - p0).count();
       const StagePlan &sp = c.plan[si];
       if (sp.n_items) {
         memcpy(pitems.p + sp.items_off, c.items.data() + sp.items_off, (size_t)sp.n_items * 4);
         CUDA_TRY(cudaMemcpyAsync(c.d_items.p + sp.items_off, pitems.p + sp.items_off, (size_t)sp.n_items * 4,
                                  cudaMemcpyHostToDevice, st));
+      }
+      if (c.knn_ahead) {
+        // the stage's neighbour lists on the k-NN stream, from its items on
+        CUDA_TRY(cudaEventCreateWithFlags(&c.items_ev[si].e, cudaEventDisableTiming));
+        CUDA_TRY(cudaEventRecord(c.items_ev[si].e, st));
+        CUDA_TRY(cudaStreamWaitEvent(kg.s, c.items_ev[si].e, 0));
+        lt.stage = sp.p_stage;
+        run_enqueue_knn(c, kg.s, lt, (int)si);
       }
       run_enqueue_plain(c, st, lt, progress, user, (int)si);
     }
@@ -2259,6 +2643,8 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     c.g->stats.host_plan_ms = plan_ms;
     c.g->stats.host_alloc_ms = alloc_ms;
     c.g->stats.host_enqueue_ms = enqueue_ms;
+    c.g->stats.host_pick_ms = pick_ms;
+    c.g->stats.host_launch_ms = enqueue_ms - pick_ms;
     c.g->stats.host_wait_ms = wait_ms;
     c.g->stats.host_finish_ms = lap();
     c.g->stats.gpu_ms = ev.ms();
@@ -2272,6 +2658,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     lt.collect(c.g->stats, c.g->launches);
   } catch (const Failure &f) {
     // nothing of the run may be in flight when its buffers go
+    if (kg.s) cudaStreamSynchronize(kg.s);
     if (rg.s) cudaStreamSynchronize(rg.s);
     if (sg.s) cudaStreamSynchronize(sg.s);
     s->err = f.msg;
