@@ -158,6 +158,10 @@ typedef struct ts_run_stats {
    * the rest (uploads, launches and stream-order calls, and the read-back
    * copies, which wait for the device). */
   double host_pick_ms, host_launch_ms;
+  /* Chunks of batches whose neighbour lists were made ahead on a side
+   * stream (power-of-two outputs with k > 0); 0 when every batch step made
+   * its own. */
+  uint64_t knn_chunks;
 } ts_run_stats;
 
 const char *ts_status_str(int status);

@@ -79,7 +79,8 @@ class RunStats(C.Structure):
                 ("wall_ms", C.c_double), ("kernel_count", C.c_uint64 * 8), ("kernel_ms", C.c_double * 8),
                 ("host_plan_ms", C.c_double), ("host_alloc_ms", C.c_double), ("host_enqueue_ms", C.c_double),
                 ("host_wait_ms", C.c_double), ("host_finish_ms", C.c_double), ("upload_ms", C.c_double),
-                ("readback_ms", C.c_double), ("host_pick_ms", C.c_double), ("host_launch_ms", C.c_double)]
+                ("readback_ms", C.c_double), ("host_pick_ms", C.c_double), ("host_launch_ms", C.c_double),
+                ("knn_chunks", C.c_uint64)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_ if not f.startswith("kernel_") or f == "kernel_launches"}

@@ -2645,6 +2645,7 @@ extern "C" int ts_session_run(ts_session *s, ts_progress_fn progress, void *user
     c.g->stats.host_enqueue_ms = enqueue_ms;
     c.g->stats.host_pick_ms = pick_ms;
     c.g->stats.host_launch_ms = enqueue_ms - pick_ms;
+    c.g->stats.knn_chunks = c.knn_chunks.size();
     c.g->stats.host_wait_ms = wait_ms;
     c.g->stats.host_finish_ms = lap();
     c.g->stats.gpu_ms = ev.ms();
