@@ -1790,7 +1790,7 @@ bool exact_sum_ok(uint32_t W, uint32_t H, uint32_t k) {
 // latency-bound launches; the reserved SMs take those at once.  Created once
 // per device and kept; where the driver offers no green contexts the side
 // streams are ordinary (low-priority) streams.
-constexpr unsigned kReservedSms = 16;
+constexpr unsigned kReservedSms = 8;
 
 struct GreenSide {
   bool ok = false;
@@ -2871,7 +2871,12 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
   size_t current = 0;
   try {
     CUDA_TRY(cudaSetDevice(b->device));
-    CUDA_TRY(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
+    // the step chain on the highest priority, the side stream's work on the
+    // lowest and (unless the launches are captured into a graph) on the
+    // green context that leaves SMs to the chain (side_stream)
+    int prio_low = 0, prio_high = 0;
+    CUDA_TRY(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+    CUDA_TRY(cudaStreamCreateWithPriority(&sg.s, cudaStreamNonBlocking, prio_high));
     const cudaStream_t st = sg.s;
     size_t max_steps = 0;
     const auto t_plan0 = std::chrono::steady_clock::now();
@@ -3122,7 +3127,10 @@ int ts_batch_run(ts_batch *b, ts_generated **out) {
       CUDA_TRY(cudaStreamWaitEvent(st, copies_done.e, 0));
     };
     std::vector<EventHandle> rc_ev(rc_launches.size());
-    CUDA_TRY(cudaStreamCreateWithFlags(&rg.s, cudaStreamNonBlocking));
+    if (b->graph)
+      CUDA_TRY(cudaStreamCreateWithPriority(&rg.s, cudaStreamNonBlocking, prio_low));
+    else
+      CUDA_TRY(side_stream(b->device, prio_low, &rg.s));
     for (auto &e : rc_ev) CUDA_TRY(cudaEventCreateWithFlags(&e.e, cudaEventDisableTiming));
     EventHandle fork, side_done, items_ev[2];
     CUDA_TRY(cudaEventCreateWithFlags(&fork.e, cudaEventDisableTiming));
