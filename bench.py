@@ -55,20 +55,21 @@ PKG = "texture-synthesis_gb300"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
-# resolve family (k_resolve_lean, k_resolve_team, k_step_team_full) on this
-# workload: 1038.7 MB over the 131 resolve launches of one run, from
+# resolve family (k_resolve_lean, k_resolve_team) on this workload: 993.2 MB
+# over the 131 resolve launches of one run (profiles/resolve_dram_multi_example_512.md),
+# from
 #   ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum
-#       --clock-control none -k regex:"k_resolve|k_step_team" --csv python bench.py --once
+#       --clock-control none -k regex:"k_resolve" --csv python bench.py --once
 # (one pass; ncu flushes the caches before each launch, so this is a
 # cold-cache upper bound of the live traffic).
-RESOLVE_DRAM_BYTES_PER_LAUNCH = 1038.67e6 / 131
+RESOLVE_DRAM_BYTES_PER_LAUNCH = 993.2e6 / 131
 # The load path, measured in the unit both kernels share: 32-byte L1 sectors
 # requested per second by global loads (l1tex__t_sectors_pipe_lsu_mem_global_op_ld.sum
-# / gpu__time_duration.sum).  k_resolve_lean on a 13,124-item step of this
+# / gpu__time_duration.sum).  k_resolve_lean on a 26,248-item step of this
 # workload against ts_measure_gather_peak's patch kernel on this workload's
 # table (profiles/k_resolve_lean_multi_example_512.md and
 # profiles/gather_peak_probe_multi_example_512.md, ncu, one launch each).
-LOAD_PATH_SECTORS_PER_S = {"k_resolve_lean": 123.1e9, "gather_probe": 405.4e9}
+LOAD_PATH_SECTORS_PER_S = {"k_resolve_lean": 133.9e9, "gather_probe": 405.4e9}
 
 
 def _peaks():
@@ -515,6 +516,9 @@ def main():
                     help="remix: the headline line (config 1, plus configs 0 and 2, batched and served objects); "
                          "single / guided: config 0 / config 2 alone; gather_peak: the gather ceiling alone")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and served objects of the remix line")
+    ap.add_argument("--out", type=int, default=0,
+                    help="output side of the remix, single or guided workload instead of its own (sides that are "
+                         "not powers of two take the per-step k-NN form; for profilers)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -545,7 +549,11 @@ def main():
                           **measure_served(ts, wl)}))
         return
     spec = {"remix": workload, "single": wl.config0, "guided": wl.config2}[args.workload]()
-    if args.workload != "remix":
+    if args.out:
+        spec["out_w"] = spec["out_h"] = args.out
+        if spec.get("target_guide") is not None:
+            spec["target_guide"] = wl.target_guide(22, args.out, args.out)
+    if args.workload != "remix" or args.out:
         args.no_extra = True
     if args.once:
         g = ts.builder_from_spec(spec).build().run()
