@@ -27,3 +27,7 @@ extern "C" int host_weight_ff(double d, double mean, float *w) { return ts::ts_w
 extern "C" float host_weight_exact(double d, double mean) {
   return (float)ts::ts_exp64(-1.0 * (d / mean), kTab);
 }
+
+// The distance units * 2^qe as a double (ts_units_bits).
+extern "C" double host_units_dbl(uint64_t units, int32_t qe) { return ts::bits_dbl(ts::ts_units_bits(units, qe)); }
+

@@ -37,6 +37,8 @@ def host(tmp_path_factory):
     L.host_weight_ff.argtypes = [C.c_double, C.c_double, C.POINTER(C.c_float)]
     L.host_weight_exact.restype = C.c_float
     L.host_weight_exact.argtypes = [C.c_double, C.c_double]
+    L.host_units_dbl.restype = C.c_double
+    L.host_units_dbl.argtypes = [C.c_uint64, C.c_int32]
     return L
 
 
@@ -213,3 +215,21 @@ def test_non_power_of_two_sums_can_round():
             tree += d
         differ += 4.0 * tree / (4 * k) != _chain_mean(ds)
     assert differ > 0
+
+
+def test_units_distances_and_means(host):
+    """Outputs whose sides are powers of two: a sum of distances is
+    units * 2^qe, built from the integer exactly (ts_units_bits), and the
+    mean RN(4 sum / 4n) comes from integer division (ts_div_int_rn) bit for
+    bit, as the k-NN kernels compute it (exact_mean)."""
+    rng = np.random.default_rng(11)
+    for _ in range(20000):
+        qe = -2 * int(rng.integers(1, 17))
+        units = int(rng.integers(0, 1 << int(rng.integers(1, 53))))
+        d = host.host_units_dbl(units, qe)
+        assert d == math.ldexp(float(units), qe) and float(units) == units
+        n = int(rng.integers(1, 300))
+        ref = (4.0 * d) / float(4 * n)
+        got = host.host_div_int(d, n)
+        assert np.float64(got).view(np.uint64) == np.float64(ref).view(np.uint64), (units, qe, n)
+

@@ -560,6 +560,16 @@ TS_HD bool ts_weight_ff(double d, double mean, const float *tab_ff, float &w) {
   return true;
 }
 
+// units * 2^qe as the bits of a double, exactly (units < 2^53, normal
+// result): the neighbour distances and their sums of outputs whose sides
+// are powers of two, without f64 arithmetic.
+TS_HD uint64_t ts_units_bits(uint64_t units, int32_t qe) {
+  if (units == 0) return 0;
+  const int32_t p = 63 - (int32_t)clz64(units);
+  const uint64_t m = units << (52 - p);
+  return ((uint64_t)(uint32_t)(p + 1023 + qe) << 52) | (m & kFrac52);
+}
+
 #undef TS_FADD
 #undef TS_FSUB
 #undef TS_FMUL

@@ -243,9 +243,10 @@ __device__ __forceinline__ double exact_dist(const SessionDev &s, int32_t off) {
 // The mean from the list's sum in units: below 2^53, so its conversion and
 // the scaling by the power of two exact_q are exact; 4 * that is the
 // reference's in-order sum, divided by 4n and rounded once.
+// Integer arithmetic only (ts_units_bits, ts_div_int_rn): GB300's FP64 pipe
+// is narrow, and an f64 division takes it for a whole warp.
 __device__ __forceinline__ double exact_mean(const SessionDev &s, unsigned long long units, uint32_t n) {
-  const double sum = __dmul_rn(__ull2double_rn(units), s.exact_q);
-  return __ddiv_rn(__dmul_rn(4.0, sum), (double)(n * 4u));
+  return bits_dbl(ts_div_int_rn(ts_units_bits(units, s.exact_qe), n));
 }
 
 __device__ __forceinline__ unsigned long long nb_key(uint32_t d2, int x, int y) {

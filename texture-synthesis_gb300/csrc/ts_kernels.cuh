@@ -93,6 +93,7 @@ struct SessionDev {
   // 1 / max(W, H)^2, exact_sx = 2 log2(max(W, H) / W), exact_sy likewise
   uint32_t exact_sx, exact_sy;
   double exact_q;
+  int32_t exact_qe;  // exact_q = 2^exact_qe
   uint32_t W, H, wpr;  // wpr: 32-bit words per bitmap row
   int tiling;
   int32_t x_l, x_r, y_b, y_t;

@@ -2024,7 +2024,8 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
     };
     sd.exact_sx = 2 * (lg2(M) - lg2(W));
     sd.exact_sy = 2 * (lg2(M) - lg2(H));
-    sd.exact_q = std::ldexp(1.0, -2 * (int)lg2(M));
+    sd.exact_qe = -2 * (int32_t)lg2(M);
+    sd.exact_q = std::ldexp(1.0, sd.exact_qe);
   }
   sd.wpr = wpr;
   sd.tiling = p.tiling ? 1 : 0;
