@@ -890,13 +890,22 @@ __device__ uint32_t knn_exhaustive_item(const SessionDev &s, const StageDev &st,
   const uint32_t nout = n < k ? n : k;
   int32_t *nbo = b.nbuf + (size_t)local * k;
   const uint32_t nb = b.i1 - b.i0;
-  const double x2 = s.xdiv[px + s.xdiv_off], y2 = s.ydiv[py + s.ydiv_off];
+  // the f64 distances from the coordinate tables, where something reads
+  // them: every list of an inexact session, and the caller's weights when the
+  // mean is not made here (exact sums derive the rest from the offsets; runs
+  // with the k-NN made ahead have no coordinate tables)
+  const bool want_d = !s.exact_sum || (with_mean && !mean_here);
+  double x2 = 0.0, y2 = 0.0;
+  if (want_d) {
+    x2 = s.xdiv[px + s.xdiv_off];
+    y2 = s.ydiv[py + s.ydiv_off];
+  }
   unsigned long long part = 0;
   for (uint32_t i = threadIdx.x; i < nout; i += blockDim.x) {
     const unsigned long long key = sorted[i];
     const int x = (int)(key & 0xffffu) - 32768, y = (int)((key >> 16) & 0xffffu) - 32768;
     nbo[i] = pack_off(x - px, y - py);
-    const double d = neighbour_dist(s, px, py, x - px, y - py, x2, y2);
+    const double d = want_d ? neighbour_dist(s, px, py, x - px, y - py, x2, y2) : 0.0;
     if (s.exact_sum)
       part += exact_units(s, x - px, y - py);
     else

@@ -1405,6 +1405,8 @@ struct RunCtx {
   uint64_t launches = 0, batches = 0, resolves = 0;
 };
 
+bool exact_sum_ok(uint32_t W, uint32_t H, uint32_t k);
+
 // Host schedule of Generator::resolve (ms.rs:702-1051) and the device
 // buffers of the run; nothing is enqueued yet.
 void run_plan(ts_session *s, RunCtx &c) {
@@ -1503,7 +1505,8 @@ void run_plan(ts_session *s, RunCtx &c) {
   size_t n_items_total = 0;
   int32_t pyramid_level = 0;
   uint32_t max_batch_items = 1, max_stage_items = 1;
-  c.tab = knn_table(kKnnTabRadius);
+  static const std::vector<int32_t> kTab = knn_table(kKnnTabRadius);  // built once per process
+  c.tab = kTab;
   const std::vector<int32_t> &tab = c.tab;
   for (int32_t ps = (int32_t)stages; ps >= 0; --ps) {
     StagePlan sp;
@@ -1583,20 +1586,24 @@ void run_plan(ts_session *s, RunCtx &c) {
   c.x_l = x_l;
   c.y_b = y_b;
   const int32_t xo = x_l + 2, yo = y_b + 2;
-  c.xdiv.resize(W + 2 * (size_t)xo + 1);
-  c.ydiv.resize(H + 2 * (size_t)yo + 1);
+  // The coordinate tables below serve the f64 distances of inexact sessions
+  // and of the fused small-step kernel; a run whose k-NN is made ahead
+  // (exact sums) derives every distance from its offset and needs none.
+  const bool no_dist_tables = c.want_knn_ahead && k > 0 && exact_sum_ok(W, H, k);
+  c.xdiv.resize(no_dist_tables ? 0 : W + 2 * (size_t)xo + 1);
+  c.ydiv.resize(no_dist_tables ? 0 : H + 2 * (size_t)yo + 1);
   for (size_t i = 0; i < c.xdiv.size(); ++i) c.xdiv[i] = (double)((int64_t)i - xo) / (double)W;
   for (size_t i = 0; i < c.ydiv.size(); ++i) c.ydiv[i] = (double)((int64_t)i - yo) / (double)H;
   // per-pixel tables of the normalised offsets the weights use: dx and
   // dy * dy for |offset| <= kDistTabRadius, the same IEEE operations as
   // get_distances_to_k_neighs (ms.rs:410-415)
   const int32_t R = kDistTabRadius;
-  c.dxt.resize((size_t)W * (2 * R + 1));
-  c.dy2t.resize((size_t)H * (2 * R + 1));
-  for (uint32_t x = 0; x < W; ++x)
+  c.dxt.resize(no_dist_tables ? 0 : (size_t)W * (2 * R + 1));
+  c.dy2t.resize(no_dist_tables ? 0 : (size_t)H * (2 * R + 1));
+  for (uint32_t x = 0; x < W && !no_dist_tables; ++x)
     for (int32_t o = -R; o <= R; ++o)
       c.dxt[(size_t)x * (2 * R + 1) + o + R] = (double)((int64_t)x + o) / (double)W - (double)x / (double)W;
-  for (uint32_t y = 0; y < H; ++y)
+  for (uint32_t y = 0; y < H && !no_dist_tables; ++y)
     for (int32_t o = -R; o <= R; ++o) {
       const double dy = (double)((int64_t)y + o) / (double)H - (double)y / (double)H;
       c.dy2t[(size_t)y * (2 * R + 1) + o + R] = dy * dy;
