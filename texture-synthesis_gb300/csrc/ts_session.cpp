@@ -1407,6 +1407,16 @@ struct RunCtx {
 
 bool exact_sum_ok(uint32_t W, uint32_t H, uint32_t k);
 
+// Whether a run makes its k-NN ahead (RunCtx::knn_ahead): asked for, k > 0,
+// exact sums, and the lists of every item of the run, held at once, within
+// kKnnAheadMaxBytes (larger runs keep the per-step form's scratch).  run_plan
+// leaves out the coordinate tables of such runs, so it decides the same way.
+bool knn_ahead_fits(const RunCtx &c, uint32_t W, uint32_t H, uint32_t k) {
+  constexpr uint64_t kKnnAheadMaxBytes = 16ull << 30;
+  return c.want_knn_ahead && k > 0 && exact_sum_ok(W, H, k) &&
+         (uint64_t)c.items.size() * ((uint64_t)k * 4 + 16) <= kKnnAheadMaxBytes;
+}
+
 // Host schedule of Generator::resolve (ms.rs:702-1051) and the device
 // buffers of the run; nothing is enqueued yet.
 void run_plan(ts_session *s, RunCtx &c) {
@@ -1589,7 +1599,7 @@ void run_plan(ts_session *s, RunCtx &c) {
   // The coordinate tables below serve the f64 distances of inexact sessions
   // and of the fused small-step kernel; a run whose k-NN is made ahead
   // (exact sums) derives every distance from its offset and needs none.
-  const bool no_dist_tables = c.want_knn_ahead && k > 0 && exact_sum_ok(W, H, k);
+  const bool no_dist_tables = knn_ahead_fits(c, W, H, k);
   c.xdiv.resize(no_dist_tables ? 0 : W + 2 * (size_t)xo + 1);
   c.ydiv.resize(no_dist_tables ? 0 : H + 2 * (size_t)yo + 1);
   for (size_t i = 0; i < c.xdiv.size(); ++i) c.xdiv[i] = (double)((int64_t)i - xo) / (double)W;
@@ -1890,7 +1900,7 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   // stage with one k-NN form, each at least as large as the stage's items
   // before it, so that a chunk's k-NN overlaps the resolves of the ones
   // before)
-  c.knn_ahead = c.want_knn_ahead && k > 0 && exact_sum_ok(W, H, k);
+  c.knn_ahead = knn_ahead_fits(c, W, H, k);
   c.btab.clear();
   c.knn_chunks.clear();
   std::vector<std::pair<uint32_t, uint32_t>> chunk_batches;  // [first, last) batch of each chunk
