@@ -134,3 +134,23 @@ def test_resolve_forms(ts, oracle, wl, team, full):
     spec = wl.config2(out=64, ex=32)
     got, ref = run_both(ts, oracle, spec, team=team, full=full)
     assert_same(got, ref, "team %d full %d" % (team, full))
+
+
+@pytest.mark.parametrize("case", ["guided_tiling", "inpaint_128", "k8_m20_128", "rect_256x64"])
+def test_larger_schedules(ts, oracle, wl, case):
+    """More batches and chunks per stage than the small twins above."""
+    if case == "guided_tiling":
+        spec = wl.config2(out=64, ex=48)
+        spec["params"]["tiling_mode"] = True
+    elif case == "inpaint_128":
+        spec = wl.inpaint_session(91, side=128)
+    elif case == "k8_m20_128":
+        spec = wl.config1(out=128, ex=48)
+        spec["params"]["nearest_neighbors"] = 8
+        spec["params"]["random_sample_locations"] = 20
+    else:
+        spec = wl.config0(out=64, ex=40)
+        spec["out_w"], spec["out_h"] = 256, 64
+    got, ref = run_both(ts, oracle, spec)
+    assert_same(got, ref, case)
+    assert ahead(got)

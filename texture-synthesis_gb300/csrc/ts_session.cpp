@@ -447,9 +447,11 @@ Image device_guide_map(const Image &img, const Image &target, cudaStream_t st) {
 }
 
 // load_image (utils.rs:55-80): resize with CatmullRom when a size is given
-// and differs.  Runs on the device; returns the host image.
-Image load_image(const Image &in, bool has_size, uint32_t w, uint32_t h, cudaStream_t st) {
-  if (!has_size || (in.w == w && in.h == h)) return in;
+// and differs.  Runs on the device; returns the host image.  This form
+// takes over an input nothing reads afterwards (a consumed builder's): an
+// image already at its size is moved, not copied.
+Image load_image(Image &&in, bool has_size, uint32_t w, uint32_t h, cudaStream_t st) {
+  if (!has_size || (in.w == w && in.h == h)) return std::move(in);
   DevBuf<uint8_t> a, b;
   CUDA_TRY(a.alloc_on(in.px.size(), st));
   CUDA_TRY(b.alloc_on((size_t)w * h * 4, st));
@@ -462,6 +464,12 @@ Image load_image(const Image &in, bool has_size, uint32_t w, uint32_t h, cudaStr
   CUDA_TRY(cudaMemcpyAsync(out.px.data(), b.p, out.px.size(), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
   return out;
+}
+
+// The same for an input that stays with its owner.
+Image load_image(const Image &in, bool has_size, uint32_t w, uint32_t h, cudaStream_t st) {
+  if (!has_size || (in.w == w && in.h == h)) return in;
+  return load_image(Image(in), has_size, w, h, st);
 }
 
 
@@ -1032,19 +1040,23 @@ extern "C" int ts_builder_build(ts_builder *b, ts_session **out) {
     // the target guide at the output size (session.rs:258-266), then the
     // inputs at their final sizes (Example::resolve, lib.rs:564-603);
     // examples without a guide get the automatic one (lib.rs:575-582)
+    // (the builder is consumed: its images are taken over, except an
+    // inpainting example whose channel the mask is made from below)
     Image tg;
-    if (s->guided) tg = load_image(b->target, true, W, H, st);
+    if (s->guided) tg = load_image(std::move(b->target), true, W, H, st);
     std::vector<Image> imgs(s->n_ex), guides(s->n_ex), masks(s->n_ex);
     for (uint32_t e = 0; e < s->n_ex; ++e) {
-      const ExampleIn &ex = b->examples[e];
-      imgs[e] = load_image(ex.img, has_in, in_w, in_h, st);
+      ExampleIn &ex = b->examples[e];
+      const bool reread = b->has_inpaint && b->inpaint.channel && e == b->inpaint.example_index;
+      imgs[e] = reread ? load_image(ex.img, has_in, in_w, in_h, st) : load_image(std::move(ex.img), has_in, in_w, in_h, st);
       if (imgs[e].w > kMaxSide || imgs[e].h > kMaxSide) throw Failure{TS_ERR_LIMIT, "example side exceeds limit"};
       if (s->guided) {
-        guides[e] = ex.has_guide ? load_image(ex.guide, has_in, in_w, in_h, st) : device_guide_map(imgs[e], tg, st);
+        guides[e] = ex.has_guide ? load_image(std::move(ex.guide), has_in, in_w, in_h, st)
+                                 : device_guide_map(imgs[e], tg, st);
         if (guides[e].w > kMaxSide || guides[e].h > kMaxSide) throw Failure{TS_ERR_LIMIT, "guide side exceeds limit"};
       }
       if (ex.method == TS_SAMPLE_IMAGE) {
-        masks[e] = load_image(ex.mask, has_in, in_w, in_h, st);
+        masks[e] = load_image(std::move(ex.mask), has_in, in_w, in_h, st);
         if (masks[e].w != imgs[e].w || masks[e].h != imgs[e].h)
           throw Failure{TS_ERR_SIZE_MISMATCH, "sample mask size differs from its example"};
       }
