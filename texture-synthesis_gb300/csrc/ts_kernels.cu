@@ -1462,7 +1462,16 @@ __device__ __forceinline__ void resolve_body(const SessionDev &s, const StageDev
   const WarpSmem w = carve(smem + 2048 + (size_t)warp * warp_smem_bytes(s.k, s.m), s.k, s.m);
   __syncthreads();
   const uint32_t nb = b.i1 - b.i0;
-  for (uint32_t local = vb * kResolveWarps + warp; local < nb; local += vg * kResolveWarps) {
+  const uint32_t grid_warps = vg * kResolveWarps;
+  // the next item of this warp: the grid stride, or (BatchDev::work_ctr)
+  // the next one nobody has taken once every warp has had its first
+  auto next_item = [&](uint32_t cur) -> uint32_t {
+    if (!b.work_ctr) return cur + grid_warps;
+    uint32_t v = 0;
+    if (lane == 0) v = atomicAdd(b.work_ctr, 1u) + grid_warps;
+    return __shfl_sync(0xffffffffu, v, 0);
+  };
+  for (uint32_t local = vb * kResolveWarps + warp; local < nb; local = next_item(local)) {
     const uint32_t item = b.i0 + local;
     const uint32_t pixel = st.items[item];
     const int px = (int)(pixel % s.W), py = (int)(pixel / s.W);
@@ -2880,12 +2889,37 @@ void launch_mean(const SessionDev &s, const StageDev &st, const BatchDev &b, cud
   launch_pdl(k_mean_staged, cdiv(n, kMeanThreads), kMeanThreads, (size_t)s.k * kMeanThreads * 8, stream, s, st, b);
 }
 
+// Resident blocks of a kernel on the current device (cached per kernel and
+// dynamic shared-memory size).
+template <typename K>
+static uint32_t resident_blocks(K *kernel, int threads, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::pair<const void *, size_t>, uint32_t> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find({(const void *)kernel, smem});
+  if (it != cache.end()) return it->second;
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm <= 0)
+    return 0;  // unknown: the caller keeps a full grid
+  const uint32_t n = (uint32_t)sms * (uint32_t)per_sm;
+  cache[{(const void *)kernel, smem}] = n;
+  return n;
+}
+
 void launch_resolve(const SessionDev &s, const StageDev &st, const BatchDev &b, cudaStream_t stream,
                     const PendingCommit &pc) {
   const uint32_t n = b.i1 - b.i0;
   if (n == 0 && pc.n == 0) return;
   const size_t smem = resolve_smem_bytes(s.k, s.m, s.guided);
-  const uint32_t grid = std::max(cdiv(n, kResolveWarps), cdiv(pc.n, kResolveWarps * kWarp));
+  uint32_t grid = cdiv(n, kResolveWarps);
+  if (b.work_ctr) {
+    // a resident grid whose warps take further items from the counter
+    const uint32_t cap = s.guided ? resident_blocks(k_resolve, kResolveWarps * kWarp, smem)
+                                  : resident_blocks(k_resolve_lean, kResolveWarps * kWarp, smem);
+    if (cap) grid = std::min(grid, cap);
+  }
+  grid = std::max(grid, cdiv(pc.n, kResolveWarps * kWarp));
   if (s.guided)
     launch_pdl(k_resolve, grid, kResolveWarps * kWarp, smem, stream, s, st, b, pc);
   else

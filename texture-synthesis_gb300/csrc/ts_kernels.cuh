@@ -163,6 +163,10 @@ struct BatchDev {
   // tag) commits them while it runs (PendingCommit) and reads a tagged
   // pixel's batch-start colour and state from the shadow instead of the image
   uint32_t defer_tag, prev_tag;
+  // warp resolve of the plain path: a counter (zeroed) from which the warps
+  // of a resident grid take items after their first, so that no warp waits
+  // for its block's slowest item; null: one item per warp of a full grid
+  uint32_t *work_ctr;
 };
 
 // One batch step of one session as the multi-session kernels read it.

@@ -1395,6 +1395,7 @@ struct RunCtx {
   PinnedBuf<uint8_t> ptab;
   DevBuf<uint32_t> d_color, d_occ, d_mir, d_res, d_items, d_ncnt, d_fbl, d_fbc, d_cells, d_init;
   DevBuf<uint32_t> d_rank, d_kncnt, d_kfbl, d_kfbc;  // knn_ahead
+  DevBuf<uint32_t> d_wctr;  // per batch: the warp resolve's item counter (BatchDev::work_ctr)
   DevBuf<int32_t> d_knbuf;
   DevBuf<double> d_kmean;
   DevBuf<uint2> d_btab;
@@ -1949,7 +1950,7 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   const size_t z_color = zl.add(N * 4), z_state = zl.add(N * sizeof(uint4)), z_rscore = zl.add(c.res_total * 4),
                z_fbc = zl.add(c.n_batches * 4), z_err = zl.add(sizeof(int)), z_evals = zl.add(8),
                z_rank = zl.add(c.knn_ahead ? N * 4 : 0), z_kfbc = zl.add(n_chunks * 4),
-               z_shadow = zl.add(c.knn_ahead ? 2 * N * sizeof(uint4) : 0);
+               z_shadow = zl.add(c.knn_ahead ? 2 * N * sizeof(uint4) : 0), z_wctr = zl.add(c.n_batches * 4);
   // uploaded tables
   c.tab_parts.clear();
   auto T = [&](const auto &v) {
@@ -1992,6 +1993,7 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
   c.d_btab.view(tb + t_btab, c.btab.size());
   c.d_rank.view(z + z_rank, c.knn_ahead ? N : 0);
   c.d_shadow.view(z + z_shadow, c.knn_ahead ? 2 * N : 0);
+  c.d_wctr.view(z + z_wctr, c.n_batches);
   c.d_kfbc.view(z + z_kfbc, n_chunks);
   c.d_knbuf.view(wk + w_knbuf, n_kitems * kk);
   c.d_kncnt.view(wk + w_kncnt, n_kitems);
@@ -2134,6 +2136,7 @@ void run_alloc(RunCtx &c, cudaStream_t pool) {
         bd.res = c.d_result.p;
         stp.n = bp.i1 - bp.i0;
         stp.stage_i0 = bp.i0;
+        if (c.want_knn_ahead) bd.work_ctr = c.d_wctr.p + bidx;  // plain runs (ts_session_run) only
         stp.bidx = bidx++;
         if (c.knn_ahead) {  // the chunk's lists, made ahead on the k-NN stream
           const size_t g0 = (size_t)sp.items_off + bp.i0;
