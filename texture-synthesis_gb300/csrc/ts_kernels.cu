@@ -2753,6 +2753,8 @@ cudaError_t configure_kernels(uint32_t k, uint32_t m) {
   if (fsm <= kTeamFullMaxSmem) {
     e = raise_smem(k_resolve_team<kTeamFullThreads, true>, fsm);
     if (e != cudaSuccess) return e;
+    e = raise_smem(k_resolve_team<kStepWideThreads, true>, fsm);
+    if (e != cudaSuccess) return e;
     e = raise_smem(k_step_team_full<kTeamFullThreads>, std::max<size_t>(fsm, (size_t)kExhAllKeys * 8));
     if (e != cudaSuccess) return e;
     return raise_smem(k_step_team_full<kStepWideThreads>, std::max<size_t>(fsm, (size_t)kExhAllKeys * 8));
@@ -2932,7 +2934,11 @@ void launch_resolve_team(const SessionDev &s, const StageDev &st, const BatchDev
   if (n == 0 && pc.n == 0) return;
   uint32_t grid = n < 152u * 16u ? n : 152u * 16u;
   grid = std::max(grid, std::min(152u * 16u, cdiv(pc.n, kTeamThreads)));
-  if (full && team_full_smem_bytes(s.k, s.m) <= kTeamFullMaxSmem)
+  if (full && team_full_smem_bytes(s.k, s.m) <= kTeamFullMaxSmem && n <= 152u && pc.n == 0)
+    // at most one item per SM of a GB300: twice the threads per item
+    launch_pdl(k_resolve_team<kStepWideThreads, true>, grid, kStepWideThreads, team_full_smem_bytes(s.k, s.m), stream,
+               s, st, b, pc);
+  else if (full && team_full_smem_bytes(s.k, s.m) <= kTeamFullMaxSmem)
     launch_pdl(k_resolve_team<kTeamFullThreads, true>, grid, kTeamFullThreads, team_full_smem_bytes(s.k, s.m), stream, s,
                st, b, pc);
   else
