@@ -69,7 +69,7 @@ RESOLVE_DRAM_BYTES_PER_LAUNCH = 993.2e6 / 131
 # workload against ts_measure_gather_peak's patch kernel on this workload's
 # table (profiles/k_resolve_lean_multi_example_512.md and
 # profiles/gather_peak_probe_multi_example_512.md, ncu, one launch each).
-LOAD_PATH_SECTORS_PER_S = {"k_resolve_lean": 133.9e9, "gather_probe": 405.4e9}
+LOAD_PATH_SECTORS_PER_S = {"k_resolve_lean": 137.0e9, "gather_probe": 405.4e9}
 
 
 def _peaks():
