@@ -583,14 +583,17 @@ def main():
         "parity": "not checked (CPU baseline skipped)",
     }
     if not args.no_extra:
-        # configs 0 and 2 (single-example 256^2 and guided 512^2) with the
-        # default launch shapes; parity tests cover them at full size
+        # configs 0 and 2 (single-example 256^2 and guided 512^2), their
+        # launch shapes tuned on each the same way; parity tests cover them
+        # at full size
         for key, sp in (("config0", wl.config0()), ("config2", wl.config2())):
+            tun = ts.autotune_session(lambda sp=sp: ts.builder_from_spec(sp), repeats=3)
             with ClockSampler(0) as c2:
-                r = measure_workload(ts, sp, max(3, args.steps // 2), args.warmup, None, flush)
+                r = measure_workload(ts, sp, max(3, args.steps // 2), args.warmup, tun, flush)
             r.pop("outputs")
             r["clocks"] = c2.summary()
             r["config"] = bench_config(sp)
+            r["tuning"] = _tuning_dict(tun)
             line[key] = r
             _progress("%s measured" % key)
         line["batched"], btun = measure_batched(ts, wl)
