@@ -382,7 +382,7 @@ def gather_roofline(ts, spec, prof, peak_cache={}):
     """Roofline of the resolve family against the measured gather ceiling
     (ts_measure_gather_peak on a table the size of this workload's example
     level), with the HBM copy bandwidth beside it."""
-    kern = prof["kernels"]
+    kern = {n: v for n, v in prof["kernels"].items() if n != "knn_wait"}  # kernels only
     res = kern["resolve"]
     k = spec["params"]["nearest_neighbors"]
     guided = spec.get("target_guide") is not None
@@ -465,13 +465,22 @@ def measure_workload(ts, spec, steps, warmup, tuning, flush):
                                             "readback_ms", "gpu_ms")}})
     e2e = px / (sum(e2e_t) / len(e2e_t)) / 1e6
     breakdown = {k: sum(p[k] for p in parts) / len(parts) for k in parts[0]}
-    prof = ts.builder_from_spec(spec, profile=True, tuning=tuning).build().run().stats()
+    pg = ts.builder_from_spec(spec, profile=True, tuning=tuning).build().run()
+    prof = pg.stats()
+    waits = [r for r in pg.launches() if r["kernel"] == "knn_wait"]
+    by_stage = {}
+    for r in waits:
+        by_stage[str(r["stage"])] = by_stage.get(str(r["stage"]), 0.0) + r["ms"]
     return {"value": value, "unit": "Mpx/s", "steps": len(gpu_ms), "ms_per_step": sum(gpu_ms) / len(gpu_ms),
             "cost_evals_per_s": sum(evals) / (sum(gpu_ms) / 1e3), "gpu_launches": int(sum(launches) / len(launches)),
             "wall_ms_per_step": sum(walls) / len(walls) * 1e3,
             "e2e": {"value": e2e, "unit": "Mpx/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "breakdown_ms": breakdown},
-            "roofline": gather_roofline(ts, spec, prof), "outputs": outputs}
+            "roofline": gather_roofline(ts, spec, prof),
+            "knn_ahead_waits": {"waits": len(waits), "ms": sum(r["ms"] for r in waits), "ms_by_stage": by_stage,
+                                "source": "profiled run (CUDA events around every launch): the main stream's "
+                                          "stalls on chunks of neighbour lists made ahead, per backtrack stage"},
+            "outputs": outputs}
 
 
 def run_reference_arm(args):
@@ -578,6 +587,7 @@ def main():
         "clocks": clk.summary(),
         "e2e": m["e2e"],
         "roofline": m["roofline"],
+        "knn_ahead_waits": m["knn_ahead_waits"],
         "tuning": _tuning_dict(tuning),
         "cpu_baseline": None,
         "parity": "not checked (CPU baseline skipped)",

@@ -130,7 +130,11 @@ enum {
   TS_KERNEL_COMMIT = 4,
   TS_KERNEL_LEVEL_SWITCH = 5,
   TS_KERNEL_MEAN = 6,
-  TS_KERNEL_KINDS = 7
+  /* Not a kernel: the main stream waiting for a chunk of neighbour lists
+   * made ahead on the k-NN stream (plain path, power-of-two outputs);
+   * its time is the main stream's stall. */
+  TS_KERNEL_KNN_WAIT = 7,
+  TS_KERNEL_KINDS = 8
 };
 
 /* Run statistics of a generated image. */

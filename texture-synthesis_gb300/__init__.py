@@ -70,7 +70,8 @@ class _Progress(C.Structure):
 
 BATCH_PHASES = ("level_switch", "random_candidates", "knn_walk", "knn_exhaustive", "mean", "resolve",
                 "resolve_team", "resolve_team_full", "commit")
-KERNEL_KINDS = ("random_candidates", "knn_walk", "knn_exhaustive", "resolve", "commit", "level_switch", "mean")
+KERNEL_KINDS = ("random_candidates", "knn_walk", "knn_exhaustive", "resolve", "commit", "level_switch", "mean",
+                "knn_wait")
 
 
 class RunStats(C.Structure):

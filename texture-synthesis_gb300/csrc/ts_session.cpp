@@ -2302,7 +2302,12 @@ void enqueue_step_ahead(RunCtx &c, size_t t, cudaStream_t st, LaunchTimer &lt) {
   const SessionDev &sd = c.sd;
   const Step &stp = c.steps[t];
   if (c.pend && (stp.ls || !stp.batch || stp.stage != c.pend_stage)) commit_pending(c, st, lt);
-  if (stp.knn_wait >= 0) CUDA_TRY(cudaStreamWaitEvent(st, c.knn_ev[stp.knn_wait].e, 0));
+  if (stp.knn_wait >= 0) {
+    const uint32_t items = lt.items;
+    lt.items = stp.n;
+    lt.run(TS_KERNEL_KNN_WAIT, [&] { CUDA_TRY(cudaStreamWaitEvent(st, c.knn_ev[stp.knn_wait].e, 0)); });
+    lt.items = items;
+  }
   if (stp.ls) {
     lt.run(TS_KERNEL_LEVEL_SWITCH, [&] { launch_level_switch(sd, stp.ls_level, stp.ls_n_res, st); });
     ++c.launches;
