@@ -31,6 +31,18 @@ def test_every_declared_symbol_is_exported(ts):
     assert not unbound, unbound
 
 
+def test_kernel_kinds_match_the_header(ts):
+    """The Python names of the run statistics' record kinds follow the
+    header's TS_KERNEL_* values, and fit the stats arrays."""
+    src = open(HEADER).read()
+    kinds = dict((n, int(v)) for n, v in re.findall(r"\bTS_KERNEL_([A-Z_]+)\s*=\s*(\d+)", src))
+    count = kinds.pop("KINDS")
+    assert count == len(ts.KERNEL_KINDS) == len(kinds)
+    assert count <= len(ts.RunStats().kernel_ms)
+    for name, value in kinds.items():
+        assert ts.KERNEL_KINDS[value] == name.lower(), name
+
+
 def test_status_strings(ts):
     assert ts.lib().ts_status_str(0) == b"ok"
     assert ts.lib().ts_status_str(1) == b"invalid range"
